@@ -1,0 +1,892 @@
+/*
+ * TEST INFRASTRUCTURE ONLY -- the oracle.  CPU restatement of OpenRBC's
+ * per-timestep path, used by tests/, __graft_entry__.smoke() and bench.py's
+ * CPU baseline to check / time the GPU library.  The shipped package never
+ * links or loads this file.
+ *
+ * Every routine cites the reference file:line it restates.  Arithmetic is the
+ * reference's (same formulas, same operation order) in FP64 (R = double), or
+ * in FP32 (R = float, the reference default, src/config_static.h:34).
+ *
+ * Deliberate differences from the reference, each stated where it happens:
+ *  - pairs come from an exact cell list (every pair inside the cutoff), not the
+ *    heuristic Voronoi stencil of src/compute_pairwise_fused.h:260-315;
+ *  - each ordered pair is evaluated from its first particle's side
+ *    (full list, Newton off), so no atomics are needed;
+ *  - Langevin noise comes from Philox4x32-10 keyed by (seed, step, tag, system)
+ *    instead of per-thread xorshift128 (src/integrate_langevin.h:116-136);
+ *  - KE sums use fixed 4096-particle chunks so results do not depend on the
+ *    thread count.
+ */
+#include "orbc_oracle.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+/* ------------------------------------------------------------------ */
+/* Force field (src/forcefield_canonical.h:23-156), computed in R the  */
+/* way the reference's constexpr helpers compute it.                    */
+/* ------------------------------------------------------------------ */
+constexpr int NT = 6;
+
+template<class R> R POWr(R b, int e) {  // forcefield_canonical.h:24
+    R p = 1;
+    for (int k = 0; k < e; ++k) p = b * p;
+    return p;
+}
+template<class R> R rep_of(R cut, R req, R eps) { return eps / POWr<R>(R(cut - req), 8); }   // :27
+template<class R> R att_of(R cut, R req, R eps) {                                          // :28
+    return R(-2.0 * double(eps) / double(POWr<R>(R(cut - req), 4)));
+}
+
+template<class R> struct FF {
+    R mass[NT], radius[NT];
+    R cutlp[NT], cutsqlp[NT], replp[NT], attlp[NT], alphalp[NT];
+    R cutpp[NT * NT], cutsqpp[NT * NT], reppp[NT * NT];
+    R lj_cutsq[NT * NT], lj1[NT * NT], lj2[NT * NT];
+    double cut_pair[NT * NT];  // largest interaction range of a type pair
+    FF() {
+        const double m[NT] = {1, 4, 4, 1, 10, 10};                       // :40
+        const double rad[NT] = {0.56125, 1.12375, 1.12375, 0.56125, 1.5, 0.5};  // :41
+        const double cl[NT] = {2.6, 2.6, 2.6, 2.6, 0, 0};                // :52
+        const double rl[NT] = {1.1225, 1.685, 1.685, 1.1225, 0, 0};     // :53
+        const double el[NT] = {1.2, 1.4, 2.8, 2.8, 0, 0};                // :54
+        const double al[NT] = {1.55, 5, 5, 5, 0, 0};                     // :55
+        // protein-protein poly tables, rows/cols 0..3 (:57-73); zero elsewhere
+        const double cp4[4][4] = {{2.6, 2.6, 2.6, 2.6}, {2.6, 2.6, 2.6, 2.6}, {2.6, 2.6, 2.6, 2.6}, {2.6, 2.6, 2.6, 2.6}};
+        const double rp4[4][4] = {{1.1225, 1.685, 1.685, 1.1225}, {1.685, 2.245, 2.245, 1.685},
+                                  {1.685, 2.245, 2.245, 1.685}, {1.1225, 1.685, 1.685, 1.1225}};
+        const double ep4[4][4] = {{1.2, 1.4, 2.8, 2.8}, {1.4, 1, 1, 1}, {2.8, 1, 1, 1}, {2.8, 1, 1, 1}};
+        // LJ tables (:76-99)
+        const double lje[NT * NT] = {0, 0, 0, 0, 1, 1, 0, 0, 0, 0, 1, 1, 0, 0, 0, 0, 1, 1,
+                                     0, 0, 0, 0, 0, 0, 1, 1, 1, 0, 0, 0, 1, 1, 1, 0, 0, 0};
+        const double ljs[NT * NT] = {0, 0, 0, 0, 1, 1, 0, 0, 0, 0, 3.4, 3.4, 0, 0, 0, 0, 3.4, 1,
+                                     0, 0, 0, 0, 0, 0, 1, 3.4, 3.4, 0, 3, 1.8, 1, 3.4, 1, 0, 1.8, 1};
+        const double a = 3.4 * 1.1225;
+        const double ljc[NT * NT] = {0, 0, 0, 0, 1.1225, 1.1225, 0, 0, 0, 0, a, a, 0, 0, 0, 0, a, 1.1225,
+                                     0, 0, 0, 0, 0, 0, 1.1225, a, a, 0, 0, 0, 1.1225, a, 1.1225, 0, 0, 0};
+        for (int t = 0; t < NT; ++t) {
+            mass[t] = R(m[t]);
+            radius[t] = R(rad[t]);
+            cutlp[t] = R(cl[t]);
+            alphalp[t] = R(al[t]);
+            cutsqlp[t] = cutlp[t] * cutlp[t];  // cutsq() :25
+            if (t < 4) {
+                replp[t] = rep_of<R>(R(cl[t]), R(rl[t]), R(el[t]));
+                attlp[t] = att_of<R>(R(cl[t]), R(rl[t]), R(el[t]));
+            } else {
+                replp[t] = 0;
+                attlp[t] = 0;
+            }
+        }
+        for (int k = 0; k < NT * NT; ++k) {
+            int r = k / NT, c = k % NT;
+            if (r < 4 && c < 4) {
+                cutpp[k] = R(cp4[r][c]);
+                cutsqpp[k] = cutpp[k] * cutpp[k];
+                reppp[k] = rep_of<R>(R(cp4[r][c]), R(rp4[r][c]), R(ep4[r][c]));
+            } else {
+                cutpp[k] = cutsqpp[k] = reppp[k] = 0;
+            }
+            const R ljcut = R(ljc[k]);
+            lj_cutsq[k] = ljcut * ljcut;                               // init() :144-148
+            lj1[k] = R(48.0 * double(R(lje[k])) * std::pow(double(R(ljs[k])), 12));
+            lj2[k] = R(24.0 * double(R(lje[k])) * std::pow(double(R(ljs[k])), 6));
+        }
+        for (int ti = 0; ti < NT; ++ti)
+            for (int tj = 0; tj < NT; ++tj) {
+                double c2 = 0;
+                if (ti == 0 || tj == 0) {
+                    int p = std::max(ti, tj);
+                    c2 = std::max(double(cutsqlp[p]), double(lj_cutsq[p]));
+                } else {
+                    int k = ti + NT * tj;
+                    c2 = std::max(double(cutsqpp[k]), double(lj_cutsq[k]));
+                }
+                cut_pair[ti * NT + tj] = std::sqrt(c2);
+            }
+    }
+};
+
+template<class R> const FF<R> &ff() {
+    static const FF<R> f;
+    return f;
+}
+
+template<class R> struct V3 {
+    R x[3];
+};
+template<class R> inline R dot3(const R *a, const R *b) {  // math_vector_base.h:190-194
+    R s = 0;
+    for (int i = 0; i < 3; ++i) s += a[i] * b[i];
+    return s;
+}
+template<class R> inline void cross3(const R *u, const R *v, R *w) {  // math_vector_base.h:226-233
+    for (int i = 0; i < 3; ++i) w[i] = u[(i + 1) % 3] * v[(i + 2) % 3] - u[(i + 2) % 3] * v[(i + 1) % 3];
+}
+
+/* ------------------------------------------------------------------ */
+/* Pair interactions, evaluated from particle i's side.                */
+/* ------------------------------------------------------------------ */
+
+/* Anisotropic poly 4-8 pair: src/pairwise_kernel.h:30-68 (lipid-lipid) and
+ * src/pairwise_kernel_fused.h:22-61 (protein-lipid), same formula with the
+ * lipid-protein table row of the protein type.  Adds force/torque on i. */
+template<class R>
+inline void aniso(const R *dx, R r_sq, const R *mu1, const R *mu2, R cut, R rep, R att, R alpha, R *f,
+                  R *t, double *e) {
+    const R r = std::sqrt(r_sq);
+    const R rinv = R(1) / r;
+    R u[3];
+    for (int k = 0; k < 3; ++k) u[k] = dx[k] * rinv;
+    const R ninj = dot3(mu1, mu2);
+    const R niu = dot3(mu1, u);
+    const R nju = dot3(mu2, u);
+    const R a = ninj - niu * nju;
+    const R A = R(1.0) + alpha * (a - R(1.0));
+    const R rc = cut - r;
+    const R rc3 = rc * rc * rc;
+    const R rc4 = rc * rc3;
+    const R rc7 = rc3 * rc4;
+    R pni[3], pnj[3];
+    for (int k = 0; k < 3; ++k) {
+        pni[k] = mu1[k] - niu * u[k];
+        pnj[k] = mu2[k] - nju * u[k];
+    }
+    const R ua = att * rc4;
+    const R alphaua = alpha * ua;
+    const R alphauar = alphaua / r;
+    const R fra = R(8.0) * rep * rc7 + A * R(4.0) * att * rc3;
+    for (int k = 0; k < 3; ++k) {
+        f[k] += fra * u[k] + (nju * pni[k] + niu * pnj[k]) * alphauar;
+        t[k] -= alphaua * pnj[k];
+    }
+    if (e) *e += 0.5 * (double(rep) * double(rc4) * double(rc4) + double(A) * double(att) * double(rc4));
+}
+
+/* Lennard-Jones (WCA cut): src/pairwise_kernel_fused.h:63-77. */
+template<class R> inline void lj(const R *dx, R rsq, R lj1, R lj2, R *f, double *e) {
+    const R r2inv = R(1) / rsq;
+    const R r6inv = r2inv * r2inv * r2inv;
+    const R forcelj = r6inv * (lj1 * r6inv - lj2);
+    const R fpair = forcelj * r2inv;
+    for (int k = 0; k < 3; ++k) f[k] += dx[k] * fpair;
+    if (e) *e += 0.5 * (double(r6inv) * (double(lj1) / 12.0 * double(r6inv) - double(lj2) / 6.0));
+}
+
+/* Protein-protein repulsion: src/pairwise_kernel_fused.h:79-97. */
+template<class R> inline void prep(const R *dx, R r_sq, R cut, R rep, R *f, double *e) {
+    const R r = std::sqrt(r_sq);
+    R u[3];
+    for (int k = 0; k < 3; ++k) u[k] = dx[k] / r;
+    const R rc = cut - r;
+    const R rc3 = rc * rc * rc;
+    const R rc4 = rc * rc3;
+    const R rc7 = rc3 * rc4;
+    const R fr = R(8.0) * rep * rc7;
+    for (int k = 0; k < 3; ++k) f[k] += fr * u[k];
+    if (e) *e += 0.5 * double(rep) * double(rc4) * double(rc4);
+}
+
+/* Dispatch of src/compute_pairwise_fused.h:91-236: lipid-lipid
+ * (:109,134), protein-lipid then LJ fallback with the protein type as the
+ * table index (:168-171), protein-protein with type12 = t1 + 6 t2 (:199-203,
+ * :226-230).  Returns 1 if the pair interacted. */
+template<class R>
+inline int pair_force(int ti, int tj, const R *dx, R r_sq, const R *mui, const R *muj, R *f, R *t, double *e) {
+    const FF<R> &F = ff<R>();
+    if (!(r_sq > R(1e-5))) return 0;
+    if (ti == 0 || tj == 0) {
+        const int p = ti > tj ? ti : tj;
+        if (r_sq < F.cutsqlp[p]) {
+            aniso<R>(dx, r_sq, mui, muj, F.cutlp[p], F.replp[p], F.attlp[p], F.alphalp[p], f, t, e);
+            return 1;
+        } else if (r_sq < F.lj_cutsq[p]) {
+            lj<R>(dx, r_sq, F.lj1[p], F.lj2[p], f, e);
+            return 1;
+        }
+        return 0;
+    }
+    const int k = ti + NT * tj;
+    if (r_sq < F.cutsqpp[k]) {
+        prep<R>(dx, r_sq, F.cutpp[k], F.reppp[k], f, e);
+        return 1;
+    } else if (r_sq < F.lj_cutsq[k]) {
+        lj<R>(dx, r_sq, F.lj1[k], F.lj2[k], f, e);
+        return 1;
+    }
+    return 0;
+}
+
+/* ------------------------------------------------------------------ */
+/* Geometry helpers                                                    */
+/* ------------------------------------------------------------------ */
+struct Box {
+    double lo[3], L[3];
+    int per[3];
+};
+inline Box box_of(const orc_system *s) {
+    Box b;
+    for (int d = 0; d < 3; ++d) {
+        b.lo[d] = s->lo[d];
+        b.L[d] = s->hi[d] - s->lo[d];
+        b.per[d] = s->periodic[d];
+    }
+    return b;
+}
+inline double min_image(double d, double L, int per) {
+    if (!per) return d;
+    return d - L * std::nearbyint(d / L);
+}
+
+/* Uniform cell list over the particles (periodic dims wrap, open dims span the
+ * bounding box).  Used only to enumerate candidate pairs exactly. */
+struct CellList {
+    int nc[3];
+    double lo[3], w[3];
+    int per[3];
+    bool brute = false;
+    std::vector<int> start, idx;
+    void build(const double *x, int64_t n, const Box &b, double cmax) {
+        double lo_[3], hi_[3];
+        for (int d = 0; d < 3; ++d) {
+            per[d] = b.per[d];
+            if (per[d]) {
+                lo_[d] = b.lo[d];
+                hi_[d] = b.lo[d] + b.L[d];
+            } else {
+                lo_[d] = 1e300;
+                hi_[d] = -1e300;
+                for (int64_t i = 0; i < n; ++i) {
+                    lo_[d] = std::min(lo_[d], x[3 * i + d]);
+                    hi_[d] = std::max(hi_[d], x[3 * i + d]);
+                }
+                if (n == 0) lo_[d] = hi_[d] = 0;
+                lo_[d] -= 1e-3;
+                hi_[d] += 1e-3;
+            }
+            double L = hi_[d] - lo_[d];
+            nc[d] = std::max(1, int(std::floor(L / cmax)));
+            if (per[d] && nc[d] < 3) brute = true;
+            if (nc[d] > 4096) nc[d] = 4096;
+            lo[d] = lo_[d];
+            w[d] = L / nc[d];
+        }
+        const int64_t ncell = int64_t(nc[0]) * nc[1] * nc[2];
+        if (ncell > (int64_t(1) << 28)) brute = true;
+        if (brute) return;
+        std::vector<int> cid(n);
+        start.assign(ncell + 1, 0);
+        for (int64_t i = 0; i < n; ++i) {
+            int64_t c = cell_of(&x[3 * i]);
+            cid[i] = int(c);
+            start[c + 1]++;
+        }
+        for (int64_t c = 0; c < ncell; ++c) start[c + 1] += start[c];
+        idx.resize(n);
+        std::vector<int> fill(start.begin(), start.end() - 1);
+        for (int64_t i = 0; i < n; ++i) idx[fill[cid[i]]++] = int(i);
+    }
+    int coord(double v, int d) const {
+        double u = (v - lo[d]) / w[d];
+        int c = int(std::floor(u));
+        if (per[d]) {
+            c %= nc[d];
+            if (c < 0) c += nc[d];
+        } else {
+            c = std::min(std::max(c, 0), nc[d] - 1);
+        }
+        return c;
+    }
+    int64_t cell_of(const double *p) const {
+        return coord(p[0], 0) + int64_t(nc[0]) * (coord(p[1], 1) + int64_t(nc[1]) * coord(p[2], 2));
+    }
+    /* visit every j that may lie within cmax of particle i (j != i) */
+    template<class FN> void for_candidates(const double *x, int64_t n, int64_t i, FN &&fn) const {
+        if (brute) {
+            for (int64_t j = 0; j < n; ++j)
+                if (j != i) fn(j);
+            return;
+        }
+        int c[3];
+        for (int d = 0; d < 3; ++d) c[d] = coord(x[3 * i + d], d);
+        int lo3[3], hi3[3];
+        for (int d = 0; d < 3; ++d) {
+            if (per[d]) {
+                lo3[d] = -1;
+                hi3[d] = 1;
+            } else {
+                lo3[d] = c[d] > 0 ? -1 : 0;
+                hi3[d] = c[d] < nc[d] - 1 ? 1 : 0;
+            }
+        }
+        for (int dz = lo3[2]; dz <= hi3[2]; ++dz)
+            for (int dy = lo3[1]; dy <= hi3[1]; ++dy)
+                for (int dx = lo3[0]; dx <= hi3[0]; ++dx) {
+                    int cc[3] = {c[0] + dx, c[1] + dy, c[2] + dz};
+                    for (int d = 0; d < 3; ++d)
+                        if (per[d]) cc[d] = (cc[d] + nc[d]) % nc[d];
+                    int64_t cell = cc[0] + int64_t(nc[0]) * (cc[1] + int64_t(nc[1]) * cc[2]);
+                    for (int k = start[cell]; k < start[cell + 1]; ++k)
+                        if (idx[k] != i) fn(int64_t(idx[k]));
+                }
+    }
+};
+
+int g_threads = 0;
+
+/* Map from tag to array index (src/container.h:36-58). */
+struct TagMap {
+    std::vector<int> m;
+    void build(const int *tag, int64_t n) {
+        int mx = -1;
+        for (int64_t i = 0; i < n; ++i) mx = std::max(mx, tag[i]);
+        m.assign(size_t(mx + 1), -1);
+        for (int64_t i = 0; i < n; ++i) m[size_t(tag[i])] = int(i);
+    }
+    int operator[](int t) const { return (t >= 0 && size_t(t) < m.size()) ? m[size_t(t)] : -1; }
+};
+
+double present_cut_max(const orc_system *s) {
+    bool present[NT] = {false, false, false, false, false, false};
+    for (int64_t i = 0; i < s->n; ++i)
+        if (s->type[i] >= 0 && s->type[i] < NT) present[s->type[i]] = true;
+    const FF<double> &F = ff<double>();
+    double c = 0;
+    for (int a = 0; a < NT; ++a)
+        for (int b = 0; b < NT; ++b)
+            if (present[a] && present[b]) c = std::max(c, F.cut_pair[a * NT + b]);
+    return c > 0 ? c : 1.0;
+}
+
+/* Bond force on i with dx = x_j - x_i: F_i = kappa(r) dx; returns energy.
+ * HARMONIC: src/compute_bonded.h:109-115, kappa = K (1 - r0/r). */
+template<class R> inline R bond_kappa(int style, R K, R r0, R Rm, R r, double *en, int *flags) {
+    if (style == ORC_BOND_HARMONIC) {
+        const R rinv = R(1) / r;
+        if (en) *en = 0.5 * double(K) * (double(r) - double(r0)) * (double(r) - double(r0));
+        return K * (R(1) - r0 * rinv);
+    } else if (style == ORC_BOND_FENE) {
+        /* U = -K R^2/2 ln(1 - ((r - r0)/R)^2) */
+        R s = (r - r0) / Rm;
+        R s2 = s * s;
+        if (s2 >= R(0.99)) {
+            *flags |= 1;
+            s2 = R(0.99);
+        }
+        if (en) *en = -0.5 * double(K) * double(Rm) * double(Rm) * std::log(1.0 - double(s2));
+        return K * (r - r0) / (r * (R(1) - s2));
+    } else {
+        /* WLC + 1/r^2 repulsion, zero net force at r0:
+         * F(r) = K [1/(4(1-x)^2) - 1/4 + x] - F_wlc(r0) (r0/r)^2, x = r/lmax,
+         * lmax = Rm * r0.  Attractive for r > r0. */
+        const R lmax = Rm * r0;
+        R x = r / lmax;
+        if (x >= R(0.99)) {
+            *flags |= 1;
+            x = R(0.99);
+        }
+        const R x0 = r0 / lmax;
+        const R omx = R(1) - x, omx0 = R(1) - x0;
+        const R fw = K * (R(0.25) / (omx * omx) - R(0.25) + x);
+        const R fw0 = K * (R(0.25) / (omx0 * omx0) - R(0.25) + x0);
+        const R q = r0 / r;
+        const R fr = fw - fw0 * q * q;
+        if (en) {
+            double xd = double(x), ld = double(lmax);
+            double uw = double(K) * ld * (xd * xd / 2.0 + 0.25 / (1.0 - xd) - xd / 4.0 - 0.25);
+            double up = double(fw0) * double(r0) * double(r0) / double(r);
+            *en = uw + up;
+        }
+        return fr / r;
+    }
+}
+
+/* Forces at the current state: pair (cell list, full per-particle loop),
+ * bonds (src/compute_bonded.h:89-146), global area/volume constraint. */
+template<class R>
+int forces_impl(const orc_system *s, double *f3, double *t3, double *e, orc_thermo *th) {
+    const int64_t n = s->n;
+    const Box b = box_of(s);
+    CellList cl;
+    cl.build(s->x, n, b, present_cut_max(s) * (1 + 1e-12) + 1e-9);
+    std::vector<R> xr(3 * n), nr(3 * n);
+    for (int64_t k = 0; k < 3 * n; ++k) {
+        xr[k] = R(s->x[k]);
+        nr[k] = R(s->nrm[k]);
+    }
+    int64_t npairs = 0;
+    double epot = 0;
+    const int nthr = g_threads > 0 ? g_threads : 0;
+#pragma omp parallel for schedule(dynamic, 256) reduction(+ : npairs) num_threads(nthr > 0 ? nthr : omp_get_max_threads())
+    for (int64_t i = 0; i < n; ++i) {
+        R fi[3] = {0, 0, 0}, ti_[3] = {0, 0, 0};
+        double ei = 0;
+        const int typ_i = s->type[i];
+        cl.for_candidates(s->x, n, i, [&](int64_t j) {
+            R dx[3];
+            for (int d = 0; d < 3; ++d) {
+                if (b.per[d]) {
+                    double dd = min_image(s->x[3 * i + d] - s->x[3 * j + d], b.L[d], 1);
+                    dx[d] = R(dd);
+                } else {
+                    dx[d] = xr[3 * i + d] - xr[3 * j + d];
+                }
+            }
+            const R r_sq = dx[0] * dx[0] + dx[1] * dx[1] + dx[2] * dx[2];
+            int hit = pair_force<R>(typ_i, s->type[j], dx, r_sq, &nr[3 * i], &nr[3 * j], fi, ti_, e ? &ei : nullptr);
+            if (hit && j > i) npairs++;
+        });
+        for (int d = 0; d < 3; ++d) {
+            f3[3 * i + d] = double(fi[d]);
+            t3[3 * i + d] = double(ti_[d]);
+        }
+        if (e) e[i] = ei;
+    }
+    if (e)
+        for (int64_t i = 0; i < n; ++i) epot += e[i];
+
+    int flags = 0;
+    /* bonds */
+    if (s->nb > 0) {
+        TagMap tm;
+        tm.build(s->tag, n);
+        for (int64_t l = 0; l < s->nb; ++l) {
+            const int type = s->bonds[3 * l];
+            const int p1 = tm[s->bonds[3 * l + 1]];
+            const int p2 = tm[s->bonds[3 * l + 2]];
+            if (p1 < 0 || p2 < 0 || type < 0 || type >= ORC_MAX_BOND_TYPES) continue;
+            R dx[3];
+            for (int d = 0; d < 3; ++d) {
+                if (b.per[d])
+                    dx[d] = R(min_image(s->x[3 * p2 + d] - s->x[3 * p1 + d], b.L[d], 1));
+                else
+                    dx[d] = xr[3 * p2 + d] - xr[3 * p1 + d];
+            }
+            const R r = std::sqrt(dx[0] * dx[0] + dx[1] * dx[1] + dx[2] * dx[2]);
+            const R r0 = s->bond_r0 ? R(s->bond_r0[l]) : R(s->br0[type]);
+            double en = 0;
+            const R kap = bond_kappa<R>(s->bstyle[type], R(s->bK[type]), r0, R(s->bR[type]), r, &en, &flags);
+            for (int d = 0; d < 3; ++d) {
+                const R fo = kap * dx[d];
+                f3[3 * p1 + d] += double(fo);
+                f3[3 * p2 + d] -= double(fo);
+            }
+            if (e) {
+                e[p1] += 0.5 * en;
+                e[p2] += 0.5 * en;
+            }
+            epot += en;
+        }
+    }
+
+    /* area / volume constraint on the face mesh (FP64 always) */
+    double area = 0, volume = 0;
+    if (s->nface > 0) {
+        TagMap tm;
+        tm.build(s->tag, n);
+        const int ref = tm[s->faces[0]];
+        auto rel = [&](int p, double *out) {
+            for (int d = 0; d < 3; ++d) out[d] = min_image(s->x[3 * p + d] - s->x[3 * ref + d], b.L[d], b.per[d]);
+        };
+        for (int64_t k = 0; k < s->nface; ++k) {
+            int pa = tm[s->faces[3 * k]], pb = tm[s->faces[3 * k + 1]], pc = tm[s->faces[3 * k + 2]];
+            double A[3], B[3], C[3], e1[3], e2[3], N[3], bc[3];
+            rel(pa, A);
+            rel(pb, B);
+            rel(pc, C);
+            for (int d = 0; d < 3; ++d) {
+                e1[d] = B[d] - A[d];
+                e2[d] = C[d] - A[d];
+            }
+            cross3(e1, e2, N);
+            cross3(B, C, bc);
+            area += 0.5 * std::sqrt(dot3(N, N));
+            volume += dot3(A, bc) / 6.0;
+        }
+        const double cv = (s->kv != 0 && s->V0 != 0) ? -s->kv * (volume - s->V0) / s->V0 : 0.0;
+        const double ca = (s->ka != 0 && s->A0 != 0) ? -s->ka * (area - s->A0) / s->A0 : 0.0;
+        if (cv != 0 || ca != 0) {
+            for (int64_t k = 0; k < s->nface; ++k) {
+                int p[3] = {tm[s->faces[3 * k]], tm[s->faces[3 * k + 1]], tm[s->faces[3 * k + 2]]};
+                double P[3][3];
+                for (int q = 0; q < 3; ++q) rel(p[q], P[q]);
+                double e1[3], e2[3], N[3];
+                for (int d = 0; d < 3; ++d) {
+                    e1[d] = P[1][d] - P[0][d];
+                    e2[d] = P[2][d] - P[0][d];
+                }
+                cross3(e1, e2, N);
+                const double nn = std::sqrt(dot3(N, N));
+                double nh[3] = {N[0] / nn, N[1] / nn, N[2] / nn};
+                for (int q = 0; q < 3; ++q) {
+                    const double *a = P[q], *bb = P[(q + 1) % 3], *cc = P[(q + 2) % 3];
+                    double ba[3], ca_[3], gV[3], bmc[3], gA[3];
+                    for (int d = 0; d < 3; ++d) {
+                        ba[d] = bb[d] - a[d];
+                        ca_[d] = cc[d] - a[d];
+                        bmc[d] = bb[d] - cc[d];
+                    }
+                    cross3(ba, ca_, gV);  // 6 dV/da summed over the closed one-ring
+                    cross3(bmc, nh, gA);  // 2 dA/da
+                    for (int d = 0; d < 3; ++d) f3[3 * p[q] + d] += cv * gV[d] / 6.0 + ca * gA[d] * 0.5;
+                }
+            }
+        }
+    }
+    if (th) {
+        th->npairs = npairs;
+        th->epot = epot;
+        th->area = area;
+        th->volume = volume;
+        th->flags = flags;
+    }
+    return 0;
+}
+
+/* ------------------------------------------------------------------ */
+/* Counter-based noise: Philox4x32-10 (Salmon et al., SC'11).          */
+/* ------------------------------------------------------------------ */
+inline void philox(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) {
+    uint32_t c0 = ctr[0], c1 = ctr[1], c2 = ctr[2], c3 = ctr[3];
+    uint32_t k0 = key[0], k1 = key[1];
+    for (int r = 0; r < 10; ++r) {
+        const uint64_t p0 = uint64_t(0xD2511F53u) * c0;
+        const uint64_t p1 = uint64_t(0xCD9E8D57u) * c2;
+        const uint32_t hi0 = uint32_t(p0 >> 32), lo0 = uint32_t(p0);
+        const uint32_t hi1 = uint32_t(p1 >> 32), lo1 = uint32_t(p1);
+        c0 = hi1 ^ c1 ^ k0;
+        c1 = lo1;
+        c2 = hi0 ^ c3 ^ k1;
+        c3 = lo0;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+    out[0] = c0;
+    out[1] = c1;
+    out[2] = c2;
+    out[3] = c3;
+}
+inline void noise3(uint64_t seed, int64_t step, int tag, int sys, double r[3]) {
+    const uint32_t ctr[4] = {uint32_t(tag), uint32_t(uint64_t(step)), uint32_t(uint64_t(step) >> 32), uint32_t(sys)};
+    const uint32_t key[2] = {uint32_t(seed), uint32_t(seed >> 32)};
+    uint32_t o[4];
+    philox(ctr, key, o);
+    for (int k = 0; k < 3; ++k) r[k] = double(o[k] >> 8) * (1.0 / 8388608.0) - 1.0;
+}
+
+/* Deterministic chunked FP64 sum. */
+template<class FN> double chunked_sum(int64_t n, FN &&term) {
+    const int64_t CH = 4096;
+    const int64_t nch = (n + CH - 1) / CH;
+    std::vector<double> part(size_t(std::max<int64_t>(nch, 1)), 0.0);
+#pragma omp parallel for schedule(static)
+    for (int64_t c = 0; c < nch; ++c) {
+        double acc = 0;
+        for (int64_t i = c * CH; i < std::min(n, (c + 1) * CH); ++i) acc += term(i);
+        part[size_t(c)] = acc;
+    }
+    double s = 0;
+    for (int64_t c = 0; c < nch; ++c) s += part[size_t(c)];
+    return s;
+}
+
+/* src/integrate_langevin.h:105-146, per particle, in R. */
+template<class R> int langevin_impl(orc_system *s, int nsteps, orc_thermo *th) {
+    const int64_t n = s->n;
+    const FF<R> &F = ff<R>();
+    std::vector<double> f3(3 * n), t3(3 * n);
+    R gamma[NT], sigma[NT];
+    for (int i = 0; i < NT; ++i) {  // :110-114
+        gamma[i] = R(6.0 * M_PI * double(R(s->eta)) * double(F.radius[i]));
+        sigma[i] = R(double(std::sqrt(R(2 * R(s->kBT) * gamma[i]))) * std::sqrt(3.0 / s->dt));
+    }
+    const R dt = R(s->dt);
+    const R dt_over_m = dt / R(1);
+    for (int st = 0; st < nsteps; ++st) {
+        forces_impl<R>(s, f3.data(), t3.data(), nullptr, th);
+        const int64_t step = s->step;
+#pragma omp parallel for schedule(static)
+        for (int64_t i = 0; i < n; ++i) {
+            R x[3], nn[3], v[3], o[3], f[3], t[3], tmp[3];
+            for (int d = 0; d < 3; ++d) {
+                x[d] = R(s->x[3 * i + d]);
+                nn[d] = R(s->nrm[3 * i + d]);
+                v[d] = R(s->v[3 * i + d]);
+                o[d] = R(s->o[3 * i + d]);
+                f[d] = R(f3[3 * i + d]);
+                t[d] = R(t3[3 * i + d]);
+            }
+            // ROTATION (:124-128)
+            cross3(nn, t, tmp);
+            for (int d = 0; d < 3; ++d) t[d] = tmp[d];
+            for (int d = 0; d < 3; ++d) o[d] += dt_over_m * t[d];
+            cross3(o, nn, tmp);
+            R g[3];
+            for (int d = 0; d < 3; ++d) g[d] = nn[d] + tmp[d] * dt;
+            const R ginv = R(1) / std::sqrt(dot3(g, g));
+            for (int d = 0; d < 3; ++d) nn[d] = g[d] * ginv;
+            // TRANSLATION (:138-144)
+            double rr[3];
+            noise3(s->seed, step, s->tag[i], s->sys, rr);
+            const int ty = s->type[i];
+            for (int d = 0; d < 3; ++d) {
+                f[d] -= gamma[ty] * v[d] + sigma[ty] * R(rr[d]);
+                v[d] += f[d] * (dt / F.mass[ty]);
+                x[d] += v[d] * dt;
+            }
+            for (int d = 0; d < 3; ++d) {
+                s->x[3 * i + d] = double(x[d]);
+                s->nrm[3 * i + d] = double(nn[d]);
+                s->v[3 * i + d] = double(v[d]);
+                s->o[3 * i + d] = double(o[d]);
+                if (s->f) s->f[3 * i + d] = 0;
+                if (s->t) s->t[3 * i + d] = 0;
+            }
+        }
+        s->step++;
+    }
+    if (th) {
+        th->ke2 = chunked_sum(n, [&](int64_t i) {
+            const double *v = &s->v[3 * i];
+            return double(F.mass[s->type[i]]) * (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+        });
+        th->temperature = n ? th->ke2 / (3.0 * double(n)) : 0;
+    }
+    return 0;
+}
+
+/* post_toque_final_update (src/integrate_nh.h:237-273) + zeta update. */
+void nh_final(orc_system *s) {
+    const int64_t n = s->n;
+    const FF<double> &F = ff<double>();
+    const double dt = s->dt, zeta = s->zeta;
+    const double ke = chunked_sum(n, [&](int64_t i) {
+        double *t = &s->t[3 * i], *nn = &s->nrm[3 * i], *v = &s->v[3 * i], *o = &s->o[3 * i], *f = &s->f[3 * i];
+        double tmp[3];
+        cross3(nn, t, tmp);
+        for (int d = 0; d < 3; ++d) t[d] = tmp[d];
+        const double m = F.mass[s->type[i]];
+        for (int d = 0; d < 3; ++d) v[d] += 0.5 * dt * (f[d] / m - zeta * v[d]);
+        for (int d = 0; d < 3; ++d) o[d] += 0.5 * (dt / 1.0) * t[d];
+        return 0.5 * m * dot3(v, v);
+    });
+    if (s->Q == 0) s->Q = double(n) * 0.01;  // runtime_parameter.h:74-76
+    s->zeta += 0.5 * s->dt / s->Q * (ke - 0.5 * 3.0 * double(n) * s->kBT);  // :241-244
+}
+
+/* verlet_initial_bounce_clearforce_update (src/integrate_nh.h:178-235). */
+void nh_initial(orc_system *s) {
+    const int64_t n = s->n;
+    const FF<double> &F = ff<double>();
+    const double dt = s->dt;
+    const double gamma = 1.0 / (1.0 + 0.5 * dt * s->zeta);
+    const double ke = chunked_sum(n, [&](int64_t i) {
+        double *x = &s->x[3 * i], *v = &s->v[3 * i], *o = &s->o[3 * i], *nn = &s->nrm[3 * i];
+        double *f = &s->f[3 * i], *t = &s->t[3 * i];
+        const double m = F.mass[s->type[i]];
+        for (int d = 0; d < 3; ++d) v[d] = (v[d] + 0.5 / m * dt * f[d]) * gamma;
+        for (int d = 0; d < 3; ++d) x[d] += v[d] * dt;
+        if (s->bounce) {
+            for (int d = 0; d < 3; ++d) {
+                if (x[d] < s->lo[d]) {
+                    x[d] = s->lo[d] + (s->lo[d] - x[d]);
+                    v[d] = -v[d];
+                } else if (x[d] > s->hi[d]) {
+                    x[d] = s->hi[d] - (x[d] - s->hi[d]);
+                    v[d] = -v[d];
+                }
+            }
+        }
+        const double k = 0.5 * m * dot3(v, v);
+        for (int d = 0; d < 3; ++d) o[d] += 0.5 / 1.0 * dt * t[d];
+        double tmp[3], g[3];
+        cross3(o, nn, tmp);
+        for (int d = 0; d < 3; ++d) g[d] = nn[d] + tmp[d] * dt;
+        const double gi = 1.0 / std::sqrt(dot3(g, g));
+        for (int d = 0; d < 3; ++d) nn[d] = g[d] * gi;
+        for (int d = 0; d < 3; ++d) f[d] = t[d] = 0;
+        return k;
+    });
+    if (s->Q == 0) s->Q = double(n) * 0.01;
+    s->zeta += 0.5 * s->dt / s->Q * (ke - 0.5 * 3.0 * double(n) * s->kBT);  // :182-185
+}
+
+}  // namespace
+
+extern "C" {
+
+void orc_set_threads(int nthreads) {
+    g_threads = nthreads;
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#endif
+}
+int orc_get_threads(void) {
+#ifdef _OPENMP
+    return g_threads > 0 ? g_threads : omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+void orc_default_bond_table(orc_system *s) {
+    const double r0[4] = {2.25, 1.1225, 2.25, 2.24};
+    for (int k = 0; k < ORC_MAX_BOND_TYPES; ++k) {
+        s->bstyle[k] = ORC_BOND_HARMONIC;
+        s->bK[k] = 57;
+        s->br0[k] = k < 4 ? r0[k] : 1.0;
+        s->bR[k] = 0;
+    }
+}
+
+int orc_forces_f64(const orc_system *s, double *f3, double *t3, double *e, orc_thermo *th) {
+    return forces_impl<double>(s, f3, t3, e, th);
+}
+int orc_forces_f32(const orc_system *s, double *f3, double *t3, double *e, orc_thermo *th) {
+    return forces_impl<float>(s, f3, t3, e, th);
+}
+int orc_step_langevin_f64(orc_system *s, int nsteps, orc_thermo *th) { return langevin_impl<double>(s, nsteps, th); }
+int orc_step_langevin_f32(orc_system *s, int nsteps, orc_thermo *th) { return langevin_impl<float>(s, nsteps, th); }
+
+int orc_nh_prologue_f64(orc_system *s, orc_thermo *th) {
+    forces_impl<double>(s, s->f, s->t, nullptr, th);
+    nh_final(s);
+    return 0;
+}
+int orc_step_nh_f64(orc_system *s, int nsteps, orc_thermo *th) {
+    for (int k = 0; k < nsteps; ++k) {
+        nh_initial(s);
+        forces_impl<double>(s, s->f, s->t, nullptr, th);
+        nh_final(s);
+        s->step++;
+    }
+    if (th) orc_thermo_f64(s, th);
+    return 0;
+}
+
+int orc_thermo_f64(const orc_system *s, orc_thermo *th) {
+    const FF<double> &F = ff<double>();
+    th->ke2 = chunked_sum(s->n, [&](int64_t i) {
+        const double *v = &s->v[3 * i];
+        return F.mass[s->type[i]] * (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    });
+    th->temperature = s->n ? th->ke2 / (3.0 * double(s->n)) : 0;
+    th->area = th->volume = 0;
+    if (s->nface > 0) {
+        TagMap tm;
+        tm.build(s->tag, s->n);
+        const Box b = box_of(s);
+        const int ref = tm[s->faces[0]];
+        for (int64_t k = 0; k < s->nface; ++k) {
+            double P[3][3];
+            for (int q = 0; q < 3; ++q) {
+                int p = tm[s->faces[3 * k + q]];
+                for (int d = 0; d < 3; ++d) P[q][d] = min_image(s->x[3 * p + d] - s->x[3 * ref + d], b.L[d], b.per[d]);
+            }
+            double e1[3], e2[3], N[3], bc[3];
+            for (int d = 0; d < 3; ++d) {
+                e1[d] = P[1][d] - P[0][d];
+                e2[d] = P[2][d] - P[0][d];
+            }
+            cross3(e1, e2, N);
+            cross3(P[1], P[2], bc);
+            th->area += 0.5 * std::sqrt(dot3(N, N));
+            th->volume += dot3(P[0], bc) / 6.0;
+        }
+    }
+    return 0;
+}
+
+int64_t orc_pairs(const orc_system *s, const double *rcut2, int32_t *pairs, int64_t cap) {
+    const int64_t n = s->n;
+    const Box b = box_of(s);
+    double cmax = 0;
+    for (int k = 0; k < NT * NT; ++k) cmax = std::max(cmax, std::sqrt(std::max(0.0, rcut2[k])));
+    CellList cl;
+    cl.build(s->x, n, b, cmax * (1 + 1e-12) + 1e-9);
+    std::vector<std::vector<int32_t>> per(static_cast<size_t>(n));
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int64_t i = 0; i < n; ++i) {
+        cl.for_candidates(s->x, n, i, [&](int64_t j) {
+            if (j <= i) return;
+            double r2 = 0;
+            for (int d = 0; d < 3; ++d) {
+                double dd = min_image(s->x[3 * i + d] - s->x[3 * j + d], b.L[d], b.per[d]);
+                r2 += dd * dd;
+            }
+            if (r2 < rcut2[s->type[i] * NT + s->type[j]] && r2 > 1e-5) per[size_t(i)].push_back(int32_t(j));
+        });
+        std::sort(per[size_t(i)].begin(), per[size_t(i)].end());
+    }
+    int64_t cnt = 0;
+    for (int64_t i = 0; i < n; ++i)
+        for (int32_t j : per[size_t(i)]) {
+            if (cnt < cap) {
+                pairs[2 * cnt] = int32_t(i);
+                pairs[2 * cnt + 1] = j;
+            }
+            cnt++;
+        }
+    return cnt;
+}
+
+/* src/reorder_morton.h:25-42 */
+static inline uint32_t bit_space3(uint32_t x) {
+    x = (x | (x << 12)) & 0x00FC003Fu;
+    x = (x | (x << 6)) & 0x381C0E07u;
+    x = (x | (x << 4)) & 0x190C8643u;
+    x = (x | (x << 2)) & 0x49249249u;
+    return x;
+}
+static inline uint32_t to_uint(double v) {
+    /* static_cast<unsigned int>(double) for values in [0, 2^32); inputs
+     * below zero (outside the reference box) are out of contract. */
+    if (!(v >= 0)) return 0;
+    if (v >= 4294967296.0) return 0xFFFFFFFFu;
+    return uint32_t(v);
+}
+void orc_morton_encode(const double *p3, int64_t n, const double *bsize, uint32_t *keys) {
+    for (int64_t i = 0; i < n; ++i) {
+        uint32_t c[3];
+        for (int d = 0; d < 3; ++d) c[d] = to_uint(2 * p3[3 * i + d] + bsize[d]);
+        keys[i] = bit_space3(c[0]) | (bit_space3(c[1]) << 1) | (bit_space3(c[2]) << 2);
+    }
+}
+void orc_morton_order(const double *p3, int64_t n, const double *bsize, int32_t *order) {
+    std::vector<uint32_t> k(static_cast<size_t>(n));
+    orc_morton_encode(p3, n, bsize, k.data());
+    for (int64_t i = 0; i < n; ++i) order[i] = int32_t(i);
+    std::stable_sort(order, order + n, [&](int32_t a, int32_t b) { return k[size_t(a)] < k[size_t(b)]; });
+}
+
+void orc_noise(uint64_t seed, int64_t step, int tag, int sys, double r[3]) { noise3(seed, step, tag, sys, r); }
+
+void orc_ff_tables(double *mass6, double *radius6, double *cutsq36, double *lj_cutsq36) {
+    const FF<double> &F = ff<double>();
+    for (int t = 0; t < NT; ++t) {
+        mass6[t] = F.mass[t];
+        radius6[t] = F.radius[t];
+    }
+    for (int k = 0; k < NT * NT; ++k) {
+        const int ti = k / NT, tj = k % NT;
+        if (ti == 0 || tj == 0) {
+            const int p = std::max(ti, tj);
+            cutsq36[k] = F.cutsqlp[p];
+            lj_cutsq36[k] = F.lj_cutsq[p];
+        } else {
+            cutsq36[k] = F.cutsqpp[ti + NT * tj];
+            lj_cutsq36[k] = F.lj_cutsq[ti + NT * tj];
+        }
+    }
+}
+
+}  // extern "C"

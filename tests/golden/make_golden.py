@@ -1,0 +1,180 @@
+"""Generate the golden vectors in tests/golden/ from the reference's own code.
+
+Run in a container that holds the reference source tree:
+
+    python tests/golden/make_golden.py [--ref-src /path/to/reference/src]
+
+It builds oracle/_ref/ (a C ABI over the reference's headers, FP64 via a
+force-included configuration and the default FP32) with oracle/Makefile, then
+calls the reference's pair sweeps, compute_bonded, verlet_langevin,
+the fused Nose-Hoover functors, compute_temperature, morton_encode and
+init_rbc on seeded inputs, and writes the inputs and the reference's outputs
+to small .npz fixtures.  The tests replay these inputs through the oracle and
+the GPU library; nothing at test time needs the reference tree.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+from oracle import oracle as orc  # noqa: E402
+
+OUT = os.path.dirname(os.path.abspath(__file__))
+
+
+def lattice(nx, ny, spacing=1.1, jitter=0.05, tilt=0.05, kT=1.0, seed=1):
+    """Flat square lattice of lipids (the plain small workload's geometry)."""
+    rng = np.random.default_rng(seed)
+    ix, iy = np.meshgrid(np.arange(nx), np.arange(ny), indexing="xy")
+    x = np.stack([ix.ravel() * spacing, iy.ravel() * spacing, np.zeros(nx * ny)], 1)
+    x += rng.normal(0, jitter, x.shape)
+    n = len(x)
+    ang = rng.normal(0, tilt, n)
+    phi = rng.uniform(0, 2 * np.pi, n)
+    axis = np.stack([np.cos(phi), np.sin(phi), np.zeros(n)], 1)
+    # rotate +z about an in-plane axis by ang: n = (sin(a) * (axis x z), cos(a))
+    axz = np.cross(axis, np.array([0.0, 0.0, 1.0]))
+    nrm = np.sin(ang)[:, None] * axz + np.cos(ang)[:, None] * np.array([0.0, 0.0, 1.0])
+    v = rng.normal(0, np.sqrt(kT), (n, 3))
+    o = rng.normal(0, 0.1, (n, 3))
+    return x, nrm, v, o, np.zeros(n, np.int32), np.arange(1, n + 1, dtype=np.int32)
+
+
+def icosahedron():
+    t = (1 + 5 ** 0.5) / 2
+    v = np.array([[-1, t, 0], [1, t, 0], [-1, -t, 0], [1, -t, 0], [0, -1, t], [0, 1, t],
+                  [0, -1, -t], [0, 1, -t], [t, 0, -1], [t, 0, 1], [-t, 0, -1], [-t, 0, 1]], float)
+    v /= np.linalg.norm(v, axis=1)[:, None]
+    f = np.array([[0, 11, 5], [0, 5, 1], [0, 1, 7], [0, 7, 10], [0, 10, 11], [1, 5, 9], [5, 11, 4],
+                  [11, 10, 2], [10, 7, 6], [7, 1, 8], [3, 9, 4], [3, 4, 2], [3, 2, 6], [3, 6, 8],
+                  [3, 8, 9], [4, 9, 5], [2, 4, 11], [6, 2, 10], [8, 6, 7], [9, 8, 1]])
+    # counter-clockwise seen from outside, the convention of the shipped mesh
+    c = v[f].mean(1)
+    nn = np.cross(v[f[:, 1]] - v[f[:, 0]], v[f[:, 2]] - v[f[:, 0]])
+    flip = np.sum(nn * c, 1) < 0
+    f[flip] = f[flip][:, ::-1]
+    e = set()
+    for a, b, cc in f:
+        for p, q in ((a, b), (b, cc), (cc, a)):
+            e.add((min(p, q), max(p, q)))
+    return v, np.array(sorted(e)), f
+
+
+def whole_cell(prefix):
+    v, e, f = icosahedron()
+    np.savetxt(prefix + ".vert.txt", v, fmt="%.9f", delimiter="\t")
+    np.savetxt(prefix + ".bond.txt", e, fmt="%d", delimiter="\t")
+    np.savetxt(prefix + ".face.txt", f, fmt="%d", delimiter="\t")
+    R = orc.ref("f64")
+    cap, bcap = 200000, 200000
+    x = np.zeros((cap, 3))
+    nrm = np.zeros((cap, 3))
+    ty = np.zeros(cap, np.int32)
+    tg = np.zeros(cap, np.int32)
+    b3 = np.zeros((bcap, 3), np.int32)
+    nb = C.c_int64()
+    area = C.c_double()
+    n = R.ref_init_rbc(prefix.encode(), cap, x.ctypes.data, nrm.ctypes.data, ty.ctypes.data, tg.ctypes.data, bcap,
+                       b3.ctypes.data, C.byref(nb), C.byref(area))
+    assert n > 0
+    return x[:n].copy(), nrm[:n].copy(), ty[:n].copy(), tg[:n].copy(), b3[:nb.value].copy(), area.value
+
+
+def ref_forces(prec, x, nrm, ty, tg, bonds):
+    R = orc.ref(prec)
+    n = len(x)
+    f = np.zeros((n, 3))
+    t = np.zeros((n, 3))
+    b = np.ascontiguousarray(bonds, np.int32)
+    R.ref_forces(n, x.ctypes.data, nrm.ctypes.data, ty.ctypes.data, tg.ctypes.data, len(b),
+                 b.ctypes.data if len(b) else None, f.ctypes.data, t.ctypes.data)
+    return f, t
+
+
+def ref_langevin(prec, x, nrm, v, o, ty, tg, bonds, dt, kBT, eta, nsteps):
+    R = orc.ref(prec)
+    x, nrm, v, o = (np.ascontiguousarray(a, np.float64).copy() for a in (x, nrm, v, o))
+    b = np.ascontiguousarray(bonds, np.int32)
+    R.ref_langevin(len(x), x.ctypes.data, nrm.ctypes.data, v.ctypes.data, o.ctypes.data, ty.ctypes.data,
+                   tg.ctypes.data, len(b), b.ctypes.data if len(b) else None, dt, kBT, eta, nsteps)
+    return x, nrm, v, o
+
+
+def ref_nh(prec, x, nrm, v, o, ty, tg, bonds, dt, kBT, zeta, Q, nsteps):
+    R = orc.ref(prec)
+    x, nrm, v, o = (np.ascontiguousarray(a, np.float64).copy() for a in (x, nrm, v, o))
+    b = np.ascontiguousarray(bonds, np.int32)
+    z = C.c_double(zeta)
+    R.ref_nh(len(x), x.ctypes.data, nrm.ctypes.data, v.ctypes.data, o.ctypes.data, ty.ctypes.data,
+             tg.ctypes.data, len(b), b.ctypes.data if len(b) else None, dt, kBT, C.byref(z), Q, nsteps)
+    return x, nrm, v, o, z.value
+
+
+def ref_temperature(prec, x, nrm, v, ty, tg):
+    R = orc.ref(prec)
+    return R.ref_temperature(len(x), x.ctypes.data, nrm.ctypes.data, v.ctypes.data, ty.ctypes.data, tg.ctypes.data)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref-src", default=orc.DEFAULT_REF_SRC)
+    args = ap.parse_args()
+    orc.build(args.ref_src)
+    assert orc.ref_available("f64") and orc.ref_available("f32"), "reference harness did not build"
+    assert orc.ref("f64").ref_real_bytes() == 8 and orc.ref("f32").ref_real_bytes() == 4
+
+    # ---- plain lipid lattice ------------------------------------------------
+    x, nrm, v, o, ty, tg = lattice(24, 24)
+    nob = np.zeros((0, 3), np.int32)
+    f64, t64 = ref_forces("f64", x, nrm, ty, tg, nob)
+    f32, t32 = ref_forces("f32", x, nrm, ty, tg, nob)
+    lx, ln, lv, lo = ref_langevin("f64", x, nrm, v, o, ty, tg, nob, 0.01, 0.0, 0.01, 100)
+    nx_, nn_, nv_, no_, nz = ref_nh("f64", x, nrm, v, o, ty, tg, nob, 0.01, 1.0, 0.0, 0.0, 20)
+    T = ref_temperature("f64", x, nrm, v, ty, tg)
+    np.savez_compressed(os.path.join(OUT, "lattice_576.npz"), x=x, nrm=nrm, v=v, o=o, type=ty, tag=tg,
+                        f64=f64, t64=t64, f32=f32, t32=t32, temperature=T,
+                        lang_x=lx, lang_n=ln, lang_v=lv, lang_o=lo, lang_steps=100, lang_dt=0.01, lang_eta=0.01,
+                        nh_x=nx_, nh_n=nn_, nh_v=nv_, nh_o=no_, nh_zeta=nz, nh_steps=20, nh_dt=0.01, nh_kBT=1.0)
+    print("lattice_576:", len(x), "particles; |f|max", np.abs(f64).max())
+
+    # ---- whole cell on a 12-vertex mesh (all protein types, all bond types) --
+    os.makedirs(orc.REF_DIR, exist_ok=True)
+    x, nrm, ty, tg, bonds, area = whole_cell(os.path.join(orc.REF_DIR, "ico12"))
+    rng = np.random.default_rng(7)
+    m = np.array([1, 4, 4, 1, 10, 10], float)[ty]
+    v = rng.normal(0, 1, (len(x), 3)) * np.sqrt(0.22 / m)[:, None]
+    o = rng.normal(0, 0.05, (len(x), 3))
+    f64, t64 = ref_forces("f64", x, nrm, ty, tg, bonds)
+    f32, t32 = ref_forces("f32", x, nrm, ty, tg, bonds)
+    lx, ln, lv, lo = ref_langevin("f64", x, nrm, v, o, ty, tg, bonds, 0.01, 0.0, 0.01, 20)
+    nx_, nn_, nv_, no_, nz = ref_nh("f64", x, nrm, v, o, ty, tg, bonds, 0.01, 0.22, 0.0, 0.0, 10)
+    T = ref_temperature("f64", x, nrm, v, ty, tg)
+    np.savez_compressed(os.path.join(OUT, "cell_ico12.npz"), x=x, nrm=nrm, v=v, o=o, type=ty, tag=tg, bonds=bonds,
+                        mesh_area=area, f64=f64, t64=t64, f32=f32, t32=t32, temperature=T,
+                        lang_x=lx, lang_n=ln, lang_v=lv, lang_o=lo, lang_steps=20, lang_dt=0.01, lang_eta=0.01,
+                        nh_x=nx_, nh_n=nn_, nh_v=nv_, nh_o=no_, nh_zeta=nz, nh_steps=10, nh_dt=0.01, nh_kBT=0.22)
+    print("cell_ico12:", len(x), "particles,", len(bonds), "bonds; types", np.bincount(ty))
+
+    # ---- Morton keys -----------------------------------------------------------
+    rng = np.random.default_rng(3)
+    p = rng.uniform(-1000, 1000, (4000, 3))
+    edge = np.array([[-1000, -1000, -1000], [-488.5, -488.0, -487.5], [-488.01, 0, 0], [0, 0, 0],
+                     [999.99, 999.99, 999.99], [-1000, 0, 1000], [-500.25, 12.75, -999.5]], float)
+    p = np.concatenate([p, edge, rng.uniform(-1000, -480, (500, 3))])
+    k64 = np.zeros(len(p), np.uint32)
+    orc.ref("f64").ref_morton_encode(len(p), np.ascontiguousarray(p).ctypes.data, k64.ctypes.data)
+    p32 = p.astype(np.float32).astype(np.float64)
+    k32 = np.zeros(len(p), np.uint32)
+    orc.ref("f32").ref_morton_encode(len(p), np.ascontiguousarray(p32).ctypes.data, k32.ctypes.data)
+    np.savez_compressed(os.path.join(OUT, "morton.npz"), p=p, keys64=k64, p32=p32, keys32=k32)
+    print("morton:", len(p), "points")
+
+
+if __name__ == "__main__":
+    main()
