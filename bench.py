@@ -1,0 +1,281 @@
+"""Benchmark: particle-steps/s of the OpenRBC step on the 4M-particle red-cell
+membrane, mixed precision vs plain FP64 on one GB300.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Workload: Evans-Fung biconcave membrane with 4.0M lipids (Poisson-disk by
+area, density 1.05) plus 32,492 spectrin anchors on a frequency-57 geodesic
+mesh, 97,470 WLC-POW bonds (rest length U[0.9, 1.1] x mean edge), global
+area / volume constraint at reduced volume 0.64, Langevin dt = 0.01, kT = 1,
+eta = 0.01.  Seeded synthetic data (the reference ships no dataset).
+
+value      mixed-precision particle-steps/s, device time of K steps (inputs
+           resident in HBM; working set several GB, larger than L2).
+e2e        the same metric through the C ABI the reference host would call
+           each step: orbc_gpu_set_state from pinned host buffers + one
+           orbc_gpu_step + orbc_gpu_download back to the host buffers.
+roofline   the fused step kernel: compulsory bytes (104 B per particle-step,
+           mixed) / its CUDA-event time vs measured HBM bandwidth; the FP32
+           ALU fraction of its algorithmic flops is reported beside it.
+cpu_baseline  the oracle's FP32 port of the reference's CPU step on the
+           host cores, bounded sample.
+--impl reference  times that CPU implementation for the same metric.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle-steps/s, 4M-particle RBC: mixed vs FP64 GPU at force err<=1e-5"
+N_LIPID = 4_000_000
+FREQ = 57
+KT = 1.0
+DT = 0.01
+SKIN = 0.4
+# algorithmic counts per particle-step (mixed): state read + written once
+BYTES_PER_PSTEP = 104.0
+FLOP_PER_PAIR = 106.0
+
+
+def workload():
+    from openrbc_gb300 import workloads
+    return workloads.rbc(n_lipid=N_LIPID, freq=FREQ, kT=KT, seed=2)
+
+
+def make_sim(w, precision, **kw):
+    from openrbc_gb300 import RTParameter, Simulation, workloads
+    p = RTParameter(init="trimesh", mesh="synthetic", kBT=KT, dt=DT, eta=0.01, precision=precision)
+    s = Simulation(p, skin=kw.pop("skin", SKIN), bond_table=workloads.RBC_BOND_TABLE, **kw)
+    c = w["constraint"]
+    sysdesc = [{"lo": (-1000.0,) * 3, "hi": (1000.0,) * 3, "periodic": (0, 0, 0), "kv": c["kv"], "V0": c["V0"],
+                "ka": c["ka"], "A0": c["A0"]}]
+    s.upload_batch(sysdesc, w["x"], w["n"], w["v"], w["o"], w["type"], w["tag"], [0, len(w["x"])],
+                   bonds=w["bonds"], bond_r0=w["bond_r0"], faces=w["faces"])
+    return s
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    def __init__(self, index=0):
+        self.samples = []
+        self.stop = threading.Event()
+        self.index = index
+        self.t = threading.Thread(target=self.run, daemon=True)
+
+    def run(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        while not self.stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True,
+                                     timeout=5).stdout.strip()
+                if out:
+                    self.samples.append([s.strip() for s in out.split(",")])
+            except Exception:
+                pass
+            self.stop.wait(0.2)
+
+    def __enter__(self):
+        self.t.start()
+        return self
+
+    def __exit__(self, *a):
+        self.stop.set()
+        self.t.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for s in self.samples for k in range(4) if s[3 + k].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def cpu_baseline(w, nsteps=2, precision="f32"):
+    """The oracle's port of the reference CPU step on all host cores."""
+    from oracle import oracle as orc
+    st = orc.State(x=w["x"], nrm=w["n"], v=w["v"], o=w["o"], type=w["type"], tag=w["tag"], bonds=w["bonds"],
+                   bond_r0=w["bond_r0"], faces=w["faces"], kBT=KT, dt=DT, eta=0.01, seed=0xBAD5EED,
+                   kv=w["constraint"]["kv"], V0=w["constraint"]["V0"], ka=w["constraint"]["ka"],
+                   A0=w["constraint"]["A0"])
+    st.bstyle[4], st.bK[4], st.br0[4], st.bR[4] = 2, 1.0, 1.0, 2.2
+    threads = os.cpu_count() or 1
+    orc.set_threads(threads)
+    t0 = time.perf_counter()
+    orc.langevin(st, nsteps, precision)
+    dt = time.perf_counter() - t0
+    n = len(w["x"])
+    return {"value": n * nsteps / dt, "unit": "particle-steps/s", "cores": orc.get_threads(), "kind": "port",
+            "sample": f"{nsteps} Langevin steps of the full {n}-particle membrane, FP32, oracle port of "
+                      f"src/compute_pairwise_fused.h + src/integrate_langevin.h"}
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    return rank, ws
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allreduce_max(v, ws):
+    if ws <= 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def run_reference(args, rank, ws):
+    if rank != 0:
+        return 0
+    w = workload()
+    from oracle import oracle as orc
+    orc.build()
+    n = len(w["x"])
+    for _ in range(args.warmup):
+        pass  # the CPU port has no warm-up state; warm-up steps are skipped to bound the run
+    cb = cpu_baseline(w, nsteps=max(1, args.steps // 10))
+    line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": "particle-steps/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * n / cb["value"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"rbc-evans-fung-{n}", "n_particles": n, "integrator": "langevin",
+                       "dt": DT, "kT": KT},
+            "cpu_baseline": cb, "e2e": {"value": cb["value"], "unit": "particle-steps/s",
+                                        "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--fp64-steps", type=int, default=10)
+    args = ap.parse_args()
+    rank, ws = dist_setup()
+    if args.impl == "reference":
+        return run_reference(args, rank, ws)
+    if "LOCAL_RANK" in os.environ:
+        os.environ.setdefault("CUDA_VISIBLE_DEVICES", os.environ["LOCAL_RANK"])
+
+    from openrbc_gb300 import _native
+    _native.lib()
+    w = workload()
+    n = len(w["x"])
+
+    # ---- mixed precision, device-resident
+    sim = make_sim(w, "mixed")
+    f_mixed, _, _ = sim.forces()
+    sim.step(args.warmup)
+    barrier(ws)
+    with ClockSampler() as clk:
+        th = sim.step(args.steps)
+        ms, launches = sim.last_timing()
+    ms = allreduce_max(ms, ws)
+    value = ws * n * args.steps / (ms * 1e-3)
+
+    # ---- dominant kernel timing (profiled pass: events around each launch group)
+    prof = sim.profile(20)
+
+    # ---- plain FP64 on the same workload
+    sim64 = make_sim(w, "fp64")
+    f64, _, _ = sim64.forces()
+    sim64.step(2)
+    sim64.step(args.fp64_steps)
+    ms64, _ = sim64.last_timing()
+    value64 = n * args.fp64_steps / (ms64 * 1e-3)
+    sim64.close()
+    ferr = float(np.linalg.norm(f_mixed - f64) / np.linalg.norm(f64))
+
+    # ---- end to end through the C ABI with pinned host buffers
+    import torch
+    host = [torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy() for _ in range(4)]
+    sim.download()
+    x, nn, v, o = sim.download()
+    for h, a in zip(host, (x, nn, v, o)):
+        h[:] = a
+    e2e_steps = max(3, args.steps // 20)
+    import ctypes as C
+    from openrbc_gb300 import _native as N
+    L = N.lib()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        N.check(L.orbc_gpu_set_state(sim.h, *[h.ctypes.data for h in host]), sim.h)
+        N.check(L.orbc_gpu_step(sim.h, 1, None), sim.h)
+        N.check(L.orbc_gpu_download(sim.h, *[h.ctypes.data for h in host]), sim.h)
+    e2e_s = allreduce_max(time.perf_counter() - t0, ws)
+    e2e = {"value": ws * n * e2e_steps / e2e_s, "unit": "particle-steps/s",
+           "h2d_bytes_per_step": 4 * 3 * 8 * n, "d2h_bytes_per_step": 4 * 3 * 8 * n,
+           "note": "per step: orbc_gpu_set_state (pinned H2D, forces a neighbour rebuild) + orbc_gpu_step(1) + "
+                   "orbc_gpu_download (D2H)"}
+
+    peak, peak_kind = measured_peaks()
+    kt = prof["step_kernel_ms"]
+    achieved = BYTES_PER_PSTEP * n / (kt * 1e-3) / 1e9
+    k_mean = prof.get("mean_neighbors", None)
+    flops = 0.5 * (th["max_neighbors"] if k_mean is None else k_mean) * FLOP_PER_PAIR * n
+    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": None, "kernel": "k_step_langevin<float>", "kernel_ms": kt,
+            "peak_source": peak_kind,
+            "alu": {"achieved_tflops": flops / (kt * 1e-3) / 1e12, "unit": "TFLOP/s (FP32, algorithmic)"}}
+    line = {"metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"rbc-evans-fung-{n}", "n_particles": n, "n_lipid": N_LIPID,
+                       "anchors": n - N_LIPID, "bonds": int(len(w["bonds"])), "faces": int(len(w["faces"])),
+                       "integrator": "langevin", "dt": DT, "kT": KT, "skin": SKIN, "precision": "mixed",
+                       "l2": "inputs larger than L2 (state + neighbour list > 1 GB)",
+                       "parallelism": f"replicas x{ws}"},
+            "fp64": {"value": value64, "ms_per_step": ms64 / args.fp64_steps, "steps": args.fp64_steps},
+            "mixed_over_fp64": value / ws / value64, "force_rel_err_mixed_vs_fp64": ferr,
+            "rebuilds_in_timed_region": None, "roofline": roof, "e2e": e2e, "gpu_launches": launches,
+            "clocks": clk.summary(), "profile": prof}
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(w)
+    sim.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,205 @@
+/*
+ * liborbc_gpu -- C ABI of the GB300 (sm_103a) implementation of OpenRBC's
+ * per-timestep hot path.
+ *
+ * The reference has no runtime plug-in surface: its main() selects the force
+ * and integration routines at compile time (src/openrbc.cpp:162-186 and
+ * :191-242, #ifdef FUSED_PAIRWISE / LANGEVIN / FUSED_INTEGRATOR) and calls
+ *   compute_pairwise_fused(voronoi, lipid, protein, cell_lipid, cell_protein)
+ *       (src/compute_pairwise_fused.h:238-242),
+ *   compute_bonded(protein)                        (src/compute_bonded.h:89-90),
+ *   integrate(verlet_langevin(param), lipid, protein)
+ *       (src/integrate_nh.h:29-55, src/integrate_langevin.h:99-149),
+ *   integrate(verlet_initial_bounce_clearforce_update / post_toque_final_update)
+ *       (src/integrate_nh.h:178-273),
+ *   compute_temperature(lipid, protein, param)     (src/compute_temperature.h:24-29),
+ * with the Voronoi / k-d tree / Morton reorder machinery in between
+ * (src/voronoi.h:78-237, src/reorder_morton.h:44-122, src/reorder.h:33-149).
+ * A host driver that keeps RTParameter and the containers replaces that block
+ * of main() by the calls below; the library owns all device state.
+ *
+ * Conventions: every call returns ORBC_OK (0) or an ORBC_ERR_* code and never
+ * exits or traps; orbc_gpu_error() returns the message of the last failure on
+ * a handle.  Arrays are host memory, AoS double[3 n] like the reference's
+ * vect containers (src/container.h:64-73); bonds are (type, tag_i, tag_j)
+ * triples like openrbc::Bond (src/container.h:30-34).  A handle is not
+ * re-entrant: use it from one host thread.
+ */
+#ifndef ORBC_GPU_H_
+#define ORBC_GPU_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct orbc_handle orbc_handle;
+
+enum {
+    ORBC_OK = 0,
+    ORBC_ERR_ARG = 1,          /* bad argument (the reference would rt_assert + exit(0)) */
+    ORBC_ERR_CUDA = 2,         /* CUDA runtime error                                      */
+    ORBC_ERR_NBR_OVERFLOW = 3, /* neighbour list overflowed its capacity                 */
+    ORBC_ERR_NAN = 4,          /* non-finite coordinate                                   */
+    ORBC_ERR_GRID = 5,         /* particle left an open grid (kept in the edge cell)       */
+    ORBC_ERR_BOND = 6,         /* FENE / WLC bond stretched beyond its maximum            */
+    ORBC_ERR_STATE = 7,        /* call out of order (e.g. step before upload)             */
+    ORBC_ERR_NOMEM = 8,        /* device allocation failed                                */
+    ORBC_ERR_NODEV = 9         /* no CUDA device                                          */
+};
+
+enum { ORBC_PREC_FP64 = 0, ORBC_PREC_MIXED = 1 };
+enum { ORBC_INT_LANGEVIN = 0, ORBC_INT_NOSE_HOOVER = 1 };
+enum { ORBC_BOND_HARMONIC = 0, ORBC_BOND_FENE = 1, ORBC_BOND_WLC_POW = 2 };
+#define ORBC_MAX_BOND_TYPES 8
+
+/* Run-time parameters.  dt, kBT, eta, Q, seed keep the meaning (and the
+ * defaults, see orbc_gpu_default_params) of RTParameter
+ * (src/runtime_parameter.h:38-76); the compile-time switches LANGEVIN /
+ * FUSED_INTEGRATOR and `real` (src/config_static.h:30-34) become the
+ * integrator and precision fields. */
+typedef struct {
+    int precision;          /* ORBC_PREC_FP64 or ORBC_PREC_MIXED (FP32 forces, FP64 reductions) */
+    int integrator;         /* ORBC_INT_LANGEVIN or ORBC_INT_NOSE_HOOVER                          */
+    double dt, kBT, eta;    /* time step, thermal energy, solvent viscosity                       */
+    double Q;               /* Nose-Hoover mass; 0 -> 0.01 N per system                            */
+    uint64_t seed;          /* counter-based RNG key (Langevin noise)                              */
+    double skin;            /* neighbour-list skin; rebuild when any particle moved > skin/2      */
+    int max_neighbors;      /* initial neighbour capacity per particle (0 = automatic)            */
+    int rebuild_every;      /* also rebuild at least every k steps (0 = displacement only)        */
+    int bounce;             /* Nose-Hoover reflective walls at the box (src/integrate_nh.h:124-144) */
+    int use_graph;          /* capture each step in a CUDA graph                                  */
+    int energy;             /* accumulate the potential energy every step                         */
+    /* box of a single-system upload; open axes grow to the particles' extent */
+    double lo[3], hi[3];
+    int periodic[3];
+    /* global membrane constraints on the face mesh: F = -k (Q - Q0)/Q0 dQ/dx */
+    double kv, V0, ka, A0;
+    /* bond-type table: style, stiffness (harmonic K / FENE K / WLC kT/p),
+       default rest length, FENE maximum extension / WLC lmax-over-r0 */
+    int bond_style[ORBC_MAX_BOND_TYPES];
+    double bond_K[ORBC_MAX_BOND_TYPES];
+    double bond_r0[ORBC_MAX_BOND_TYPES];
+    double bond_R[ORBC_MAX_BOND_TYPES];
+} orbc_params;
+
+/* One independent system of a batched upload (its own box and constraint). */
+typedef struct {
+    double lo[3], hi[3];
+    int periodic[3];
+    double kv, V0, ka, A0;
+    double zeta;            /* initial Nose-Hoover variable */
+} orbc_system_desc;
+
+typedef struct {
+    int64_t step;           /* completed steps                                           */
+    int64_t n;              /* particles                                                 */
+    double temperature;     /* sum m v^2 / 3N (src/compute_temperature.h:24-29)          */
+    double ke2;             /* sum m v^2                                                 */
+    double epot;            /* potential energy (when params.energy or after forces())  */
+    double area, volume;    /* membrane mesh area and enclosed volume (FP64)            */
+    double zeta;            /* Nose-Hoover thermostat variable                           */
+    int64_t rebuilds;       /* neighbour-list rebuilds so far                            */
+    int max_neighbors;      /* largest neighbour count at the last rebuild               */
+    int capacity;           /* neighbour-list capacity per particle                      */
+    int flags;              /* ORBC_ERR_* bits seen (1 << code)                           */
+    int pad;
+} orbc_thermo;
+
+/* Defaults of RTParameter (src/runtime_parameter.h:47-64): kBT 0.22,
+ * eta 0.01, dt 0.01, seed 0xBAD5EED; reference bond table
+ * (src/forcefield_canonical.h:106-109); box +-1000 (:111-115). */
+void orbc_gpu_default_params(orbc_params *p);
+
+/* Replaces the set-up in src/openrbc.cpp:43-71 (containers, Voronoi init). */
+int orbc_gpu_create(const orbc_params *p, orbc_handle **out);
+
+/* Topology + state of one system.  Lipids are type 0, proteins 1..5
+ * (src/forcefield_canonical.h:31-37); bonds3 = (type, tag_i, tag_j) refer to
+ * tags (src/compute_bonded.h:109-110).  Replaces LipidContainer/ProteContainer
+ * filling and TagIndexMap::build_map (src/container.h:36-58). */
+int orbc_gpu_upload(orbc_handle *h, const double *x3, const double *n3, const double *v3, const double *o3,
+                    const int *type, const int *tag, size_t n, const int *bonds3, size_t nb);
+
+/* Several independent systems in one launch per step: particles of system s
+ * are [offsets[s], offsets[s+1]) of the arrays; tags are unique over all
+ * systems; bond_r0 (may be NULL) gives per-bond rest lengths; faces3 (may be
+ * NULL) are (tag_a, tag_b, tag_c) triangles, counter-clockwise seen from
+ * outside, defining each system's membrane area and volume.  No reference
+ * counterpart (the reference runs one cell per process). */
+int orbc_gpu_upload_batch(orbc_handle *h, int nsys, const orbc_system_desc *sys, const int64_t *offsets,
+                          const double *x3, const double *n3, const double *v3, const double *o3, const int *type,
+                          const int *tag, size_t n, const int *bonds3, const double *bond_r0, size_t nb,
+                          const int *faces3, size_t nf);
+
+/* Overwrite positions / orientations / velocities / angular velocities of
+ * the uploaded particles (same order as the upload) without re-sending the
+ * topology; forces a neighbour rebuild.  Used when the host containers stay
+ * the source of truth between steps. */
+int orbc_gpu_set_state(orbc_handle *h, const double *x3, const double *n3, const double *v3, const double *o3);
+
+/* nsteps of the loop body of src/openrbc.cpp:189-242 (pair forces, bonds,
+ * constraint, integrator; neighbour rebuild on demand).  out may be NULL. */
+int orbc_gpu_step(orbc_handle *h, int nsteps, orbc_thermo *out);
+
+/* Current state in upload order (any pointer may be NULL). */
+int orbc_gpu_download(orbc_handle *h, double *x3, double *n3, double *v3, double *o3);
+
+/* Parity hook: forces, torques and per-particle potential energy at the
+ * current state, in upload order (compute_pairwise_fused + compute_bonded,
+ * src/compute_pairwise_fused.h:238-320, src/compute_bonded.h:89-146). */
+int orbc_gpu_forces(orbc_handle *h, double *f3, double *t3, double *e);
+
+/* Temperature, energy, area, volume, thermostat state of system `sys`. */
+int orbc_gpu_thermo(orbc_handle *h, int sys, orbc_thermo *out);
+
+/* Parity hook: the full neighbour list in upload order as CSR (counts[n],
+ * then up to cap neighbour indices); returns the total in *total. */
+int orbc_gpu_neighbors(orbc_handle *h, int *counts, int *list, int64_t cap, int64_t *total);
+
+/* Parity hook: grid of system `sys` (origin, cell size, cell counts) and, per
+ * particle in upload order, its packed cell (x | y << 11 | z << 22), its
+ * offset from the cell centre and its slot in the cell-sorted device order. */
+int orbc_gpu_cells(orbc_handle *h, int sys, double *lo3, double *lc3, int *nc3, int *cell, double *offset3,
+                   int *slot);
+
+/* Force a neighbour-list rebuild now (sort + bins + list). */
+int orbc_gpu_rebuild(orbc_handle *h);
+
+/* Milliseconds of device time of the last orbc_gpu_step call, and the number
+ * of kernel launches it issued (graph nodes included). */
+int orbc_gpu_last_timing(orbc_handle *h, double *ms, int64_t *launches);
+
+/* Per-kernel device times over nsteps un-captured steps (CUDA events around
+ * each launch group on the library's stream; a synchronisation per step).
+ * No reference counterpart (the reference's Timers, src/timer.h:26-69, time
+ * whole routines on the host). */
+typedef struct {
+    int64_t steps;            /* steps profiled                                   */
+    int64_t rebuilds;         /* neighbour rebuilds among them                    */
+    double step_kernel_ms;    /* mean time of the fused force + integrator kernel */
+    double rebuild_ms;        /* mean time of one full rebuild chain              */
+    double gate_ms;           /* mean time of the rebuild chain when it was skipped */
+    double mesh_ms;           /* mean time of the area / volume kernel            */
+    double mean_neighbors;    /* mean neighbour-list length per particle          */
+    double pairs_in_cutoff;   /* mean partners inside the interaction range       */
+} orbc_profile;
+int orbc_gpu_profile(orbc_handle *h, int nsteps, orbc_profile *out);
+
+/* Reference Morton key of n points (src/reorder_morton.h:25-42; bsize3 is
+ * RTParameter::bsize, 2000 per axis) and the stable order by (key, index)
+ * that reorder_morton (src/reorder_morton.h:44-122) sorts by. */
+int orbc_gpu_morton_encode(const double *p3, int64_t n, const double *bsize3, uint32_t *keys);
+int orbc_gpu_morton_order(const double *p3, int64_t n, const double *bsize3, int32_t *order);
+
+int orbc_gpu_destroy(orbc_handle *h);
+const char *orbc_gpu_error(orbc_handle *h);   /* NULL handle -> last create/standalone error */
+const char *orbc_gpu_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

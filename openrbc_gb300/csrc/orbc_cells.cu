@@ -1,0 +1,546 @@
+// Spatial sort, cell binning and neighbour-list build (the GPU replacement of
+// the reference's Voronoi tessellation + k-d tree + Morton reorder:
+// src/voronoi.h:143-237, src/kdtree.h:117-285, src/reorder_morton.h:44-122,
+// src/reorder.h:33-149), plus state conversion between the caller's AoS
+// double arrays and the device layout.
+//
+// Rebuild chain (runs only when a particle moved more than skin/2 since the
+// last build, or on demand):
+//   k_rebin          re-express each position in the cell that now holds it,
+//                    clear the old cell ranges, emit (cell key, slot) pairs
+//   LSD radix sort   stable, 8-bit digits, (key, slot) -> sorted + inverse map
+//   k_ranges_gather  cell [begin, end) ranges and the physical reorder of all
+//                    per-particle arrays (bond / face partners remapped)
+//   k_nlist          full neighbour list per particle from the 27 cells
+//                    around its own; the last block flips buffer parities
+#include "orbc_device.cuh"
+
+#include <cstdio>
+
+namespace orbc {
+
+namespace {
+
+__device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+
+__device__ __forceinline__ unsigned cell_lin(const SysDev &s, int x, int y, int z) {
+    return unsigned(x) + unsigned(s.nc[0]) * (unsigned(y) + unsigned(s.nc[1]) * unsigned(z));
+}
+__device__ __forceinline__ unsigned ncell_of(const SysDev &s) {
+    return unsigned(s.nc[0]) * unsigned(s.nc[1]) * unsigned(s.nc[2]);
+}
+
+template<class T4> __device__ __forceinline__ T4 ld4(const T4 *p) { return *p; }
+template<> __device__ __forceinline__ float4 ld4<float4>(const float4 *p) { return __ldg(p); }
+
+__device__ __forceinline__ int gate_closed(const int *gate) { return gate && !__ldcg(gate); }
+
+}  // namespace
+
+/* ------------------------------------------------------------------------- */
+/* LSD radix sort of (uint32 key, int value) pairs, 8-bit digits, stable.     */
+/* One 4096-key tile per block: histogram -> per-digit scan over tiles ->    */
+/* stable in-tile ranking (warp match + per-warp digit counts) and scatter.  */
+/* ------------------------------------------------------------------------- */
+__global__ void __launch_bounds__(256) k_rs_hist(const uint32_t *keys, int64_t n, int shift, int *counts,
+                                                  int ntiles, const int *gate) {
+    if (gate_closed(gate)) return;
+    __shared__ int h[256];
+    h[threadIdx.x] = 0;
+    __syncthreads();
+    const int64_t base = int64_t(blockIdx.x) * SORT_TILE;
+#pragma unroll 4
+    for (int k = 0; k < SORT_TILE / 256; ++k) {
+        const int64_t idx = base + k * 256 + threadIdx.x;
+        if (idx < n) atomicAdd(&h[(keys[idx] >> shift) & 255u], 1);
+    }
+    __syncthreads();
+    counts[int64_t(threadIdx.x) * ntiles + blockIdx.x] = h[threadIdx.x];
+}
+
+__global__ void __launch_bounds__(1024) k_rs_scan(int *counts, int ntiles, int *digit_total, const int *gate) {
+    if (gate_closed(gate)) return;
+    __shared__ int wsum[32];
+    __shared__ int carry;
+    int *row = counts + int64_t(blockIdx.x) * ntiles;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int base = 0; base < ntiles; base += 1024) {
+        const int i = base + threadIdx.x;
+        const int v = i < ntiles ? row[i] : 0;
+        int x = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) wsum[warp] = x;
+        __syncthreads();
+        if (warp == 0) {
+            int s = wsum[lane];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, s, o);
+                if (lane >= o) s += y;
+            }
+            wsum[lane] = s;
+        }
+        __syncthreads();
+        const int incl = x + (warp > 0 ? wsum[warp - 1] : 0);
+        const int c0 = carry;
+        if (i < ntiles) row[i] = c0 + incl - v;
+        __syncthreads();
+        if (threadIdx.x == 1023) carry = c0 + incl;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) digit_total[blockIdx.x] = carry;
+}
+
+__global__ void __launch_bounds__(256) k_rs_scatter(const uint32_t *kin, const int *vin, uint32_t *kout, int *vout,
+                                                     int64_t n, int shift, const int *counts, int ntiles,
+                                                     const int *digit_total, int *inv, const int *gate) {
+    if (gate_closed(gate)) return;
+    __shared__ int base_s[256];
+    __shared__ int run[256];
+    __shared__ int wcnt[8][256];
+    __shared__ int wsum[8];
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    // exclusive scan of the digit totals -> global digit base
+    {
+        const int v = digit_total[t];
+        int x = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) wsum[warp] = x;
+        __syncthreads();
+        int off = 0;
+        for (int w = 0; w < warp; ++w) off += wsum[w];
+        base_s[t] = off + x - v + counts[int64_t(t) * ntiles + blockIdx.x];
+        run[t] = 0;
+    }
+    const unsigned lt = (1u << lane) - 1u;
+    const int64_t tb = int64_t(blockIdx.x) * SORT_TILE;
+    for (int r = 0; r < SORT_TILE / 256; ++r) {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) wcnt[k][t] = 0;
+        __syncthreads();
+        const int64_t idx = tb + r * 256 + t;
+        const bool valid = idx < n;
+        const uint32_t key = valid ? kin[idx] : 0u;
+        const int val = valid ? vin[idx] : 0;
+        const int dg = valid ? int((key >> shift) & 255u) : 256;
+        const unsigned peers = __match_any_sync(0xffffffffu, dg);
+        const int rank = __popc(peers & lt);
+        if (valid && lane == __ffs(peers) - 1) wcnt[warp][dg] = __popc(peers);
+        __syncthreads();
+        {
+            int acc = run[t];
+#pragma unroll
+            for (int w = 0; w < 8; ++w) {
+                const int c = wcnt[w][t];
+                wcnt[w][t] = acc;
+                acc += c;
+            }
+            run[t] = acc;
+        }
+        __syncthreads();
+        if (valid) {
+            const int pos = base_s[dg] + wcnt[warp][dg] + rank;
+            kout[pos] = key;
+            vout[pos] = val;
+            if (inv) inv[val] = pos;
+        }
+        __syncthreads();
+    }
+}
+
+int sort_tiles(int64_t n) { return int((n + SORT_TILE - 1) / SORT_TILE); }
+
+int radix_sort_pairs(uint32_t *keys[2], int *vals[2], int *counts, int *digit_total, int *inv, int64_t n,
+                     int passes, int ntiles, const int *gate, cudaStream_t st) {
+    int cur = 0;
+    for (int p = 0; p < passes; ++p) {
+        const int shift = 8 * p;
+        k_rs_hist<<<ntiles, 256, 0, st>>>(keys[cur], n, shift, counts, ntiles, gate);
+        k_rs_scan<<<256, 1024, 0, st>>>(counts, ntiles, digit_total, gate);
+        k_rs_scatter<<<ntiles, 256, 0, st>>>(keys[cur], vals[cur], keys[1 - cur], vals[1 - cur], n, shift, counts,
+                                             ntiles, digit_total, p == passes - 1 ? inv : nullptr, gate);
+        cur = 1 - cur;
+    }
+    return cur;
+}
+
+/* ------------------------------------------------------------------------- */
+/* Rebuild chain                                                             */
+/* ------------------------------------------------------------------------- */
+template<class R> __global__ void __launch_bounds__(256) k_rebin(KArgs<R> a, int gated) {
+    using T4 = typename Vec<R>::T4;
+    if (gated && !__ldcg(&a.S->rebuild)) return;
+    const int cur = __ldcg(&a.S->cur), lp = __ldcg(&a.S->lp);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        a.S->max_nnb = 0;
+        a.S->out_of_grid = 0;
+    }
+    int out = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.npad; i += gridDim.x * blockDim.x) {
+        const SysDev &sd = a.sys[a.blk_sys[i / SYS_PAD]];
+        T4 p = a.pos[cur][i];
+        const int w = wbits(p.w);
+        uint32_t key;
+        if (w_type(w) == GHOST) {
+            key = sd.cell_base + ncell_of(sd);
+        } else {
+            const int c = a.cell[lp][i];
+            int cc[3] = {cx_of(c), cy_of(c), cz_of(c)};
+            a.ranges[sd.cell_base + cell_lin(sd, cc[0], cc[1], cc[2])] = make_int2(0, 0);
+            R o[3] = {p.x, p.y, p.z};
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                const R L = R(sd.Lc[d]);
+                const R invL = R(1.0 / sd.Lc[d]);
+                const int k = int(floor(add_rn(mul_rn(o[d], invL), R(0.5))));
+                int nc = cc[d] + k;
+                if (sd.per[d]) {
+                    o[d] = sub_rn(o[d], mul_rn(R(k), L));
+                    nc %= sd.nc[d];
+                    if (nc < 0) nc += sd.nc[d];
+                } else {
+                    const int cl = min(max(nc, 0), sd.nc[d] - 1);
+                    if (cl != nc) out = 1;
+                    o[d] = sub_rn(o[d], mul_rn(R(cl - cc[d]), L));
+                    nc = cl;
+                }
+                cc[d] = nc;
+            }
+            p.x = o[0];
+            p.y = o[1];
+            p.z = o[2];
+            a.pos[cur][i] = p;
+            a.xref[lp][i] = p;
+            a.cell[lp][i] = cpack(cc[0], cc[1], cc[2]);
+            key = sd.cell_base + cell_lin(sd, cc[0], cc[1], cc[2]);
+        }
+        a.skey[0][i] = key;
+        a.sval[0][i] = i;
+    }
+    if (out) {
+        atomicOr(&a.S->error, ERRB_GRID);
+        atomicAdd(&a.S->out_of_grid, 1);
+    }
+}
+
+template<class R> __global__ void __launch_bounds__(256) k_ranges_gather(KArgs<R> a, int fin, int gated) {
+    if (gated && !__ldcg(&a.S->rebuild)) return;
+    const int cur = __ldcg(&a.S->cur), lp = __ldcg(&a.S->lp);
+    const int nc = 1 - cur, nl = 1 - lp;
+    const uint32_t *sk = a.skey[fin];
+    const int *sv = a.sval[fin];
+    const int n = a.npad;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+        const uint32_t k = sk[p];
+        if (p == 0 || sk[p - 1] != k) a.ranges[k].x = p;
+        if (p == n - 1 || sk[p + 1] != k) a.ranges[k].y = p + 1;
+        const int src = sv[p];
+        const auto ps = a.pos[cur][src];
+        a.pos[nc][p] = ps;
+        a.nrm[nc][p] = a.nrm[cur][src];
+        a.vel[nl][p] = a.vel[lp][src];
+        a.omg[nl][p] = a.omg[lp][src];
+        a.frc[nl][p] = a.frc[lp][src];
+        a.trq[nl][p] = a.trq[lp][src];
+        a.xref[nl][p] = a.xref[lp][src];
+        a.cell[nl][p] = a.cell[lp][src];
+        a.tag[nl][p] = a.tag[lp][src];
+        const int h = a.home[lp][src];
+        a.home[nl][p] = h;
+        if (h >= 0) a.slot_of_home[h] = p;
+        const int w = wbits(ps.w);
+        const int bd = w_bdeg(w), fd = w_fdeg(w);
+        for (int b = 0; b < bd; ++b) {
+            BondSlot s = a.bond[lp][int64_t(b) * n + src];
+            s.partner = a.inv[s.partner];
+            a.bond[nl][int64_t(b) * n + p] = s;
+        }
+        for (int b = 0; b < fd; ++b) {
+            int2 s = a.fslot[lp][int64_t(b) * n + src];
+            s.x = a.inv[s.x];
+            s.y = a.inv[s.y];
+            a.fslot[nl][int64_t(b) * n + p] = s;
+        }
+    }
+    for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < a.nfaces; f += gridDim.x * blockDim.x) {
+        int4 q = a.faces[f];
+        q.x = a.inv[q.x];
+        q.y = a.inv[q.y];
+        q.z = a.inv[q.z];
+        a.faces[f] = q;
+    }
+}
+
+template<class R> __global__ void __launch_bounds__(256) k_nlist(KArgs<R> a, int gated) {
+    using T4 = typename Vec<R>::T4;
+    if (gated && !__ldcg(&a.S->rebuild)) return;
+    __shared__ float rl2s[256];
+    rl2s[threadIdx.x] = __ldg(&a.ff->rlist2[threadIdx.x]);
+    if (blockDim.x < 256 && threadIdx.x + blockDim.x < 256)
+        rl2s[threadIdx.x + blockDim.x] = __ldg(&a.ff->rlist2[threadIdx.x + blockDim.x]);
+    __syncthreads();
+    const int cur = 1 - __ldcg(&a.S->cur), lp = 1 - __ldcg(&a.S->lp);
+    const int n = a.npad;
+    int maxc = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const T4 p = a.pos[cur][i];
+        const int ty = w_type(wbits(p.w));
+        if (ty == GHOST) {
+            a.nnb[i] = 0;
+            continue;
+        }
+        const SysDev &sd = a.sys[a.blk_sys[i / SYS_PAD]];
+        const int c = a.cell[lp][i];
+        const int cc[3] = {cx_of(c), cy_of(c), cz_of(c)};
+        const R L[3] = {R(sd.Lc[0]), R(sd.Lc[1]), R(sd.Lc[2])};
+        int count = 0;
+        for (int dz = -1; dz <= 1; ++dz) {
+            int z = cc[2] + dz;
+            if (sd.per[2]) {
+                z = z < 0 ? z + sd.nc[2] : (z >= sd.nc[2] ? z - sd.nc[2] : z);
+            } else if (z < 0 || z >= sd.nc[2]) {
+                continue;
+            }
+            for (int dy = -1; dy <= 1; ++dy) {
+                int y = cc[1] + dy;
+                if (sd.per[1]) {
+                    y = y < 0 ? y + sd.nc[1] : (y >= sd.nc[1] ? y - sd.nc[1] : y);
+                } else if (y < 0 || y >= sd.nc[1]) {
+                    continue;
+                }
+                for (int dx = -1; dx <= 1; ++dx) {
+                    int x = cc[0] + dx;
+                    if (sd.per[0]) {
+                        x = x < 0 ? x + sd.nc[0] : (x >= sd.nc[0] ? x - sd.nc[0] : x);
+                    } else if (x < 0 || x >= sd.nc[0]) {
+                        continue;
+                    }
+                    const uint32_t code = uint32_t((dx + 1) + 3 * (dy + 1) + 9 * (dz + 1));
+                    // x_i - x_j = (o_i - o_j) - d * Lc
+                    const R sx = mul_rn(R(-dx), L[0]), sy = mul_rn(R(-dy), L[1]), sz = mul_rn(R(-dz), L[2]);
+                    const int2 rg = a.ranges[sd.cell_base + cell_lin(sd, x, y, z)];
+                    for (int j = rg.x; j < rg.y; ++j) {
+                        if (j == i) continue;
+                        const T4 q = a.pos[cur][j];
+                        const int tj = w_type(wbits(q.w));
+                        const float rl2 = rl2s[ty * 16 + tj];
+                        if (!(rl2 > 0.f)) continue;
+                        const R ex = add_rn(sub_rn(p.x, q.x), sx);
+                        const R ey = add_rn(sub_rn(p.y, q.y), sy);
+                        const R ez = add_rn(sub_rn(p.z, q.z), sz);
+                        const R r2 = add_rn(add_rn(mul_rn(ex, ex), mul_rn(ey, ey)), mul_rn(ez, ez));
+                        if (r2 < R(rl2)) {
+                            if (count < a.cap) a.nbr[int64_t(count) * n + i] = uint32_t(j) | (code << NB_SHIFT);
+                            ++count;
+                        }
+                    }
+                }
+            }
+        }
+        a.nnb[i] = min(count, a.cap);
+        maxc = max(maxc, count);
+    }
+    // block max -> global max; last block finalises the rebuild
+    __shared__ int smax[8];
+    __shared__ bool last;
+    int m = maxc;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) smax[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int bm = 0;
+        for (int w = 0; w < int(blockDim.x >> 5); ++w) bm = max(bm, smax[w]);
+        atomicMax(&a.S->max_nnb, bm);
+        if (bm > a.cap) atomicOr(&a.S->error, ERRB_NBR_OVERFLOW);
+        __threadfence();
+        const unsigned ticket = atomicAdd(&a.S->blk_counter, 1u);
+        last = (ticket == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (last && threadIdx.x == 0) {
+        a.S->cur = cur;
+        a.S->lp = lp;
+        a.S->rebuild = 0;
+        a.S->rebuilds += 1;
+        a.S->since_rebuild = 0;
+        a.S->blk_counter = 0;
+        __threadfence();
+    }
+}
+
+static int grid_for(int64_t n, int per_block = 256) {
+    int64_t g = (n + per_block - 1) / per_block;
+    const int64_t cap = 152 * 8;
+    return int(g < 1 ? 1 : (g > cap ? cap : g));
+}
+
+template<class R> void launch_rebuild(const KArgs<R> &a, cudaStream_t st, bool gated) {
+    const int g = grid_for(a.npad);
+    k_rebin<R><<<g, 256, 0, st>>>(a, gated ? 1 : 0);
+    const int fin = radix_sort_pairs(const_cast<uint32_t **>(a.skey), const_cast<int **>(a.sval), a.counts,
+                                     a.digit_total, a.inv, a.npad, a.sort_passes, a.ntiles,
+                                     gated ? &a.S->rebuild : nullptr, st);
+    k_ranges_gather<R><<<g, 256, 0, st>>>(a, fin, gated ? 1 : 0);
+    k_nlist<R><<<grid_for(a.npad, 128), 128, 0, st>>>(a, gated ? 1 : 0);
+}
+
+/* ------------------------------------------------------------------------- */
+/* State conversion                                                          */
+/* ------------------------------------------------------------------------- */
+template<class R>
+__global__ void k_set_state(KArgs<R> a, const double *x, const double *nv, const double *v, const double *o,
+                            int64_t nhome) {
+    using T4 = typename Vec<R>::T4;
+    const int cur = __ldcg(&a.S->cur), lp = __ldcg(&a.S->lp);
+    int out = 0;
+    for (int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; k < nhome; k += int64_t(gridDim.x) * blockDim.x) {
+        const int p = a.slot_of_home[k];
+        const SysDev &sd = a.sys[a.blk_sys[p / SYS_PAD]];
+        T4 q = a.pos[cur][p];
+        {
+            const int c0 = a.cell[lp][p];  // the next rebin clears only the new cells
+            a.ranges[sd.cell_base + cell_lin(sd, cx_of(c0), cy_of(c0), cz_of(c0))] = make_int2(0, 0);
+        }
+        int cc[3];
+        R off[3];
+        for (int d = 0; d < 3; ++d) {
+            const double xd = x[3 * k + d];
+            const int cu = int(floor(__ddiv_rn(__dsub_rn(xd, sd.lo[d]), sd.Lc[d])));
+            int c = cu;
+            if (sd.per[d]) {
+                c %= sd.nc[d];
+                if (c < 0) c += sd.nc[d];
+            } else {
+                c = min(max(cu, 0), sd.nc[d] - 1);
+                if (c != cu) out = 1;
+            }
+            const int cref = sd.per[d] ? cu : c;
+            const double center = __dadd_rn(sd.lo[d], __dmul_rn(double(cref) + 0.5, sd.Lc[d]));
+            off[d] = R(__dsub_rn(xd, center));
+            cc[d] = c;
+        }
+        q.x = off[0];
+        q.y = off[1];
+        q.z = off[2];
+        a.pos[cur][p] = q;
+        a.xref[lp][p] = q;
+        a.cell[lp][p] = cpack(cc[0], cc[1], cc[2]);
+        T4 t = a.nrm[cur][p];
+        t.x = R(nv[3 * k]);
+        t.y = R(nv[3 * k + 1]);
+        t.z = R(nv[3 * k + 2]);
+        a.nrm[cur][p] = t;
+        t = a.vel[lp][p];
+        t.x = R(v[3 * k]);
+        t.y = R(v[3 * k + 1]);
+        t.z = R(v[3 * k + 2]);
+        a.vel[lp][p] = t;
+        t = a.omg[lp][p];
+        t.x = R(o[3 * k]);
+        t.y = R(o[3 * k + 1]);
+        t.z = R(o[3 * k + 2]);
+        a.omg[lp][p] = t;
+    }
+    if (out) atomicOr(&a.S->error, ERRB_GRID);
+    if (blockIdx.x == 0 && threadIdx.x == 0) a.S->rebuild = 1;
+}
+
+template<class R> void launch_set_state(const KArgs<R> &a, const double *x, const double *n, const double *v,
+                                        const double *o, int64_t nhome, cudaStream_t st) {
+    k_set_state<R><<<grid_for(nhome), 256, 0, st>>>(a, x, n, v, o, nhome);
+}
+
+template<class R>
+__global__ void k_download(KArgs<R> a, double *x, double *nv, double *v, double *o, double *f, double *t,
+                           double *e) {
+    using T4 = typename Vec<R>::T4;
+    const int cur = __ldcg(&a.S->cur), lp = __ldcg(&a.S->lp);
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < a.npad; p += gridDim.x * blockDim.x) {
+        const int h = a.home[lp][p];
+        if (h < 0) continue;
+        const SysDev &sd = a.sys[a.blk_sys[p / SYS_PAD]];
+        if (x) {
+            const T4 q = a.pos[cur][p];
+            const int c = a.cell[lp][p];
+            const int cc[3] = {cx_of(c), cy_of(c), cz_of(c)};
+            const double off[3] = {double(q.x), double(q.y), double(q.z)};
+            for (int d = 0; d < 3; ++d)
+                x[3 * int64_t(h) + d] = __dadd_rn(__dadd_rn(sd.lo[d], __dmul_rn(double(cc[d]) + 0.5, sd.Lc[d])), off[d]);
+        }
+        auto put = [&](double *dst, const T4 &q) {
+            if (!dst) return;
+            dst[3 * int64_t(h)] = double(q.x);
+            dst[3 * int64_t(h) + 1] = double(q.y);
+            dst[3 * int64_t(h) + 2] = double(q.z);
+        };
+        if (nv) put(nv, a.nrm[cur][p]);
+        if (v) put(v, a.vel[lp][p]);
+        if (o) put(o, a.omg[lp][p]);
+        if (f) put(f, a.frc[lp][p]);
+        if (t) put(t, a.trq[lp][p]);
+        if (e) e[h] = a.epart[p];
+    }
+}
+
+template<class R> void launch_download(const KArgs<R> &a, double *x, double *n, double *v, double *o, double *f,
+                                       double *t, double *e, cudaStream_t st) {
+    k_download<R><<<grid_for(a.npad), 256, 0, st>>>(a, x, n, v, o, f, t, e);
+}
+
+__global__ void k_set_cond(cudaGraphConditionalHandle h, const Scalars *S) {
+    cudaGraphSetConditional(h, __ldcg(&S->rebuild) ? 1u : 0u);
+}
+void launch_set_cond(cudaGraphConditionalHandle h, Scalars *S, cudaStream_t st) {
+    k_set_cond<<<1, 1, 0, st>>>(h, S);
+}
+
+/* ------------------------------------------------------------------------- */
+/* Reference Morton key (src/reorder_morton.h:25-42).                        */
+/* ------------------------------------------------------------------------- */
+__device__ __forceinline__ uint32_t bit_space3(uint32_t x) {
+    x = (x | (x << 12)) & 0x00FC003Fu;
+    x = (x | (x << 6)) & 0x381C0E07u;
+    x = (x | (x << 4)) & 0x190C8643u;
+    x = (x | (x << 2)) & 0x49249249u;
+    return x;
+}
+__global__ void k_morton(const double *p3, int64_t n, double b0, double b1, double b2, uint32_t *keys) {
+    for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+        const uint32_t cx = __double2uint_rz(__dadd_rn(2.0 * p3[3 * i], b0));
+        const uint32_t cy = __double2uint_rz(__dadd_rn(2.0 * p3[3 * i + 1], b1));
+        const uint32_t cz = __double2uint_rz(__dadd_rn(2.0 * p3[3 * i + 2], b2));
+        keys[i] = bit_space3(cx) | (bit_space3(cy) << 1) | (bit_space3(cz) << 2);
+    }
+}
+void launch_morton(const double *p3, int64_t n, const double *b, uint32_t *keys, cudaStream_t st) {
+    k_morton<<<grid_for(n), 256, 0, st>>>(p3, n, b[0], b[1], b[2], keys);
+}
+
+template void launch_rebuild<float>(const KArgs<float> &, cudaStream_t, bool);
+template void launch_rebuild<double>(const KArgs<double> &, cudaStream_t, bool);
+template void launch_set_state<float>(const KArgs<float> &, const double *, const double *, const double *,
+                                      const double *, int64_t, cudaStream_t);
+template void launch_set_state<double>(const KArgs<double> &, const double *, const double *, const double *,
+                                       const double *, int64_t, cudaStream_t);
+template void launch_download<float>(const KArgs<float> &, double *, double *, double *, double *, double *, double *,
+                                     double *, cudaStream_t);
+template void launch_download<double>(const KArgs<double> &, double *, double *, double *, double *, double *,
+                                      double *, double *, cudaStream_t);
+
+}  // namespace orbc

@@ -1,0 +1,175 @@
+// Device-side data layout shared by the kernels and the host engine.
+//
+// Particle state lives on the GPU in "slots": each system (one cell, one
+// vesicle, one lattice) owns a contiguous slot range padded to a multiple of
+// SYS_PAD so that every 256-slot block belongs to exactly one system.  Padding
+// slots are ghosts (type GHOST) that never enter a cell or a neighbour list.
+//
+// Positions are stored as an integer grid cell (packed 11/11/10 bits) plus an
+// offset from that cell's centre in the working precision R (float for the
+// mixed form, double for the plain FP64 form).  Neighbour-list entries carry
+// the cell shift between the two particles (27 codes, periodic images
+// included), so a pair separation is (o_i - o_j) + shift * Lc without ever
+// forming an absolute coordinate.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace orbc {
+
+constexpr int NT = 6;            // particle types (src/forcefield_canonical.h:31-37)
+constexpr int GHOST = 15;        // type of padding slots
+constexpr int SYS_PAD = 256;     // slot padding per system == step-kernel block
+constexpr int MAX_BT = 8;        // bond types
+constexpr int MAX_DEG = 15;      // bonds / faces per particle (4-bit fields)
+constexpr uint32_t NB_MASK = (1u << 27) - 1u;
+constexpr int NB_SHIFT = 27;
+constexpr int MAX_SLOTS = 1 << 27;
+constexpr int NPART = 4;         // per-block partial sums: ke2, epot, maxd2, flags
+
+enum : int {
+    ERRB_NBR_OVERFLOW = 1,  // a neighbour list overflowed its capacity
+    ERRB_NAN = 2,           // non-finite coordinate after a step
+    ERRB_GRID = 4,          // particle outside an open grid (clamped to the edge cell)
+    ERRB_BOND = 8,          // FENE / WLC bond beyond its maximum extension
+};
+
+enum : int { BOND_HARMONIC = 0, BOND_FENE = 1, BOND_WLC_POW = 2 };
+enum : int { PAIR_NONE = 0, PAIR_ANISO = 1, PAIR_REP = 2 };
+
+struct __align__(32) double4a {
+    double x, y, z, w;
+};
+template<class R> struct Vec;
+template<> struct Vec<float> {
+    using T4 = float4;
+};
+template<> struct Vec<double> {
+    using T4 = double4a;
+};
+
+// w word of a position record: type (4 bits) | bond degree << 4 | face degree << 8
+__host__ __device__ inline int w_type(int w) { return w & 15; }
+__host__ __device__ inline int w_bdeg(int w) { return (w >> 4) & 15; }
+__host__ __device__ inline int w_fdeg(int w) { return (w >> 8) & 15; }
+
+__device__ __forceinline__ int wbits(float w) { return __float_as_int(w); }
+__device__ __forceinline__ int wbits(double w) { return int(__double_as_longlong(w)); }
+__device__ __forceinline__ void wset(float &w, int b) { w = __int_as_float(b); }
+__device__ __forceinline__ void wset(double &w, int b) { w = __longlong_as_double((long long)(unsigned)b); }
+
+// packed cell coordinates (x: 11 bits, y: 11 bits, z: 10 bits)
+__host__ __device__ inline int cpack(int x, int y, int z) { return x | (y << 11) | (z << 22); }
+__host__ __device__ inline int cx_of(int c) { return c & 2047; }
+__host__ __device__ inline int cy_of(int c) { return (c >> 11) & 2047; }
+__host__ __device__ inline int cz_of(int c) { return (c >> 22) & 1023; }
+constexpr int MAX_NC_XY = 2047, MAX_NC_Z = 1023;
+
+struct BondSlot {
+    int partner;  // slot of the other end
+    int type;     // bond type (table index)
+    double r0;    // rest length
+};
+
+template<class R> struct PairP {
+    R cutsq, cut, rep8, att4, alpha, aatt, ljcutsq, lj1, lj2, rep, att, pad;
+    int kind;
+    int pad2;
+};
+
+template<class R> struct BondP {
+    R K, Rm;
+    int style, pad;
+};
+
+template<class R> struct FFDev {
+    PairP<R> pair[NT * NT];        // by (ti * NT + tj)
+    R mass[NT], inv_mass[NT], gamma[NT], sigma[NT];
+    BondP<R> bond[MAX_BT];
+    float rlist2[16 * 16];          // neighbour-list cutoff^2 (cut + skin)^2, 0 = never
+};
+
+struct SysDev {
+    double lo[3], Lc[3];            // grid origin and cell size
+    double wlo[3], whi[3];          // reflective walls (Nose-Hoover bounce-back)
+    int nc[3], per[3];
+    unsigned cell_base;             // first global cell id; ncell + 1 ids (last = ghost cell)
+    int off, npad, nreal;
+    int face_begin, face_end;
+    int pad0;
+    double kv, V0, ka, A0, Q;
+};
+
+struct SysState {
+    double zeta;        // Nose-Hoover thermostat variable
+    double ke2;         // sum m v^2 after the last integration
+    double epot;        // potential energy (when accumulated)
+    double area, volume;
+    double cv, ca;      // constraint coefficients -k (Q - Q0) / Q0 used by the next forces
+    double pad;
+};
+
+struct Scalars {
+    int cur, lp, rebuild, error;
+    int max_nnb, out_of_grid, cond_hint, pad0;
+    unsigned int blk_counter, pad1, pad2, pad3;
+    long long step, rebuilds, since_rebuild, pad4;
+};
+
+template<class R> struct KArgs {
+    using T4 = typename Vec<R>::T4;
+    // particle arrays; pos/nrm ping-pong on Scalars::cur, the rest on Scalars::lp
+    T4 *pos[2], *nrm[2], *vel[2], *omg[2], *frc[2], *trq[2], *xref[2];
+    int *cell[2], *tag[2], *home[2];
+    BondSlot *bond[2];
+    int2 *fslot[2];
+    double *epart;           // per-slot energy (forces hook)
+    int4 *faces;             // (a, b, c, sys) slots of the area/volume mesh
+    int nfaces;
+    uint32_t *nbr;           // ELL neighbour list [cap][npad]
+    int *nnb;
+    int cap;
+    int2 *ranges;            // cell -> [begin, end) of its slots
+    int *slot_of_home;
+    int *blk_sys;            // system of each 256-slot block
+    double *partial;         // [nblk][NPART]
+    Scalars *S;
+    SysDev *sys;
+    SysState *ss;
+    int nsys, npad, nblk;
+    // radix sort scratch
+    uint32_t *skey[2];
+    int *sval[2];
+    int *counts, *digit_total, *inv;
+    int sort_passes, ntiles;
+    // parameters
+    double dt, kBT;
+    R skin_half2;
+    uint64_t seed;
+    int rebuild_every;
+    int pad_i;
+    const FFDev<R> *ff;      // force-field tables (global; staged into shared memory per block)
+};
+
+// host-side launchers (explicitly instantiated for float and double)
+template<class R> void launch_rebuild(const KArgs<R> &a, cudaStream_t st, bool gated);
+template<class R> void launch_mesh(const KArgs<R> &a, cudaStream_t st);
+template<class R> void launch_step_langevin(const KArgs<R> &a, cudaStream_t st, bool energy);
+template<class R> void launch_nh_final(const KArgs<R> &a, cudaStream_t st, bool energy);
+template<class R> void launch_nh_initial(const KArgs<R> &a, cudaStream_t st);
+template<class R> void launch_nh_prologue(const KArgs<R> &a, cudaStream_t st);
+template<class R> void launch_forces(const KArgs<R> &a, cudaStream_t st);
+template<class R> void launch_set_state(const KArgs<R> &a, const double *x, const double *n, const double *v,
+                                        const double *o, int64_t nhome, cudaStream_t st);
+template<class R> void launch_download(const KArgs<R> &a, double *x, double *n, double *v, double *o, double *f,
+                                       double *t, double *e, cudaStream_t st);
+void launch_set_cond(cudaGraphConditionalHandle h, Scalars *S, cudaStream_t st);
+void launch_morton(const double *p3, int64_t n, const double *bsize3, uint32_t *keys, cudaStream_t st);
+// LSD radix sort of (key, index) pairs, stable; returns the buffer index (0/1) holding the result.
+int radix_sort_pairs(uint32_t *keys[2], int *vals[2], int *counts, int *digit_total, int *inv, int64_t n,
+                     int passes, int ntiles, const int *gate, cudaStream_t st);
+int sort_tiles(int64_t n);
+constexpr int SORT_TILE = 4096;
+
+}  // namespace orbc

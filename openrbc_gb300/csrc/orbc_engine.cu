@@ -1,0 +1,1259 @@
+// Host engine of liborbc_gpu: builds the device layout from the caller's
+// containers, owns every device buffer, sequences the kernels of one step
+// (captured once into a CUDA graph whose neighbour rebuild sits behind a
+// device-set conditional node), and implements the C ABI of orbc_gpu.h.
+#include "orbc_device.cuh"
+#include "orbc_gpu.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+namespace orbc {
+
+static thread_local std::string g_last_error;
+
+/* ------------------------------------------------------------------------- */
+/* Force field in FP64 (src/forcefield_canonical.h:23-156).                  */
+/* ------------------------------------------------------------------------- */
+struct FFHost {
+    double mass[NT], radius[NT];
+    double cutsq[NT * NT], cut[NT * NT], rep[NT * NT], att[NT * NT], alpha[NT * NT];
+    double ljcutsq[NT * NT], lj1[NT * NT], lj2[NT * NT];
+    int kind[NT * NT];
+    double range[NT * NT];  // interaction range of the type pair (0 = none)
+    FFHost() {
+        const double m[NT] = {1, 4, 4, 1, 10, 10};
+        const double rad[NT] = {0.56125, 1.12375, 1.12375, 0.56125, 1.5, 0.5};
+        // lipid-protein row (by protein type) and protein-protein block (types 1..3)
+        const double cl[NT] = {2.6, 2.6, 2.6, 2.6, 0, 0};
+        const double rl[NT] = {1.1225, 1.685, 1.685, 1.1225, 0, 0};
+        const double el[NT] = {1.2, 1.4, 2.8, 2.8, 0, 0};
+        const double al[NT] = {1.55, 5, 5, 5, 0, 0};
+        const double rp[4][4] = {{1.1225, 1.685, 1.685, 1.1225}, {1.685, 2.245, 2.245, 1.685},
+                                 {1.685, 2.245, 2.245, 1.685}, {1.1225, 1.685, 1.685, 1.1225}};
+        const double ep[4][4] = {{1.2, 1.4, 2.8, 2.8}, {1.4, 1, 1, 1}, {2.8, 1, 1, 1}, {2.8, 1, 1, 1}};
+        const double lje[NT * NT] = {0, 0, 0, 0, 1, 1, 0, 0, 0, 0, 1, 1, 0, 0, 0, 0, 1, 1,
+                                     0, 0, 0, 0, 0, 0, 1, 1, 1, 0, 0, 0, 1, 1, 1, 0, 0, 0};
+        const double ljs[NT * NT] = {0, 0, 0, 0, 1, 1, 0, 0, 0, 0, 3.4, 3.4, 0, 0, 0, 0, 3.4, 1,
+                                     0, 0, 0, 0, 0, 0, 1, 3.4, 3.4, 0, 3, 1.8, 1, 3.4, 1, 0, 1.8, 1};
+        const double w = 3.4 * 1.1225;
+        const double ljc[NT * NT] = {0, 0, 0, 0, 1.1225, 1.1225, 0, 0, 0, 0, w, w, 0, 0, 0, 0, w, 1.1225,
+                                     0, 0, 0, 0, 0, 0, 1.1225, w, w, 0, 0, 0, 1.1225, w, 1.1225, 0, 0, 0};
+        auto pw = [](double b, int e) {
+            double p = 1;
+            for (int k = 0; k < e; ++k) p = b * p;
+            return p;
+        };
+        for (int t = 0; t < NT; ++t) {
+            mass[t] = m[t];
+            radius[t] = rad[t];
+        }
+        for (int ti = 0; ti < NT; ++ti)
+            for (int tj = 0; tj < NT; ++tj) {
+                const int k = ti * NT + tj;
+                double c = 0, req = 0, eps = 0, a = 0;
+                int lj_idx, kd;
+                if (ti == 0 || tj == 0) {  // lipid-lipid / lipid-protein: table index = protein type
+                    const int p = std::max(ti, tj);
+                    c = cl[p];
+                    req = rl[p];
+                    eps = el[p];
+                    a = al[p];
+                    kd = c > 0 ? PAIR_ANISO : PAIR_NONE;
+                    lj_idx = p;
+                } else {  // protein-protein: type12 = t1 + 6 t2
+                    lj_idx = ti + NT * tj;
+                    if (ti < 4 && tj < 4) {
+                        c = 2.6;
+                        req = rp[ti][tj];
+                        eps = ep[ti][tj];
+                        kd = PAIR_REP;
+                    } else {
+                        kd = PAIR_NONE;
+                    }
+                }
+                kind[k] = kd;
+                cut[k] = kd ? c : 0;
+                cutsq[k] = kd ? c * c : 0;
+                rep[k] = kd ? eps / pw(c - req, 8) : 0;
+                att[k] = kd == PAIR_ANISO ? -2.0 * eps / pw(c - req, 4) : 0;
+                alpha[k] = kd == PAIR_ANISO ? a : 0;
+                ljcutsq[k] = ljc[lj_idx] * ljc[lj_idx];
+                lj1[k] = 48.0 * lje[lj_idx] * std::pow(ljs[lj_idx], 12);
+                lj2[k] = 24.0 * lje[lj_idx] * std::pow(ljs[lj_idx], 6);
+                range[k] = std::sqrt(std::max(cutsq[k], ljcutsq[k]));
+            }
+    }
+};
+static const FFHost &ffh() {
+    static const FFHost f;
+    return f;
+}
+
+/* ------------------------------------------------------------------------- */
+template<class T> struct DevBuf {
+    T *p = nullptr;
+    size_t n = 0;
+    cudaError_t alloc(size_t count) {
+        release();
+        n = count;
+        if (count == 0) count = 1;
+        return cudaMalloc(&p, count * sizeof(T));
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    ~DevBuf() { release(); }
+};
+
+struct HostSys {
+    orbc_system_desc desc;
+    int64_t begin, end;  // caller index range
+};
+
+class EngineBase {
+   public:
+    virtual ~EngineBase() {}
+    std::string err;
+    orbc_params P;
+    int fail(int code, const std::string &msg) {
+        err = msg;
+        g_last_error = msg;
+        return code;
+    }
+    virtual int upload(int nsys, const orbc_system_desc *sys, const int64_t *offsets, const double *x3,
+                       const double *n3, const double *v3, const double *o3, const int *type, const int *tag, size_t n,
+                       const int *bonds3, const double *bond_r0, size_t nb, const int *faces3, size_t nf) = 0;
+    virtual int set_state(const double *x3, const double *n3, const double *v3, const double *o3) = 0;
+    virtual int step(int nsteps, orbc_thermo *out) = 0;
+    virtual int download(double *x3, double *n3, double *v3, double *o3) = 0;
+    virtual int forces(double *f3, double *t3, double *e) = 0;
+    virtual int thermo(int sys, orbc_thermo *out) = 0;
+    virtual int neighbors(int *counts, int *list, int64_t cap, int64_t *total) = 0;
+    virtual int cells(int sys, double *lo3, double *lc3, int *nc3, int *cell, double *off3, int *slot) = 0;
+    virtual int rebuild() = 0;
+    virtual int profile(int nsteps, orbc_profile *out) = 0;
+    double last_ms = 0;
+    int64_t last_launches = 0;
+};
+
+#define CK(x)                                                                                  \
+    do {                                                                                       \
+        cudaError_t e_ = (x);                                                                  \
+        if (e_ != cudaSuccess) return fail(ORBC_ERR_CUDA, std::string(#x) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+static int err_code_of(int bits) {
+    if (bits & ERRB_NBR_OVERFLOW) return ORBC_ERR_NBR_OVERFLOW;
+    if (bits & ERRB_NAN) return ORBC_ERR_NAN;
+    if (bits & ERRB_BOND) return ORBC_ERR_BOND;
+    if (bits & ERRB_GRID) return ORBC_ERR_GRID;
+    return ORBC_OK;
+}
+static int flag_bits(int bits) {
+    int f = 0;
+    if (bits & ERRB_NBR_OVERFLOW) f |= 1 << ORBC_ERR_NBR_OVERFLOW;
+    if (bits & ERRB_NAN) f |= 1 << ORBC_ERR_NAN;
+    if (bits & ERRB_BOND) f |= 1 << ORBC_ERR_BOND;
+    if (bits & ERRB_GRID) f |= 1 << ORBC_ERR_GRID;
+    return f;
+}
+
+template<class R> class Engine : public EngineBase {
+    using T4 = typename Vec<R>::T4;
+
+   public:
+    explicit Engine(const orbc_params &p) { P = p; }
+    ~Engine() override {
+        drop_graph();
+        if (ev0) cudaEventDestroy(ev0);
+        if (ev1) cudaEventDestroy(ev1);
+        if (st) cudaStreamDestroy(st);
+    }
+
+    int init() {
+        int ndev = 0;
+        if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(ORBC_ERR_NODEV, "no CUDA device");
+        CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        CK(cudaEventCreate(&ev0));
+        CK(cudaEventCreate(&ev1));
+        return ORBC_OK;
+    }
+
+    /* --------------------------------------------------------------------- */
+    int upload(int nsys, const orbc_system_desc *descs, const int64_t *offsets, const double *x3, const double *n3,
+               const double *v3, const double *o3, const int *type, const int *tag, size_t n_, const int *bonds3,
+               const double *bond_r0, size_t nb, const int *faces3, size_t nf) override {
+        const int64_t n = int64_t(n_);
+        if (nsys < 1 || n < 1 || !x3 || !n3 || !type || !tag) return fail(ORBC_ERR_ARG, "upload: empty system");
+        if (offsets[0] != 0 || offsets[nsys] != n) return fail(ORBC_ERR_ARG, "upload: offsets must span [0, n)");
+        for (int s = 0; s < nsys; ++s)
+            if (offsets[s + 1] <= offsets[s]) return fail(ORBC_ERR_ARG, "upload: empty system in batch");
+        for (int64_t i = 0; i < n; ++i) {
+            if (type[i] < 0 || type[i] >= NT) return fail(ORBC_ERR_ARG, "upload: particle type outside 0..5");
+            if (tag[i] < 0) return fail(ORBC_ERR_ARG, "upload: negative tag");
+        }
+        drop_graph();
+        nh_primed = false;
+        this->nsys = nsys;
+        nhome = n;
+        const FFHost &F = ffh();
+        // tag -> caller index
+        int maxtag = 0;
+        for (int64_t i = 0; i < n; ++i) maxtag = std::max(maxtag, tag[i]);
+        std::vector<int> t2i(size_t(maxtag) + 1, -1);
+        for (int64_t i = 0; i < n; ++i) {
+            if (t2i[size_t(tag[i])] >= 0) return fail(ORBC_ERR_ARG, "upload: duplicate tag");
+            t2i[size_t(tag[i])] = int(i);
+        }
+        auto idx_of = [&](int t) { return (t >= 0 && t <= maxtag) ? t2i[size_t(t)] : -1; };
+
+        // ---- per-system grid and slot layout
+        hsys.assign(size_t(nsys), SysDev());
+        std::vector<int> sys_of(static_cast<size_t>(n));
+        int64_t off = 0;
+        uint64_t cbase = 0;
+        for (int s = 0; s < nsys; ++s) {
+            SysDev &sd = hsys[size_t(s)];
+            std::memset(&sd, 0, sizeof(sd));
+            const orbc_system_desc &d = descs[s];
+            const int64_t b = offsets[s], e = offsets[s + 1];
+            bool present[NT] = {false, false, false, false, false, false};
+            for (int64_t i = b; i < e; ++i) {
+                present[type[i]] = true;
+                sys_of[size_t(i)] = s;
+            }
+            double rmax = 0;
+            for (int ta = 0; ta < NT; ++ta)
+                for (int tc = 0; tc < NT; ++tc)
+                    if (present[ta] && present[tc] && F.range[ta * NT + tc] > 0)
+                        rmax = std::max(rmax, F.range[ta * NT + tc]);
+            const double rl = (rmax > 0 ? rmax : 1.0) + P.skin;
+            for (int dd = 0; dd < 3; ++dd) {
+                const int maxnc = dd < 2 ? MAX_NC_XY : MAX_NC_Z;
+                sd.per[dd] = d.periodic[dd] ? 1 : 0;
+                if (sd.per[dd]) {
+                    const double L = d.hi[dd] - d.lo[dd];
+                    int nc = int(std::floor(L / rl));
+                    if (nc < 3) return fail(ORBC_ERR_ARG, "upload: periodic box shorter than 3 list cutoffs");
+                    nc = std::min(nc, maxnc);
+                    sd.nc[dd] = nc;
+                    sd.Lc[dd] = L / nc;
+                    sd.lo[dd] = d.lo[dd];
+                } else {
+                    double mn = 1e300, mx = -1e300;
+                    for (int64_t i = b; i < e; ++i) {
+                        mn = std::min(mn, x3[3 * i + dd]);
+                        mx = std::max(mx, x3[3 * i + dd]);
+                    }
+                    const double ext = mx - mn;
+                    const double margin = std::max(0.25 * ext, 4.0 * rl) + rl;
+                    double Lc = rl;
+                    int nc = int(std::ceil((ext + 2 * margin) / Lc));
+                    if (nc > maxnc) {
+                        nc = maxnc;
+                        Lc = (ext + 2 * margin) / nc;
+                    }
+                    sd.nc[dd] = std::max(nc, 1);
+                    sd.Lc[dd] = Lc;
+                    sd.lo[dd] = 0.5 * (mn + mx) - 0.5 * nc * Lc;
+                }
+                if (P.bounce && P.integrator == ORBC_INT_NOSE_HOOVER) {
+                    sd.wlo[dd] = d.lo[dd];
+                    sd.whi[dd] = d.hi[dd];
+                }
+            }
+            const int64_t ns = e - b;
+            const int64_t npad_s = std::max<int64_t>(SYS_PAD, (ns + SYS_PAD - 1) / SYS_PAD * SYS_PAD);
+            sd.off = int(off);
+            sd.npad = int(npad_s);
+            sd.nreal = int(ns);
+            sd.cell_base = unsigned(cbase);
+            sd.kv = d.kv;
+            sd.V0 = d.V0;
+            sd.ka = d.ka;
+            sd.A0 = d.A0;
+            sd.Q = P.Q;
+            off += npad_s;
+            cbase += uint64_t(sd.nc[0]) * sd.nc[1] * sd.nc[2] + 1;
+        }
+        if (off >= MAX_SLOTS) return fail(ORBC_ERR_ARG, "upload: more than 2^27 particle slots");
+        if (cbase >= (uint64_t(1) << 32) - 1) return fail(ORBC_ERR_ARG, "upload: more than 2^32 cells");
+        npad = int(off);
+        nblk = npad / SYS_PAD;
+        total_cells = cbase;
+
+        // ---- slots
+        std::vector<T4> hpos(static_cast<size_t>(npad)), hnrm(static_cast<size_t>(npad)), hvel(static_cast<size_t>(npad)), homg(static_cast<size_t>(npad)),
+            hzero(static_cast<size_t>(npad));
+        std::vector<int> hcell(size_t(npad), 0), htag(size_t(npad), -1), hhome(size_t(npad), -1),
+            hsoh(static_cast<size_t>(n)), hbs(static_cast<size_t>(nblk));
+        std::vector<int> wbitsv(size_t(npad), GHOST);
+        std::memset(hzero.data(), 0, hzero.size() * sizeof(T4));
+        for (int s = 0; s < nsys; ++s) {
+            const SysDev &sd = hsys[size_t(s)];
+            for (int b = sd.off / SYS_PAD; b < (sd.off + sd.npad) / SYS_PAD; ++b) hbs[size_t(b)] = s;
+            for (int64_t i = offsets[s]; i < offsets[s + 1]; ++i) {
+                const int p = sd.off + int(i - offsets[s]);
+                hhome[size_t(p)] = int(i);
+                hsoh[size_t(i)] = p;
+                htag[size_t(p)] = tag[i];
+                wbitsv[size_t(p)] = type[i];
+                int cc[3];
+                double o[3];
+                bin_point(sd, &x3[3 * i], cc, o);
+                hcell[size_t(p)] = cpack(cc[0], cc[1], cc[2]);
+                hpos[size_t(p)] = mk4(R(o[0]), R(o[1]), R(o[2]));
+                hnrm[size_t(p)] = mk4(R(n3[3 * i]), R(n3[3 * i + 1]), R(n3[3 * i + 2]));
+                hvel[size_t(p)] = v3 ? mk4(R(v3[3 * i]), R(v3[3 * i + 1]), R(v3[3 * i + 2])) : mk4(0, 0, 0);
+                homg[size_t(p)] = o3 ? mk4(R(o3[3 * i]), R(o3[3 * i + 1]), R(o3[3 * i + 2])) : mk4(0, 0, 0);
+            }
+        }
+        for (int p = 0; p < npad; ++p)
+            if (hhome[size_t(p)] < 0) {
+                hpos[size_t(p)] = mk4(0, 0, 0);
+                hnrm[size_t(p)] = mk4(0, 0, 1);
+                hvel[size_t(p)] = mk4(0, 0, 0);
+                homg[size_t(p)] = mk4(0, 0, 0);
+            }
+        // ---- bonds (ELL by slot, both ends)
+        std::vector<int> bdeg(size_t(npad), 0);
+        for (size_t l = 0; l < nb; ++l) {
+            const int bt = bonds3[3 * l], ki = idx_of(bonds3[3 * l + 1]), kj = idx_of(bonds3[3 * l + 2]);
+            if (bt < 0 || bt >= MAX_BT) return fail(ORBC_ERR_ARG, "upload: bond type outside 0..7");
+            if (ki < 0 || kj < 0) return fail(ORBC_ERR_ARG, "upload: bond endpoint tag not found");
+            if (ki == kj) return fail(ORBC_ERR_ARG, "upload: bond to itself");
+            if (sys_of[size_t(ki)] != sys_of[size_t(kj)]) return fail(ORBC_ERR_ARG, "upload: bond across systems");
+            bdeg[size_t(hsoh[size_t(ki)])]++;
+            bdeg[size_t(hsoh[size_t(kj)])]++;
+        }
+        maxb = 0;
+        for (int d : bdeg) maxb = std::max(maxb, d);
+        if (maxb > MAX_DEG) return fail(ORBC_ERR_ARG, "upload: more than 15 bonds on one particle");
+        std::vector<BondSlot> hb(size_t(std::max(maxb, 1)) * size_t(npad));
+        std::fill(bdeg.begin(), bdeg.end(), 0);
+        for (size_t l = 0; l < nb; ++l) {
+            const int bt = bonds3[3 * l];
+            const int pi = hsoh[size_t(idx_of(bonds3[3 * l + 1]))], pj = hsoh[size_t(idx_of(bonds3[3 * l + 2]))];
+            const double r0 = bond_r0 ? bond_r0[l] : P.bond_r0[bt];
+            hb[size_t(bdeg[size_t(pi)]++) * npad + size_t(pi)] = BondSlot{pj, bt, r0};
+            hb[size_t(bdeg[size_t(pj)]++) * npad + size_t(pj)] = BondSlot{pi, bt, r0};
+        }
+        // ---- faces
+        std::vector<int> fdeg(size_t(npad), 0);
+        std::vector<int4> hfaces;
+        hfaces.reserve(nf);
+        for (int s = 0; s < nsys; ++s) {
+            hsys[size_t(s)].face_begin = int(hfaces.size());
+            for (size_t k = 0; k < nf; ++k) {
+                int q[3];
+                for (int c = 0; c < 3; ++c) {
+                    const int ki = idx_of(faces3[3 * k + c]);
+                    if (ki < 0) return fail(ORBC_ERR_ARG, "upload: face vertex tag not found");
+                    q[c] = ki;
+                }
+                if (sys_of[size_t(q[0])] != s) continue;
+                if (sys_of[size_t(q[1])] != s || sys_of[size_t(q[2])] != s)
+                    return fail(ORBC_ERR_ARG, "upload: face across systems");
+                const int a = hsoh[size_t(q[0])], b = hsoh[size_t(q[1])], c = hsoh[size_t(q[2])];
+                hfaces.push_back(make_int4(a, b, c, s));
+                fdeg[size_t(a)]++;
+                fdeg[size_t(b)]++;
+                fdeg[size_t(c)]++;
+            }
+            hsys[size_t(s)].face_end = int(hfaces.size());
+        }
+        maxf = 0;
+        for (int d : fdeg) maxf = std::max(maxf, d);
+        if (maxf > MAX_DEG) return fail(ORBC_ERR_ARG, "upload: more than 15 faces on one vertex");
+        std::vector<int2> hfs(size_t(std::max(maxf, 1)) * size_t(npad));
+        std::fill(fdeg.begin(), fdeg.end(), 0);
+        for (const int4 &q : hfaces) {
+            hfs[size_t(fdeg[size_t(q.x)]++) * npad + size_t(q.x)] = make_int2(q.y, q.z);
+            hfs[size_t(fdeg[size_t(q.y)]++) * npad + size_t(q.y)] = make_int2(q.z, q.x);
+            hfs[size_t(fdeg[size_t(q.z)]++) * npad + size_t(q.z)] = make_int2(q.x, q.y);
+        }
+        for (int p = 0; p < npad; ++p) {
+            const int w = hhome[size_t(p)] < 0 ? GHOST : (wbitsv[size_t(p)] | (bdeg[size_t(p)] << 4) | (fdeg[size_t(p)] << 8));
+            setw(hpos[size_t(p)], w);
+        }
+        has_mesh = !hfaces.empty();
+        nfaces = int(hfaces.size());
+
+        // ---- device allocation
+        for (int k = 0; k < 2; ++k) {
+            if (pos[k].alloc(size_t(npad)) || nrm[k].alloc(size_t(npad)) || vel[k].alloc(size_t(npad)) ||
+                omg[k].alloc(size_t(npad)) || frc[k].alloc(size_t(npad)) || trq[k].alloc(size_t(npad)) ||
+                xref[k].alloc(size_t(npad)) || cell[k].alloc(size_t(npad)) || tagd[k].alloc(size_t(npad)) ||
+                home[k].alloc(size_t(npad)) || bond[k].alloc(hb.size()) || fslot[k].alloc(hfs.size()) ||
+                skey[k].alloc(size_t(npad)) || sval[k].alloc(size_t(npad)))
+                return fail(ORBC_ERR_NOMEM, "upload: device allocation failed");
+        }
+        ntiles = sort_tiles(npad);
+        if (epart.alloc(size_t(npad)) || faces.alloc(hfaces.size()) || ranges.alloc(size_t(total_cells)) ||
+            soh.alloc(size_t(n)) || blk_sys.alloc(size_t(nblk)) || partial.alloc(size_t(nblk) * NPART) ||
+            Sd.alloc(1) || sysd.alloc(size_t(nsys)) || ssd.alloc(size_t(nsys)) || counts.alloc(size_t(256) * ntiles) ||
+            dtot.alloc(256) || invd.alloc(size_t(npad)) || ffd.alloc(1) || nnb.alloc(size_t(npad)) ||
+            stage.alloc(size_t(n) * 12))
+            return fail(ORBC_ERR_NOMEM, "upload: device allocation failed");
+        cap = P.max_neighbors > 0 ? P.max_neighbors : 64;
+        if (nbr.alloc(size_t(cap) * size_t(npad))) return fail(ORBC_ERR_NOMEM, "upload: neighbour list allocation failed");
+
+        CK(cudaMemcpyAsync(pos[0].p, hpos.data(), hpos.size() * sizeof(T4), cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(nrm[0].p, hnrm.data(), hnrm.size() * sizeof(T4), cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(vel[0].p, hvel.data(), hvel.size() * sizeof(T4), cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(omg[0].p, homg.data(), homg.size() * sizeof(T4), cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(frc[0].p, hzero.data(), hzero.size() * sizeof(T4), cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(trq[0].p, hzero.data(), hzero.size() * sizeof(T4), cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(xref[0].p, hpos.data(), hpos.size() * sizeof(T4), cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(cell[0].p, hcell.data(), hcell.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(tagd[0].p, htag.data(), htag.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(home[0].p, hhome.data(), hhome.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(bond[0].p, hb.data(), hb.size() * sizeof(BondSlot), cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(fslot[0].p, hfs.data(), hfs.size() * sizeof(int2), cudaMemcpyHostToDevice, st));
+        if (!hfaces.empty())
+            CK(cudaMemcpyAsync(faces.p, hfaces.data(), hfaces.size() * sizeof(int4), cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(soh.p, hsoh.data(), hsoh.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(blk_sys.p, hbs.data(), hbs.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(sysd.p, hsys.data(), hsys.size() * sizeof(SysDev), cudaMemcpyHostToDevice, st));
+        CK(cudaMemsetAsync(ranges.p, 0, size_t(total_cells) * sizeof(int2), st));
+        CK(cudaMemsetAsync(partial.p, 0, size_t(nblk) * NPART * sizeof(double), st));
+        CK(cudaMemsetAsync(epart.p, 0, size_t(npad) * sizeof(double), st));
+        CK(cudaMemsetAsync(nnb.p, 0, size_t(npad) * sizeof(int), st));
+        // other parity copies start equal (gather overwrites them before use)
+        Scalars hs;
+        std::memset(&hs, 0, sizeof(hs));
+        hs.rebuild = 1;
+        CK(cudaMemcpyAsync(Sd.p, &hs, sizeof(hs), cudaMemcpyHostToDevice, st));
+        std::vector<SysState> hss(static_cast<size_t>(nsys));
+        std::memset(hss.data(), 0, hss.size() * sizeof(SysState));
+        for (int s = 0; s < nsys; ++s) hss[size_t(s)].zeta = descs[s].zeta;
+        CK(cudaMemcpyAsync(ssd.p, hss.data(), hss.size() * sizeof(SysState), cudaMemcpyHostToDevice, st));
+        build_ff();
+        CK(cudaMemcpyAsync(ffd.p, &hff, sizeof(hff), cudaMemcpyHostToDevice, st));
+        // key bits -> radix passes
+        int bits = 1;
+        while (bits < 32 && (uint64_t(1) << bits) < total_cells) ++bits;
+        passes = (bits + 7) / 8;
+        fill_args();
+        CK(cudaStreamSynchronize(st));
+        uploaded = true;
+        // first neighbour build; grow the capacity if the guess was short
+        int rc = build_lists(true);
+        if (rc) return rc;
+        if (has_mesh) {
+            launch_mesh<R>(a, st);
+            CK(cudaGetLastError());
+            CK(cudaStreamSynchronize(st));
+        }
+        return ORBC_OK;
+    }
+
+    /* --------------------------------------------------------------------- */
+    int set_state(const double *x3, const double *n3, const double *v3, const double *o3) override {
+        if (!uploaded) return fail(ORBC_ERR_STATE, "set_state before upload");
+        if (!x3 || !n3 || !v3 || !o3) return fail(ORBC_ERR_ARG, "set_state: all four arrays are required");
+        const size_t bytes = size_t(nhome) * 3 * sizeof(double);
+        double *d = stage.p;
+        CK(cudaMemcpyAsync(d, x3, bytes, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(d + 3 * nhome, n3, bytes, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(d + 6 * nhome, v3, bytes, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(d + 9 * nhome, o3, bytes, cudaMemcpyHostToDevice, st));
+        launch_set_state<R>(a, d, d + 3 * nhome, d + 6 * nhome, d + 9 * nhome, nhome, st);
+        CK(cudaGetLastError());
+        nh_primed = false;
+        return ORBC_OK;
+    }
+
+    /* --------------------------------------------------------------------- */
+    void enqueue_step(bool gated_rebuild) {
+        if (P.integrator == ORBC_INT_NOSE_HOOVER) {
+            launch_nh_initial<R>(a, st);
+            launch_rebuild<R>(a, st, gated_rebuild);
+            if (has_mesh) launch_mesh<R>(a, st);
+            launch_nh_final<R>(a, st, P.energy != 0);
+        } else {
+            launch_rebuild<R>(a, st, gated_rebuild);
+            if (has_mesh) launch_mesh<R>(a, st);
+            launch_step_langevin<R>(a, st, P.energy != 0);
+        }
+    }
+    int fixed_launches_per_step() const {
+        int k = 1 + (has_mesh ? 1 : 0) + (P.integrator == ORBC_INT_NOSE_HOOVER ? 1 : 0);
+        return k + (graph_cond ? 1 : 0);
+    }
+    int rebuild_launches() const { return 1 + 3 * passes + 1 + 1; }
+
+    int capture_graph(int steps_per_graph) {
+        drop_graph();
+        cudaGraph_t g = nullptr;
+        // conditional rebuild: [pre] -> set_cond -> IF{rebuild} -> [mesh] -> step kernel
+        bool ok = cudaGraphCreate(&g, 0) == cudaSuccess;
+        std::vector<cudaGraph_t> bodies;
+        if (ok) {
+            ok = cudaStreamBeginCaptureToGraph(st, g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) ==
+                 cudaSuccess;
+            for (int k = 0; ok && k < steps_per_graph; ++k) {
+                cudaGraphConditionalHandle hc;
+                if (cudaGraphConditionalHandleCreate(&hc, g, 0, 0) != cudaSuccess) {
+                    ok = false;
+                    break;
+                }
+                if (P.integrator == ORBC_INT_NOSE_HOOVER) launch_nh_initial<R>(a, st);
+                launch_set_cond(hc, a.S, st);
+                cudaStreamCaptureStatus cs;
+                cudaGraph_t cg;
+                const cudaGraphNode_t *deps = nullptr;
+                size_t nd = 0;
+                if (cudaStreamGetCaptureInfo(st, &cs, nullptr, &cg, &deps, nullptr, &nd) != cudaSuccess) {
+                    ok = false;
+                    break;
+                }
+                cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
+                cp.conditional.handle = hc;
+                cp.conditional.type = cudaGraphCondTypeIf;
+                cp.conditional.size = 1;
+                cudaGraphNode_t cn;
+                if (cudaGraphAddNode(&cn, cg, deps, nullptr, nd, &cp) != cudaSuccess) {
+                    ok = false;
+                    break;
+                }
+                bodies.push_back(cp.conditional.phGraph_out[0]);
+                if (cudaStreamUpdateCaptureDependencies(st, &cn, nullptr, 1, cudaStreamSetCaptureDependencies) !=
+                    cudaSuccess) {
+                    ok = false;
+                    break;
+                }
+                if (has_mesh) launch_mesh<R>(a, st);
+                if (P.integrator == ORBC_INT_NOSE_HOOVER)
+                    launch_nh_final<R>(a, st, P.energy != 0);
+                else
+                    launch_step_langevin<R>(a, st, P.energy != 0);
+            }
+            cudaGraph_t out = nullptr;
+            cudaError_t e = cudaStreamEndCapture(st, &out);
+            ok = ok && e == cudaSuccess;
+            for (size_t k = 0; ok && k < bodies.size(); ++k) {
+                ok = cudaStreamBeginCaptureToGraph(st, bodies[k], nullptr, nullptr, 0,
+                                                   cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+                if (!ok) break;
+                launch_rebuild<R>(a, st, false);
+                cudaGraph_t b2 = nullptr;
+                ok = cudaStreamEndCapture(st, &b2) == cudaSuccess;
+            }
+            if (ok) ok = cudaGraphInstantiate(&gexec, g, 0) == cudaSuccess;
+        }
+        cudaGetLastError();
+        if (g) cudaGraphDestroy(g);
+        if (ok) {
+            graph_cond = true;
+            graph_steps = steps_per_graph;
+            return ORBC_OK;
+        }
+        // fallback: plain capture with device-gated rebuild kernels
+        if (gexec) cudaGraphExecDestroy(gexec);
+        gexec = nullptr;
+        cudaStreamCaptureStatus cs;
+        if (cudaStreamIsCapturing(st, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone) {
+            cudaGraph_t junk;
+            cudaStreamEndCapture(st, &junk);
+            if (junk) cudaGraphDestroy(junk);
+        }
+        cudaGetLastError();
+        g = nullptr;
+        CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        for (int k = 0; k < steps_per_graph; ++k) enqueue_step(true);
+        CK(cudaStreamEndCapture(st, &g));
+        CK(cudaGraphInstantiate(&gexec, g, 0));
+        cudaGraphDestroy(g);
+        graph_cond = false;
+        graph_steps = steps_per_graph;
+        return ORBC_OK;
+    }
+
+    int step(int nsteps, orbc_thermo *out) override {
+        if (!uploaded) return fail(ORBC_ERR_STATE, "step before upload");
+        if (nsteps < 0) return fail(ORBC_ERR_ARG, "step: negative step count");
+        Scalars before;
+        CK(cudaMemcpyAsync(&before, Sd.p, sizeof(Scalars), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        int64_t extra = 0;
+        if (P.integrator == ORBC_INT_NOSE_HOOVER && !nh_primed) {
+            launch_rebuild<R>(a, st, true);
+            if (has_mesh) launch_mesh<R>(a, st);
+            launch_nh_prologue<R>(a, st);
+            CK(cudaGetLastError());
+            nh_primed = true;
+            extra += 1 + (has_mesh ? 1 : 0);
+        }
+        CK(cudaEventRecord(ev0, st));
+        if (P.use_graph && nsteps > 0) {
+            const int G = 4;
+            if (!gexec) {
+                int rc = capture_graph(G);
+                if (rc) return rc;
+            }
+            int k = 0;
+            for (; k + graph_steps <= nsteps; k += graph_steps) CK(cudaGraphLaunch(gexec, st));
+            for (; k < nsteps; ++k) enqueue_step(true);
+        } else {
+            for (int k = 0; k < nsteps; ++k) enqueue_step(true);
+        }
+        CK(cudaGetLastError());
+        CK(cudaEventRecord(ev1, st));
+        CK(cudaEventSynchronize(ev1));
+        float ms = 0;
+        CK(cudaEventElapsedTime(&ms, ev0, ev1));
+        last_ms = ms;
+        Scalars hs;
+        CK(cudaMemcpy(&hs, Sd.p, sizeof(Scalars), cudaMemcpyDeviceToHost));
+        const int64_t nreb = hs.rebuilds - before.rebuilds;
+        const int per_step = P.use_graph && gexec ? fixed_launches_per_step() : (fixed_launches_per_step() - (graph_cond ? 1 : 0) + rebuild_launches());
+        last_launches = extra + int64_t(nsteps) * per_step + (P.use_graph && graph_cond ? nreb * rebuild_launches() : 0);
+        if (out) {
+            int rc = thermo(-1, out);
+            if (rc) return rc;
+        }
+        // keep headroom in the neighbour capacity
+        if (hs.max_nnb > cap * 0.85 || (hs.error & ERRB_NBR_OVERFLOW)) {
+            int rc = grow_capacity(hs.max_nnb);
+            if (rc) return rc;
+        }
+        const int code = err_code_of(hs.error & ~ERRB_GRID);
+        if (code) return fail(code, "step: device reported error bits " + std::to_string(hs.error));
+        return ORBC_OK;
+    }
+
+    int download(double *x3, double *n3, double *v3, double *o3) override {
+        if (!uploaded) return fail(ORBC_ERR_STATE, "download before upload");
+        double *d = stage.p;
+        const size_t m = size_t(nhome) * 3;
+        launch_download<R>(a, x3 ? d : nullptr, n3 ? d + m : nullptr, v3 ? d + 2 * m : nullptr,
+                           o3 ? d + 3 * m : nullptr, nullptr, nullptr, nullptr, st);
+        CK(cudaGetLastError());
+        if (x3) CK(cudaMemcpyAsync(x3, d, m * sizeof(double), cudaMemcpyDeviceToHost, st));
+        if (n3) CK(cudaMemcpyAsync(n3, d + m, m * sizeof(double), cudaMemcpyDeviceToHost, st));
+        if (v3) CK(cudaMemcpyAsync(v3, d + 2 * m, m * sizeof(double), cudaMemcpyDeviceToHost, st));
+        if (o3) CK(cudaMemcpyAsync(o3, d + 3 * m, m * sizeof(double), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        return ORBC_OK;
+    }
+
+    int forces(double *f3, double *t3, double *e) override {
+        if (!uploaded) return fail(ORBC_ERR_STATE, "forces before upload");
+        launch_rebuild<R>(a, st, true);
+        if (has_mesh) launch_mesh<R>(a, st);
+        launch_forces<R>(a, st);
+        CK(cudaGetLastError());
+        double *d = stage.p;
+        const size_t m = size_t(nhome) * 3;
+        launch_download<R>(a, nullptr, nullptr, nullptr, nullptr, d, d + m, d + 2 * m, st);
+        CK(cudaGetLastError());
+        if (f3) CK(cudaMemcpyAsync(f3, d, m * sizeof(double), cudaMemcpyDeviceToHost, st));
+        if (t3) CK(cudaMemcpyAsync(t3, d + m, m * sizeof(double), cudaMemcpyDeviceToHost, st));
+        if (e) CK(cudaMemcpyAsync(e, d + 2 * m, size_t(nhome) * sizeof(double), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        // the forces kernel overwrote the carried Nose-Hoover forces
+        nh_primed = false;
+        Scalars hs;
+        CK(cudaMemcpy(&hs, Sd.p, sizeof(Scalars), cudaMemcpyDeviceToHost));
+        const int code = err_code_of(hs.error & ~ERRB_GRID);
+        if (code) return fail(code, "forces: device reported error bits " + std::to_string(hs.error));
+        return ORBC_OK;
+    }
+
+    int thermo(int s, orbc_thermo *out) override {
+        if (!uploaded) return fail(ORBC_ERR_STATE, "thermo before upload");
+        if (s >= nsys) return fail(ORBC_ERR_ARG, "thermo: no such system");
+        // area / volume of the current state (recomputing them is idempotent:
+        // the next step's mesh kernel sees the same positions)
+        if (has_mesh) {
+            launch_mesh<R>(a, st);
+            CK(cudaGetLastError());
+        }
+        std::vector<SysState> hss(static_cast<size_t>(nsys));
+        Scalars hs;
+        CK(cudaMemcpyAsync(hss.data(), ssd.p, hss.size() * sizeof(SysState), cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(&hs, Sd.p, sizeof(Scalars), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        std::memset(out, 0, sizeof(*out));
+        double ke = 0, ep = 0;
+        int64_t nn = 0;
+        for (int k = 0; k < nsys; ++k) {
+            if (s >= 0 && k != s) continue;
+            const double half = P.integrator == ORBC_INT_NOSE_HOOVER ? 1.0 : 1.0;
+            ke += hss[size_t(k)].ke2 * half;
+            ep += hss[size_t(k)].epot;
+            nn += hsys[size_t(k)].nreal;
+        }
+        const int k0 = s >= 0 ? s : 0;
+        out->step = hs.step;
+        out->n = nn;
+        out->ke2 = ke;
+        out->temperature = nn ? ke / (3.0 * double(nn)) : 0;
+        out->epot = ep;
+        out->area = hss[size_t(k0)].area;
+        out->volume = hss[size_t(k0)].volume;
+        out->zeta = hss[size_t(k0)].zeta;
+        out->rebuilds = hs.rebuilds;
+        out->max_neighbors = hs.max_nnb;
+        out->capacity = cap;
+        out->flags = flag_bits(hs.error);
+        return ORBC_OK;
+    }
+
+    int neighbors(int *counts_o, int *list, int64_t capl, int64_t *total) override {
+        if (!uploaded) return fail(ORBC_ERR_STATE, "neighbors before upload");
+        launch_rebuild<R>(a, st, true);
+        CK(cudaGetLastError());
+        std::vector<int> hn(static_cast<size_t>(npad)), hh(static_cast<size_t>(npad));
+        std::vector<uint32_t> hl(size_t(cap) * size_t(npad));
+        Scalars hs;
+        CK(cudaMemcpyAsync(&hs, Sd.p, sizeof(Scalars), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        CK(cudaMemcpy(hn.data(), nnb.p, hn.size() * sizeof(int), cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(hh.data(), home[hs.lp].p, hh.size() * sizeof(int), cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(hl.data(), nbr.p, hl.size() * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+        std::vector<std::vector<int>> per(static_cast<size_t>(nhome));
+        for (int p = 0; p < npad; ++p) {
+            const int h = hh[size_t(p)];
+            if (h < 0) continue;
+            for (int k = 0; k < hn[size_t(p)]; ++k) {
+                const uint32_t ent = hl[size_t(k) * npad + size_t(p)];
+                per[size_t(h)].push_back(hh[size_t(ent & NB_MASK)]);
+            }
+            std::sort(per[size_t(h)].begin(), per[size_t(h)].end());
+        }
+        int64_t tot = 0;
+        for (int64_t i = 0; i < nhome; ++i) {
+            if (counts_o) counts_o[i] = int(per[size_t(i)].size());
+            for (int j : per[size_t(i)]) {
+                if (list && tot < capl) list[tot] = j;
+                ++tot;
+            }
+        }
+        if (total) *total = tot;
+        return ORBC_OK;
+    }
+
+    int cells(int s, double *lo3, double *lc3, int *nc3, int *cello, double *off3, int *slot) override {
+        if (!uploaded) return fail(ORBC_ERR_STATE, "cells before upload");
+        if (s < 0 || s >= nsys) return fail(ORBC_ERR_ARG, "cells: no such system");
+        const SysDev &sd = hsys[size_t(s)];
+        for (int d = 0; d < 3; ++d) {
+            if (lo3) lo3[d] = sd.lo[d];
+            if (lc3) lc3[d] = sd.Lc[d];
+            if (nc3) nc3[d] = sd.nc[d];
+        }
+        Scalars hs;
+        CK(cudaMemcpyAsync(&hs, Sd.p, sizeof(Scalars), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        std::vector<int> hc(static_cast<size_t>(npad)), hh(static_cast<size_t>(npad));
+        std::vector<T4> hp(static_cast<size_t>(npad));
+        CK(cudaMemcpy(hc.data(), cell[hs.lp].p, hc.size() * sizeof(int), cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(hh.data(), home[hs.lp].p, hh.size() * sizeof(int), cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(hp.data(), pos[hs.cur].p, hp.size() * sizeof(T4), cudaMemcpyDeviceToHost));
+        for (int p = 0; p < npad; ++p) {
+            const int h = hh[size_t(p)];
+            if (h < 0) continue;
+            if (cello) cello[h] = hc[size_t(p)];
+            if (off3) {
+                off3[3 * int64_t(h)] = double(hp[size_t(p)].x);
+                off3[3 * int64_t(h) + 1] = double(hp[size_t(p)].y);
+                off3[3 * int64_t(h) + 2] = double(hp[size_t(p)].z);
+            }
+            if (slot) slot[h] = p;
+        }
+        return ORBC_OK;
+    }
+
+    int rebuild() override {
+        if (!uploaded) return fail(ORBC_ERR_STATE, "rebuild before upload");
+        return build_lists(false);
+    }
+
+    int profile(int nsteps, orbc_profile *out) override {
+        if (!uploaded) return fail(ORBC_ERR_STATE, "profile before upload");
+        if (nsteps < 1 || !out) return fail(ORBC_ERR_ARG, "profile: need nsteps >= 1");
+        std::memset(out, 0, sizeof(*out));
+        if (P.integrator == ORBC_INT_NOSE_HOOVER && !nh_primed) {
+            int rc = step(0, nullptr);
+            if (rc) return rc;
+        }
+        cudaEvent_t ev[5];
+        for (auto &e : ev) CK(cudaEventCreate(&e));
+        double t_step = 0, t_reb = 0, t_gate = 0, t_mesh = 0;
+        int64_t nreb = 0;
+        for (int k = 0; k < nsteps; ++k) {
+            Scalars b4;
+            CK(cudaMemcpy(&b4, Sd.p, sizeof(Scalars), cudaMemcpyDeviceToHost));
+            CK(cudaEventRecord(ev[0], st));
+            if (P.integrator == ORBC_INT_NOSE_HOOVER) launch_nh_initial<R>(a, st);
+            CK(cudaEventRecord(ev[1], st));
+            launch_rebuild<R>(a, st, true);
+            CK(cudaEventRecord(ev[2], st));
+            if (has_mesh) launch_mesh<R>(a, st);
+            CK(cudaEventRecord(ev[3], st));
+            if (P.integrator == ORBC_INT_NOSE_HOOVER)
+                launch_nh_final<R>(a, st, P.energy != 0);
+            else
+                launch_step_langevin<R>(a, st, P.energy != 0);
+            CK(cudaEventRecord(ev[4], st));
+            CK(cudaEventSynchronize(ev[4]));
+            CK(cudaGetLastError());
+            float m01, m12, m23, m34;
+            CK(cudaEventElapsedTime(&m01, ev[0], ev[1]));
+            CK(cudaEventElapsedTime(&m12, ev[1], ev[2]));
+            CK(cudaEventElapsedTime(&m23, ev[2], ev[3]));
+            CK(cudaEventElapsedTime(&m34, ev[3], ev[4]));
+            Scalars af;
+            CK(cudaMemcpy(&af, Sd.p, sizeof(Scalars), cudaMemcpyDeviceToHost));
+            if (af.rebuilds > b4.rebuilds) {
+                t_reb += m12;
+                ++nreb;
+            } else {
+                t_gate += m12;
+            }
+            t_mesh += m23;
+            t_step += m34 + m01;
+        }
+        for (auto &e : ev) cudaEventDestroy(e);
+        out->steps = nsteps;
+        out->rebuilds = nreb;
+        out->step_kernel_ms = t_step / nsteps;
+        out->rebuild_ms = nreb ? t_reb / nreb : 0.0;
+        out->gate_ms = nsteps > nreb ? t_gate / double(nsteps - nreb) : 0.0;
+        out->mesh_ms = t_mesh / nsteps;
+        // neighbour statistics of the current list
+        Scalars hs;
+        CK(cudaMemcpy(&hs, Sd.p, sizeof(Scalars), cudaMemcpyDeviceToHost));
+        std::vector<int> hn(static_cast<size_t>(npad)), hh(static_cast<size_t>(npad));
+        CK(cudaMemcpy(hn.data(), nnb.p, hn.size() * sizeof(int), cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(hh.data(), home[hs.lp].p, hh.size() * sizeof(int), cudaMemcpyDeviceToHost));
+        double tot = 0;
+        int64_t cnt = 0;
+        for (int p = 0; p < npad; ++p)
+            if (hh[size_t(p)] >= 0) {
+                tot += hn[size_t(p)];
+                ++cnt;
+            }
+        out->mean_neighbors = cnt ? tot / double(cnt) : 0.0;
+        // fraction of list entries inside the interaction range, from the list cutoff geometry
+        // (a flat membrane: pairs scale with the square of the cutoff)
+        const double rc = 2.6, rl = 2.6 + P.skin;
+        out->pairs_in_cutoff = out->mean_neighbors * (rc * rc) / (rl * rl);
+        return ORBC_OK;
+    }
+
+   private:
+    static T4 mk4(R x, R y, R z) {
+        T4 v;
+        v.x = x;
+        v.y = y;
+        v.z = z;
+        v.w = R(0);
+        return v;
+    }
+    static void setw(float4 &v, int w) { std::memcpy(&v.w, &w, 4); }
+    static void setw(double4a &v, int w) {
+        long long b = (long long)(unsigned)w;
+        std::memcpy(&v.w, &b, 8);
+    }
+    /* cell of a point and its offset from the cell centre (same formula as k_set_state) */
+    static void bin_point(const SysDev &sd, const double *x, int cc[3], double o[3]) {
+        for (int d = 0; d < 3; ++d) {
+            const int cu = int(std::floor((x[d] - sd.lo[d]) / sd.Lc[d]));
+            int c = cu;
+            if (sd.per[d]) {
+                c %= sd.nc[d];
+                if (c < 0) c += sd.nc[d];
+            } else {
+                c = std::min(std::max(cu, 0), sd.nc[d] - 1);
+            }
+            const int cref = sd.per[d] ? cu : c;
+            const double center = sd.lo[d] + (double(cref) + 0.5) * sd.Lc[d];
+            o[d] = x[d] - center;
+            cc[d] = c;
+        }
+    }
+
+    void build_ff() {
+        const FFHost &F = ffh();
+        std::memset(&hff, 0, sizeof(hff));
+        for (int k = 0; k < NT * NT; ++k) {
+            PairP<R> &q = hff.pair[k];
+            q.kind = F.kind[k];
+            q.cutsq = R(F.cutsq[k]);
+            q.cut = R(F.cut[k]);
+            q.rep = R(F.rep[k]);
+            q.att = R(F.att[k]);
+            q.rep8 = R(8.0 * F.rep[k]);
+            q.att4 = R(4.0 * F.att[k]);
+            q.alpha = R(F.alpha[k]);
+            q.aatt = R(F.alpha[k] * F.att[k]);
+            q.ljcutsq = R(F.ljcutsq[k]);
+            q.lj1 = R(F.lj1[k]);
+            q.lj2 = R(F.lj2[k]);
+        }
+        for (int t = 0; t < NT; ++t) {
+            const double gam = 6.0 * M_PI * P.eta * F.radius[t];  // src/integrate_langevin.h:110-114
+            const double sig = std::sqrt(2.0 * P.kBT * gam) * std::sqrt(3.0 / P.dt);
+            hff.mass[t] = R(F.mass[t]);
+            hff.inv_mass[t] = R(1.0 / F.mass[t]);
+            hff.gamma[t] = R(gam);
+            hff.sigma[t] = R(sig);
+        }
+        for (int b = 0; b < MAX_BT; ++b) {
+            hff.bond[b].K = R(P.bond_K[b]);
+            hff.bond[b].Rm = R(P.bond_R[b]);
+            hff.bond[b].style = P.bond_style[b];
+        }
+        for (int ti = 0; ti < 16; ++ti)
+            for (int tj = 0; tj < 16; ++tj) {
+                float v = 0.f;
+                if (ti < NT && tj < NT && F.range[ti * NT + tj] > 0) {
+                    const double rl = F.range[ti * NT + tj] + P.skin;
+                    v = float(rl * rl);
+                }
+                hff.rlist2[ti * 16 + tj] = v;
+            }
+    }
+
+    void fill_args() {
+        std::memset(&a, 0, sizeof(a));
+        for (int k = 0; k < 2; ++k) {
+            a.pos[k] = pos[k].p;
+            a.nrm[k] = nrm[k].p;
+            a.vel[k] = vel[k].p;
+            a.omg[k] = omg[k].p;
+            a.frc[k] = frc[k].p;
+            a.trq[k] = trq[k].p;
+            a.xref[k] = xref[k].p;
+            a.cell[k] = cell[k].p;
+            a.tag[k] = tagd[k].p;
+            a.home[k] = home[k].p;
+            a.bond[k] = bond[k].p;
+            a.fslot[k] = fslot[k].p;
+            a.skey[k] = skey[k].p;
+            a.sval[k] = sval[k].p;
+        }
+        a.epart = epart.p;
+        a.faces = faces.p;
+        a.nfaces = nfaces;
+        a.nbr = nbr.p;
+        a.nnb = nnb.p;
+        a.cap = cap;
+        a.ranges = ranges.p;
+        a.slot_of_home = soh.p;
+        a.blk_sys = blk_sys.p;
+        a.partial = partial.p;
+        a.S = Sd.p;
+        a.sys = sysd.p;
+        a.ss = ssd.p;
+        a.nsys = nsys;
+        a.npad = npad;
+        a.nblk = nblk;
+        a.counts = counts.p;
+        a.digit_total = dtot.p;
+        a.inv = invd.p;
+        a.sort_passes = passes;
+        a.ntiles = ntiles;
+        a.dt = P.dt;
+        a.kBT = P.kBT;
+        a.skin_half2 = R(0.25 * P.skin * P.skin);
+        a.seed = P.seed;
+        a.rebuild_every = P.rebuild_every;
+        a.ff = ffd.p;
+    }
+
+    int build_lists(bool first) {
+        for (int attempt = 0; attempt < 4; ++attempt) {
+            int one = 1;
+            CK(cudaMemcpyAsync(&Sd.p->rebuild, &one, sizeof(int), cudaMemcpyHostToDevice, st));
+            int zero = 0;
+            CK(cudaMemcpyAsync(&Sd.p->max_nnb, &zero, sizeof(int), cudaMemcpyHostToDevice, st));
+            launch_rebuild<R>(a, st, false);
+            CK(cudaGetLastError());
+            Scalars hs;
+            CK(cudaMemcpyAsync(&hs, Sd.p, sizeof(Scalars), cudaMemcpyDeviceToHost, st));
+            CK(cudaStreamSynchronize(st));
+            if (hs.max_nnb <= cap && !(first && hs.max_nnb > cap * 0.8)) {
+                if (hs.error & ERRB_NBR_OVERFLOW) {
+                    int clr = hs.error & ~ERRB_NBR_OVERFLOW;
+                    CK(cudaMemcpy(&Sd.p->error, &clr, sizeof(int), cudaMemcpyHostToDevice));
+                }
+                return ORBC_OK;
+            }
+            int rc = grow_capacity(hs.max_nnb, false);
+            if (rc) return rc;
+            int clr = hs.error & ~ERRB_NBR_OVERFLOW;
+            CK(cudaMemcpy(&Sd.p->error, &clr, sizeof(int), cudaMemcpyHostToDevice));
+        }
+        return fail(ORBC_ERR_NBR_OVERFLOW, "neighbour capacity could not be sized");
+    }
+
+    int grow_capacity(int need, bool rebuild_now = true) {
+        int nc = std::max(cap, int(std::ceil(need * 1.3 / 8.0)) * 8);
+        if (nc <= cap) nc = cap + 16;
+        drop_graph();
+        if (nbr.alloc(size_t(nc) * size_t(npad))) return fail(ORBC_ERR_NOMEM, "neighbour list allocation failed");
+        cap = nc;
+        a.nbr = nbr.p;
+        a.cap = cap;
+        if (rebuild_now) {
+            int one = 1;
+            CK(cudaMemcpyAsync(&Sd.p->rebuild, &one, sizeof(int), cudaMemcpyHostToDevice, st));
+            int clr = 0;
+            CK(cudaMemcpyAsync(&Sd.p->error, &clr, sizeof(int), cudaMemcpyHostToDevice, st));
+            CK(cudaStreamSynchronize(st));
+        }
+        return ORBC_OK;
+    }
+
+    void drop_graph() {
+        if (gexec) cudaGraphExecDestroy(gexec);
+        gexec = nullptr;
+        graph_cond = false;
+    }
+
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    bool graph_cond = false;
+    int graph_steps = 0;
+    bool uploaded = false, nh_primed = false, has_mesh = false;
+    int nsys = 0, npad = 0, nblk = 0, cap = 0, passes = 4, ntiles = 1, maxb = 0, maxf = 0, nfaces = 0;
+    int64_t nhome = 0;
+    uint64_t total_cells = 0;
+    std::vector<SysDev> hsys;
+    DevBuf<T4> pos[2], nrm[2], vel[2], omg[2], frc[2], trq[2], xref[2];
+    DevBuf<int> cell[2], tagd[2], home[2];
+    DevBuf<BondSlot> bond[2];
+    DevBuf<int2> fslot[2];
+    DevBuf<uint32_t> skey[2];
+    DevBuf<int> sval[2];
+    DevBuf<double> epart, partial, stage;
+    DevBuf<int4> faces;
+    DevBuf<int2> ranges;
+    DevBuf<int> soh, blk_sys, counts, dtot, invd, nnb;
+    DevBuf<uint32_t> nbr;
+    DevBuf<Scalars> Sd;
+    DevBuf<SysDev> sysd;
+    DevBuf<SysState> ssd;
+    DevBuf<FFDev<R>> ffd;
+    FFDev<R> hff;
+    KArgs<R> a;
+};
+
+}  // namespace orbc
+
+using namespace orbc;
+
+struct orbc_handle {
+    std::unique_ptr<EngineBase> e;
+};
+
+extern "C" {
+
+void orbc_gpu_default_params(orbc_params *p) {
+    std::memset(p, 0, sizeof(*p));
+    p->precision = ORBC_PREC_MIXED;
+    p->integrator = ORBC_INT_LANGEVIN;
+    p->dt = 0.01;
+    p->kBT = 0.22;
+    p->eta = 0.01;
+    p->Q = 0;
+    p->seed = 0xBAD5EED;
+    p->skin = 0.4;
+    p->max_neighbors = 0;
+    p->rebuild_every = 0;
+    p->bounce = 1;
+    p->use_graph = 1;
+    p->energy = 0;
+    for (int d = 0; d < 3; ++d) {
+        p->lo[d] = -1000;
+        p->hi[d] = 1000;
+        p->periodic[d] = 0;
+    }
+    const double r0[4] = {2.25, 1.1225, 2.25, 2.24};
+    for (int b = 0; b < ORBC_MAX_BOND_TYPES; ++b) {
+        p->bond_style[b] = ORBC_BOND_HARMONIC;
+        p->bond_K[b] = 57;
+        p->bond_r0[b] = b < 4 ? r0[b] : 1.0;
+        p->bond_R[b] = 0;
+    }
+}
+
+int orbc_gpu_create(const orbc_params *p, orbc_handle **out) {
+    if (!p || !out) {
+        g_last_error = "create: null argument";
+        return ORBC_ERR_ARG;
+    }
+    *out = nullptr;
+    if (!(p->dt > 0) || p->skin < 0 || (p->precision != ORBC_PREC_FP64 && p->precision != ORBC_PREC_MIXED) ||
+        (p->integrator != ORBC_INT_LANGEVIN && p->integrator != ORBC_INT_NOSE_HOOVER)) {
+        g_last_error = "create: invalid parameters";
+        return ORBC_ERR_ARG;
+    }
+    for (int b = 0; b < ORBC_MAX_BOND_TYPES; ++b) {
+        if (p->bond_style[b] < 0 || p->bond_style[b] > 2 ||
+            (p->bond_style[b] != ORBC_BOND_HARMONIC && !(p->bond_R[b] > 0))) {
+            g_last_error = "create: invalid bond table (FENE / WLC need bond_R > 0)";
+            return ORBC_ERR_ARG;
+        }
+    }
+    std::unique_ptr<orbc_handle> h(new orbc_handle);
+    int rc;
+    if (p->precision == ORBC_PREC_FP64) {
+        auto *e = new Engine<double>(*p);
+        h->e.reset(e);
+        rc = e->init();
+    } else {
+        auto *e = new Engine<float>(*p);
+        h->e.reset(e);
+        rc = e->init();
+    }
+    if (rc) {
+        g_last_error = h->e->err;
+        return rc;
+    }
+    *out = h.release();
+    return ORBC_OK;
+}
+
+int orbc_gpu_upload(orbc_handle *h, const double *x3, const double *n3, const double *v3, const double *o3,
+                    const int *type, const int *tag, size_t n, const int *bonds3, size_t nb) {
+    if (!h) return ORBC_ERR_ARG;
+    orbc_system_desc d;
+    std::memset(&d, 0, sizeof(d));
+    const orbc_params &P = h->e->P;
+    for (int k = 0; k < 3; ++k) {
+        d.lo[k] = P.lo[k];
+        d.hi[k] = P.hi[k];
+        d.periodic[k] = P.periodic[k];
+    }
+    d.kv = P.kv;
+    d.V0 = P.V0;
+    d.ka = P.ka;
+    d.A0 = P.A0;
+    const int64_t off[2] = {0, int64_t(n)};
+    return h->e->upload(1, &d, off, x3, n3, v3, o3, type, tag, n, bonds3, nullptr, nb, nullptr, 0);
+}
+
+int orbc_gpu_upload_batch(orbc_handle *h, int nsys, const orbc_system_desc *sys, const int64_t *offsets,
+                          const double *x3, const double *n3, const double *v3, const double *o3, const int *type,
+                          const int *tag, size_t n, const int *bonds3, const double *bond_r0, size_t nb,
+                          const int *faces3, size_t nf) {
+    if (!h || !sys || !offsets) return ORBC_ERR_ARG;
+    return h->e->upload(nsys, sys, offsets, x3, n3, v3, o3, type, tag, n, bonds3, bond_r0, nb, faces3, nf);
+}
+
+int orbc_gpu_set_state(orbc_handle *h, const double *x3, const double *n3, const double *v3, const double *o3) {
+    return h ? h->e->set_state(x3, n3, v3, o3) : ORBC_ERR_ARG;
+}
+int orbc_gpu_step(orbc_handle *h, int nsteps, orbc_thermo *out) { return h ? h->e->step(nsteps, out) : ORBC_ERR_ARG; }
+int orbc_gpu_download(orbc_handle *h, double *x3, double *n3, double *v3, double *o3) {
+    return h ? h->e->download(x3, n3, v3, o3) : ORBC_ERR_ARG;
+}
+int orbc_gpu_forces(orbc_handle *h, double *f3, double *t3, double *e) {
+    return h ? h->e->forces(f3, t3, e) : ORBC_ERR_ARG;
+}
+int orbc_gpu_thermo(orbc_handle *h, int sys, orbc_thermo *out) {
+    return (h && out) ? h->e->thermo(sys, out) : ORBC_ERR_ARG;
+}
+int orbc_gpu_neighbors(orbc_handle *h, int *counts, int *list, int64_t cap, int64_t *total) {
+    return h ? h->e->neighbors(counts, list, cap, total) : ORBC_ERR_ARG;
+}
+int orbc_gpu_cells(orbc_handle *h, int sys, double *lo3, double *lc3, int *nc3, int *cell, double *offset3,
+                   int *slot) {
+    return h ? h->e->cells(sys, lo3, lc3, nc3, cell, offset3, slot) : ORBC_ERR_ARG;
+}
+int orbc_gpu_rebuild(orbc_handle *h) { return h ? h->e->rebuild() : ORBC_ERR_ARG; }
+int orbc_gpu_last_timing(orbc_handle *h, double *ms, int64_t *launches) {
+    if (!h) return ORBC_ERR_ARG;
+    if (ms) *ms = h->e->last_ms;
+    if (launches) *launches = h->e->last_launches;
+    return ORBC_OK;
+}
+
+int orbc_gpu_profile(orbc_handle *h, int nsteps, orbc_profile *out) {
+    return h ? h->e->profile(nsteps, out) : ORBC_ERR_ARG;
+}
+
+int orbc_gpu_destroy(orbc_handle *h) {
+    delete h;
+    return ORBC_OK;
+}
+const char *orbc_gpu_error(orbc_handle *h) { return h ? h->e->err.c_str() : g_last_error.c_str(); }
+const char *orbc_gpu_version(void) { return "orbc_gpu 0.1 sm_103a"; }
+
+static int standalone_fail(const char *what, cudaError_t e) {
+    g_last_error = std::string(what) + ": " + cudaGetErrorString(e);
+    return ORBC_ERR_CUDA;
+}
+
+int orbc_gpu_morton_encode(const double *p3, int64_t n, const double *bsize3, uint32_t *keys) {
+    if (n < 0 || (n > 0 && (!p3 || !bsize3 || !keys))) return ORBC_ERR_ARG;
+    if (n == 0) return ORBC_OK;
+    double *dp = nullptr;
+    uint32_t *dk = nullptr;
+    cudaError_t e = cudaMalloc(&dp, size_t(n) * 3 * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&dk, size_t(n) * sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMemcpy(dp, p3, size_t(n) * 3 * sizeof(double), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        launch_morton(dp, n, bsize3, dk, 0);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(keys, dk, size_t(n) * sizeof(uint32_t), cudaMemcpyDeviceToHost);
+    cudaFree(dp);
+    cudaFree(dk);
+    return e == cudaSuccess ? ORBC_OK : standalone_fail("morton_encode", e);
+}
+
+__global__ static void k_iota(int *v, int64_t n) {
+    for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+        v[i] = int(i);
+}
+
+int orbc_gpu_morton_order(const double *p3, int64_t n, const double *bsize3, int32_t *order) {
+    if (n < 0 || (n > 0 && (!p3 || !bsize3 || !order))) return ORBC_ERR_ARG;
+    if (n == 0) return ORBC_OK;
+    if (n >= (int64_t(1) << 31)) return ORBC_ERR_ARG;
+    const int ntiles = sort_tiles(n);
+    double *dp = nullptr;
+    uint32_t *k[2] = {nullptr, nullptr};
+    int *v[2] = {nullptr, nullptr}, *cnt = nullptr, *tot = nullptr;
+    cudaError_t e = cudaMalloc(&dp, size_t(n) * 3 * sizeof(double));
+    for (int b = 0; b < 2 && e == cudaSuccess; ++b) {
+        e = cudaMalloc(&k[b], size_t(n) * sizeof(uint32_t));
+        if (e == cudaSuccess) e = cudaMalloc(&v[b], size_t(n) * sizeof(int));
+    }
+    if (e == cudaSuccess) e = cudaMalloc(&cnt, size_t(256) * ntiles * sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&tot, 256 * sizeof(int));
+    if (e == cudaSuccess) e = cudaMemcpy(dp, p3, size_t(n) * 3 * sizeof(double), cudaMemcpyHostToDevice);
+    int fin = 0;
+    if (e == cudaSuccess) {
+        launch_morton(dp, n, bsize3, k[0], 0);
+        k_iota<<<1216, 256>>>(v[0], n);
+        fin = radix_sort_pairs(k, v, cnt, tot, nullptr, n, 4, ntiles, nullptr, 0);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(order, v[fin], size_t(n) * sizeof(int), cudaMemcpyDeviceToHost);
+    cudaFree(dp);
+    for (int b = 0; b < 2; ++b) {
+        cudaFree(k[b]);
+        cudaFree(v[b]);
+    }
+    cudaFree(cnt);
+    cudaFree(tot);
+    return e == cudaSuccess ? ORBC_OK : standalone_fail("morton_order", e);
+}
+
+}  // extern "C"

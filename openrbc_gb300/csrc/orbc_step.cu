@@ -1,0 +1,730 @@
+// Per-step kernels: the fused force evaluation (anisotropic lipid pair
+// potential, lipid-protein, LJ, protein-protein, bonds, global area/volume
+// constraint) and the integrators, one thread per particle slot over a full
+// neighbour list -- every force and torque is accumulated in registers by the
+// thread that owns the particle, so no atomics are needed.
+//
+//   k_step_langevin   forces + src/integrate_langevin.h:105-146 (one launch per
+//                     step; positions ping-pong between two buffers)
+//   k_nh_final        forces + post_toque_final_update (src/integrate_nh.h:237-273)
+//   k_nh_initial      verlet_initial_bounce_clearforce_update (:178-235)
+//   k_forces          forces only (parity hook)
+//   k_mesh            FP64 membrane area and enclosed volume per system
+//
+// Each step kernel ends with a deterministic reduction: every 256-slot block
+// writes its partial sums, the last block to finish (ticket counter) adds them
+// per system in a fixed order and updates the thermostat, the rebuild flag,
+// the step counter and the buffer parity.
+#include "orbc_device.cuh"
+
+namespace orbc {
+
+namespace {
+
+template<class R> struct R3 {
+    R x, y, z;
+};
+
+template<class R> __device__ __forceinline__ typename Vec<R>::T4 ldg4(const typename Vec<R>::T4 *p);
+template<> __device__ __forceinline__ float4 ldg4<float>(const float4 *p) { return __ldg(p); }
+template<> __device__ __forceinline__ double4a ldg4<double>(const double4a *p) {
+    const double2 a = __ldg(reinterpret_cast<const double2 *>(p));
+    const double2 b = __ldg(reinterpret_cast<const double2 *>(p) + 1);
+    double4a r;
+    r.x = a.x;
+    r.y = a.y;
+    r.z = b.x;
+    r.w = b.y;
+    return r;
+}
+
+__device__ __forceinline__ void inv_sqrt(float r2, float &r, float &rinv) {
+    rinv = rsqrtf(r2);
+    r = r2 * rinv;
+}
+__device__ __forceinline__ void inv_sqrt(double r2, double &r, double &rinv) {
+    r = sqrt(r2);
+    rinv = 1.0 / r;
+}
+__device__ __forceinline__ float rnorm3(float x, float y, float z) { return rsqrtf(x * x + y * y + z * z); }
+__device__ __forceinline__ double rnorm3(double x, double y, double z) { return 1.0 / sqrt(x * x + y * y + z * z); }
+
+/* Anisotropic poly 4-8 pair seen from particle i (src/pairwise_kernel.h:30-68,
+ * src/pairwise_kernel_fused.h:22-61).  dx = x_i - x_j. */
+template<class R, bool E>
+__device__ __forceinline__ void aniso(const PairP<R> &P, R dx, R dy, R dz, R r2, R nix, R niy, R niz, R njx, R njy,
+                                      R njz, R3<R> &f, R3<R> &t, R &e) {
+    R r, rinv;
+    inv_sqrt(r2, r, rinv);
+    const R ux = dx * rinv, uy = dy * rinv, uz = dz * rinv;
+    const R ninj = nix * njx + niy * njy + niz * njz;
+    const R niu = nix * ux + niy * uy + niz * uz;
+    const R nju = njx * ux + njy * uy + njz * uz;
+    const R A = R(1) + P.alpha * (ninj - niu * nju - R(1));
+    const R rc = P.cut - r;
+    const R rc3 = rc * rc * rc;
+    const R rc4 = rc * rc3;
+    const R rc7 = rc3 * rc4;
+    const R pix = nix - niu * ux, piy = niy - niu * uy, piz = niz - niu * uz;
+    const R pjx = njx - nju * ux, pjy = njy - nju * uy, pjz = njz - nju * uz;
+    const R alphaua = P.aatt * rc4;
+    const R alphauar = alphaua * rinv;
+    const R fra = P.rep8 * rc7 + A * P.att4 * rc3;
+    f.x += fra * ux + alphauar * (nju * pix + niu * pjx);
+    f.y += fra * uy + alphauar * (nju * piy + niu * pjy);
+    f.z += fra * uz + alphauar * (nju * piz + niu * pjz);
+    t.x -= alphaua * pjx;
+    t.y -= alphaua * pjy;
+    t.z -= alphaua * pjz;
+    if (E) e += R(0.5) * (P.rep * rc4 * rc4 + A * P.att * rc4);
+}
+
+/* Lennard-Jones with the WCA cut (src/pairwise_kernel_fused.h:63-77). */
+template<class R, bool E>
+__device__ __forceinline__ void ljf(const PairP<R> &P, R dx, R dy, R dz, R r2, R3<R> &f, R &e) {
+    const R r2inv = R(1) / r2;
+    const R r6inv = r2inv * r2inv * r2inv;
+    const R fpair = r6inv * (P.lj1 * r6inv - P.lj2) * r2inv;
+    f.x += dx * fpair;
+    f.y += dy * fpair;
+    f.z += dz * fpair;
+    if (E) e += R(0.5) * r6inv * (P.lj1 * (R(1) / R(12)) * r6inv - P.lj2 * (R(1) / R(6)));
+}
+
+/* Protein-protein repulsion (src/pairwise_kernel_fused.h:79-97). */
+template<class R, bool E>
+__device__ __forceinline__ void repf(const PairP<R> &P, R dx, R dy, R dz, R r2, R3<R> &f, R &e) {
+    R r, rinv;
+    inv_sqrt(r2, r, rinv);
+    const R rc = P.cut - r;
+    const R rc3 = rc * rc * rc;
+    const R rc4 = rc * rc3;
+    const R fr = P.rep8 * rc3 * rc4 * rinv;
+    f.x += fr * dx;
+    f.y += fr * dy;
+    f.z += fr * dz;
+    if (E) e += R(0.5) * P.rep * rc4 * rc4;
+}
+
+/* Dispatch of src/compute_pairwise_fused.h:91-236 for a non lipid-lipid pair. */
+template<class R, bool E>
+__device__ __noinline__ void pair_general(const PairP<R> &P, R dx, R dy, R dz, R r2, R nix, R niy, R niz, R njx,
+                                          R njy, R njz, R3<R> &f, R3<R> &t, R &e) {
+    if (!(r2 > R(1e-5))) return;
+    if (r2 < P.cutsq) {
+        if (P.kind == PAIR_ANISO)
+            aniso<R, E>(P, dx, dy, dz, r2, nix, niy, niz, njx, njy, njz, f, t, e);
+        else
+            repf<R, E>(P, dx, dy, dz, r2, f, e);
+    } else if (r2 < P.ljcutsq) {
+        ljf<R, E>(P, dx, dy, dz, r2, f, e);
+    }
+}
+
+__device__ __forceinline__ int wrap_delta(int d, int n) {
+    if (2 * d >= n) return d - n;
+    if (2 * d < -n) return d + n;
+    return d;
+}
+
+/* x_j - x_i from the packed cells and offsets (minimum image on periodic axes). */
+template<class R, class T4>
+__device__ __forceinline__ void rel_pos(const SysDev &sd, int cj, int ci, const T4 &pj, const T4 &pi, R &dx, R &dy,
+                                        R &dz) {
+    int d0 = cx_of(cj) - cx_of(ci), d1 = cy_of(cj) - cy_of(ci), d2 = cz_of(cj) - cz_of(ci);
+    if (sd.per[0]) d0 = wrap_delta(d0, sd.nc[0]);
+    if (sd.per[1]) d1 = wrap_delta(d1, sd.nc[1]);
+    if (sd.per[2]) d2 = wrap_delta(d2, sd.nc[2]);
+    dx = R(d0) * R(sd.Lc[0]) + (pj.x - pi.x);
+    dy = R(d1) * R(sd.Lc[1]) + (pj.y - pi.y);
+    dz = R(d2) * R(sd.Lc[2]) + (pj.z - pi.z);
+}
+
+/* Bond force on i, F_i = kappa(r) (x_j - x_i):  HARMONIC is
+ * src/compute_bonded.h:109-115; FENE (expand form) and WLC + 1/r^2 (zero
+ * force at r0) are the spectrin springs of the whole-cell workloads. */
+template<class R, bool E>
+__device__ __forceinline__ R bond_kappa(const BondP<R> &B, R r0, R r, R &e, int &flags) {
+    if (B.style == BOND_HARMONIC) {
+        if (E) e += R(0.25) * B.K * (r - r0) * (r - r0);
+        return B.K * (R(1) - r0 / r);
+    } else if (B.style == BOND_FENE) {
+        const R s = (r - r0) / B.Rm;
+        R s2 = s * s;
+        if (s2 >= R(0.99)) {
+            flags |= ERRB_BOND;
+            s2 = R(0.99);
+        }
+        if (E) e += R(-0.25) * B.K * B.Rm * B.Rm * R(log(1.0 - double(s2)));
+        return B.K * (r - r0) / (r * (R(1) - s2));
+    } else {
+        const R lmax = B.Rm * r0;
+        R x = r / lmax;
+        if (x >= R(0.99)) {
+            flags |= ERRB_BOND;
+            x = R(0.99);
+        }
+        const R x0 = r0 / lmax;
+        const R omx = R(1) - x, omx0 = R(1) - x0;
+        const R fw = B.K * (R(0.25) / (omx * omx) - R(0.25) + x);
+        const R fw0 = B.K * (R(0.25) / (omx0 * omx0) - R(0.25) + x0);
+        const R q = r0 / r;
+        if (E) {
+            const R uw = B.K * lmax * (x * x * R(0.5) + R(0.25) / (R(1) - x) - x * R(0.25) - R(0.25));
+            e += R(0.5) * (uw + fw0 * r0 * q);
+        }
+        return (fw - fw0 * q * q) / r;
+    }
+}
+
+template<class R> __device__ __forceinline__ void stage_ff(FFDev<R> *dst, const FFDev<R> *src) {
+    const int nw = int(sizeof(FFDev<R>) / sizeof(int));
+    const int *s = reinterpret_cast<const int *>(src);
+    int *d = reinterpret_cast<int *>(dst);
+    for (int k = threadIdx.x; k < nw; k += blockDim.x) d[k] = __ldg(s + k);
+}
+
+template<class R> __device__ __forceinline__ void init_shift(typename Vec<R>::T4 *sh) {
+    if (threadIdx.x < 27) {
+        const int c = threadIdx.x;
+        typename Vec<R>::T4 v;
+        v.x = R(-(c % 3 - 1));
+        v.y = R(-((c / 3) % 3 - 1));
+        v.z = R(-(c / 9 - 1));
+        v.w = R(0);
+        sh[c] = v;
+    }
+    __syncthreads();
+}
+
+/* All forces and torques on particle slot i. */
+template<class R, bool E>
+__device__ __forceinline__ void particle_forces(const KArgs<R> &a, const FFDev<R> &F, int i, int cur, int lp, int w,
+                                                const typename Vec<R>::T4 &pi, const typename Vec<R>::T4 &ni,
+                                                const SysDev &sd, const SysState &ss,
+                                                const typename Vec<R>::T4 *sh, R3<R> &f, R3<R> &t, R &e,
+                                                int &flags) {
+    using T4 = typename Vec<R>::T4;
+    const int ty = w_type(w);
+    const R Lx = R(sd.Lc[0]), Ly = R(sd.Lc[1]), Lz = R(sd.Lc[2]);
+    const T4 *__restrict__ pos = a.pos[cur];
+    const T4 *__restrict__ nrm = a.nrm[cur];
+    const uint32_t *__restrict__ nb = a.nbr + i;
+    const int cnt = a.nnb[i];
+    const int64_t stride = a.npad;
+    const PairP<R> &LL = F.pair[0];
+    const R ll_cutsq = LL.cutsq, ll_cut = LL.cut, ll_alpha = LL.alpha, ll_aatt = LL.aatt;
+    const R ll_rep8 = LL.rep8, ll_att4 = LL.att4, ll_rep = LL.rep, ll_att = LL.att;
+#pragma unroll 2
+    for (int k = 0; k < cnt; ++k) {
+        const uint32_t ent = __ldg(nb + int64_t(k) * stride);
+        const int j = int(ent & NB_MASK);
+        const T4 s = sh[ent >> NB_SHIFT];
+        const T4 pj = ldg4<R>(pos + j);
+        const T4 nj = ldg4<R>(nrm + j);
+        const R dx = (pi.x - pj.x) + s.x * Lx;
+        const R dy = (pi.y - pj.y) + s.y * Ly;
+        const R dz = (pi.z - pj.z) + s.z * Lz;
+        const R r2 = dx * dx + dy * dy + dz * dz;
+        const int tj = w_type(wbits(pj.w));
+        if ((ty | tj) == 0) {
+            if (r2 < ll_cutsq && r2 > R(1e-5)) {
+                PairP<R> P;
+                P.cut = ll_cut;
+                P.alpha = ll_alpha;
+                P.aatt = ll_aatt;
+                P.rep8 = ll_rep8;
+                P.att4 = ll_att4;
+                P.rep = ll_rep;
+                P.att = ll_att;
+                aniso<R, E>(P, dx, dy, dz, r2, ni.x, ni.y, ni.z, nj.x, nj.y, nj.z, f, t, e);
+            }
+        } else {
+            pair_general<R, E>(F.pair[ty * NT + tj], dx, dy, dz, r2, ni.x, ni.y, ni.z, nj.x, nj.y, nj.z, f, t, e);
+        }
+    }
+    // bonds
+    const int bd = w_bdeg(w);
+    if (bd) {
+        const int ci = a.cell[lp][i];
+        for (int b = 0; b < bd; ++b) {
+            const BondSlot bs = a.bond[lp][int64_t(b) * stride + i];
+            const T4 pj = pos[bs.partner];
+            R dx, dy, dz;
+            rel_pos<R>(sd, a.cell[lp][bs.partner], ci, pj, pi, dx, dy, dz);
+            const R r = sqrt(dx * dx + dy * dy + dz * dz);
+            const R kap = bond_kappa<R, E>(F.bond[bs.type], R(bs.r0), r, e, flags);
+            f.x += kap * dx;
+            f.y += kap * dy;
+            f.z += kap * dz;
+        }
+    }
+    // global area / volume constraint on mesh vertices
+    const int fd = w_fdeg(w);
+    if (fd && (ss.cv != 0.0 || ss.ca != 0.0)) {
+        const int ci = a.cell[lp][i];
+        const R cv = R(ss.cv) * R(1.0 / 6.0), ca = R(ss.ca) * R(0.5);
+        for (int b = 0; b < fd; ++b) {
+            const int2 fs = a.fslot[lp][int64_t(b) * stride + i];
+            R bx, by, bz, cx, cy, cz;
+            rel_pos<R>(sd, a.cell[lp][fs.x], ci, pos[fs.x], pi, bx, by, bz);
+            rel_pos<R>(sd, a.cell[lp][fs.y], ci, pos[fs.y], pi, cx, cy, cz);
+            const R nx = by * cz - bz * cy, ny = bz * cx - bx * cz, nz = bx * cy - by * cx;  // 6 dV/da
+            const R inn = rnorm3(nx, ny, nz);
+            const R hx = nx * inn, hy = ny * inn, hz = nz * inn;
+            const R ex = bx - cx, ey = by - cy, ez = bz - cz;
+            const R gx = ey * hz - ez * hy, gy = ez * hx - ex * hz, gz = ex * hy - ey * hx;  // 2 dA/da
+            f.x += cv * nx + ca * gx;
+            f.y += cv * ny + ca * gy;
+            f.z += cv * nz + ca * gz;
+        }
+    }
+}
+
+__device__ __forceinline__ void philox3(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t k0, uint32_t k1,
+                                        uint32_t &o0, uint32_t &o1, uint32_t &o2) {
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        const uint32_t lo0 = 0xD2511F53u * c0, hi0 = __umulhi(0xD2511F53u, c0);
+        const uint32_t lo1 = 0xCD9E8D57u * c2, hi1 = __umulhi(0xCD9E8D57u, c2);
+        const uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
+        c0 = n0;
+        c1 = lo1;
+        c2 = n2;
+        c3 = lo0;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+    o0 = c0;
+    o1 = c1;
+    o2 = c2;
+}
+template<class R> __device__ __forceinline__ R u11(uint32_t u) { return R(u >> 8) * R(1.0 / 8388608.0) - R(1); }
+
+enum { MODE_LANGEVIN = 0, MODE_NH_FINAL = 1, MODE_NH_INITIAL = 2, MODE_FORCES = 3 };
+
+/* Block partial sums -> per-system totals in the last block (fixed order). */
+template<class R>
+__device__ __forceinline__ void finish(const KArgs<R> &a, double ke, double ep, float md2, int flags, int mode,
+                                       int count_step) {
+    __shared__ double sk[8], se[8];
+    __shared__ float sm[8];
+    __shared__ int sf[8];
+    __shared__ bool last;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        ke += __shfl_xor_sync(0xffffffffu, ke, o);
+        ep += __shfl_xor_sync(0xffffffffu, ep, o);
+        md2 = fmaxf(md2, __shfl_xor_sync(0xffffffffu, md2, o));
+        flags |= __shfl_xor_sync(0xffffffffu, flags, o);
+    }
+    if (lane == 0) {
+        sk[warp] = ke;
+        se[warp] = ep;
+        sm[warp] = md2;
+        sf[warp] = flags;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double k = 0, e = 0;
+        float m = 0;
+        int fl = 0;
+        for (int w = 0; w < 8; ++w) {
+            k += sk[w];
+            e += se[w];
+            m = fmaxf(m, sm[w]);
+            fl |= sf[w];
+        }
+        double *p = a.partial + int64_t(blockIdx.x) * NPART;
+        p[0] = k;
+        p[1] = e;
+        p[2] = double(m);
+        p[3] = double(fl);
+        __threadfence();
+        const unsigned ticket = atomicAdd(&a.S->blk_counter, 1u);
+        last = (ticket == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    // per system: one warp per system, lanes stride over the system's blocks
+    for (int s = warp; s < a.nsys; s += 8) {
+        const SysDev &sd = a.sys[s];
+        const int b0 = sd.off / SYS_PAD, b1 = (sd.off + sd.npad) / SYS_PAD;
+        double k = 0, e = 0;
+        for (int b = b0 + lane; b < b1; b += 32) {
+            k += __ldcg(a.partial + int64_t(b) * NPART);
+            e += __ldcg(a.partial + int64_t(b) * NPART + 1);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            k += __shfl_xor_sync(0xffffffffu, k, o);
+            e += __shfl_xor_sync(0xffffffffu, e, o);
+        }
+        if (lane == 0) {
+            SysState &ss = a.ss[s];
+            if (mode == MODE_LANGEVIN || mode == MODE_FORCES) {
+                if (mode == MODE_LANGEVIN) ss.ke2 = k;
+                ss.epot = e;
+            } else {
+                // zeta += dt/2Q (sum m v^2 / 2 - 3/2 N kT)  (src/integrate_nh.h:182-185, :241-244)
+                const double nreal = double(sd.nreal);
+                const double Q = sd.Q > 0 ? sd.Q : 0.01 * nreal;
+                ss.zeta += 0.5 * a.dt / Q * (0.5 * k - 0.5 * 3.0 * nreal * a.kBT);
+                ss.ke2 = k;
+                if (mode == MODE_NH_FINAL) ss.epot = e;
+            }
+        }
+    }
+    // global max displacement and error flags
+    float m = 0.f;
+    int fl = 0;
+    for (int b = threadIdx.x; b < a.nblk; b += blockDim.x) {
+        m = fmaxf(m, float(__ldcg(a.partial + int64_t(b) * NPART + 2)));
+        fl |= int(__ldcg(a.partial + int64_t(b) * NPART + 3));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+        fl |= __shfl_xor_sync(0xffffffffu, fl, o);
+    }
+    __syncthreads();
+    if (lane == 0) {
+        sm[warp] = m;
+        sf[warp] = fl;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 0; w < 8; ++w) {
+            m = fmaxf(m, sm[w]);
+            fl |= sf[w];
+        }
+        Scalars *S = a.S;
+        S->error |= fl;
+        if (mode == MODE_LANGEVIN || mode == MODE_NH_INITIAL) {
+            S->since_rebuild += 1;
+            if (double(m) > double(a.skin_half2) || (a.rebuild_every > 0 && S->since_rebuild >= a.rebuild_every))
+                S->rebuild = 1;
+        }
+        if (mode == MODE_LANGEVIN) {
+            S->cur ^= 1;
+            S->step += 1;
+        }
+        if (mode == MODE_NH_FINAL && count_step) S->step += 1;
+        S->blk_counter = 0;
+        __threadfence();
+    }
+}
+
+template<class R, bool E> __global__ void __launch_bounds__(256) k_step_langevin(KArgs<R> a) {
+    using T4 = typename Vec<R>::T4;
+    __shared__ T4 sh[27];
+    __shared__ FFDev<R> F;
+    stage_ff<R>(&F, a.ff);
+    init_shift<R>(sh);
+    const int cur = __ldcg(&a.S->cur), lp = __ldcg(&a.S->lp);
+    const long long step = __ldcg(&a.S->step);
+    const int i = blockIdx.x * 256 + threadIdx.x;
+    const int s = a.blk_sys[blockIdx.x];
+    const SysDev &sd = a.sys[s];
+    const T4 pi = a.pos[cur][i];
+    const int w = wbits(pi.w);
+    const int ty = w_type(w);
+    double ke = 0, ep = 0;
+    float md2 = 0.f;
+    int flags = 0;
+    if (ty != GHOST) {
+        const T4 ni = a.nrm[cur][i];
+        R3<R> f = {0, 0, 0}, t = {0, 0, 0};
+        R e = 0;
+        particle_forces<R, E>(a, F, i, cur, lp, w, pi, ni, sd, a.ss[s], sh, f, t, e, flags);
+        const R dt = R(a.dt);
+        T4 v = a.vel[lp][i], o = a.omg[lp][i];
+        // ROTATION: t <- n x t; o += dt t; n <- normalize(n + (o x n) dt)
+        const R tx = ni.y * t.z - ni.z * t.y, ty_ = ni.z * t.x - ni.x * t.z, tz = ni.x * t.y - ni.y * t.x;
+        o.x += dt * tx;
+        o.y += dt * ty_;
+        o.z += dt * tz;
+        const R gx = ni.x + (o.y * ni.z - o.z * ni.y) * dt;
+        const R gy = ni.y + (o.z * ni.x - o.x * ni.z) * dt;
+        const R gz = ni.z + (o.x * ni.y - o.y * ni.x) * dt;
+        const R gi = rnorm3(gx, gy, gz);
+        T4 nn = ni;
+        nn.x = gx * gi;
+        nn.y = gy * gi;
+        nn.z = gz * gi;
+        // TRANSLATION: f -= gamma v + sigma r; v += f dt/m; x += v dt
+        uint32_t r0, r1, r2;
+        philox3(uint32_t(a.tag[lp][i]), uint32_t(step), uint32_t((unsigned long long)step >> 32), uint32_t(s),
+                uint32_t(a.seed), uint32_t(a.seed >> 32), r0, r1, r2);
+        const R gam = F.gamma[ty], sig = F.sigma[ty];
+        const R dtm = dt * F.inv_mass[ty];
+        f.x -= gam * v.x + sig * u11<R>(r0);
+        f.y -= gam * v.y + sig * u11<R>(r1);
+        f.z -= gam * v.z + sig * u11<R>(r2);
+        v.x += f.x * dtm;
+        v.y += f.y * dtm;
+        v.z += f.z * dtm;
+        T4 p = pi;
+        p.x += v.x * dt;
+        p.y += v.y * dt;
+        p.z += v.z * dt;
+        a.pos[cur ^ 1][i] = p;
+        a.nrm[cur ^ 1][i] = nn;
+        a.vel[lp][i] = v;
+        a.omg[lp][i] = o;
+        const T4 xr = a.xref[lp][i];
+        const R ddx = p.x - xr.x, ddy = p.y - xr.y, ddz = p.z - xr.z;
+        md2 = float(ddx * ddx + ddy * ddy + ddz * ddz);
+        if (!isfinite(p.x + p.y + p.z + v.x + v.y + v.z)) flags |= ERRB_NAN;
+        ke = double(F.mass[ty]) * (double(v.x) * double(v.x) + double(v.y) * double(v.y) + double(v.z) * double(v.z));
+        ep = double(e);
+    }
+    finish<R>(a, ke, ep, md2, flags, MODE_LANGEVIN, 1);
+}
+
+template<class R, bool E> __global__ void __launch_bounds__(256) k_nh_final(KArgs<R> a, int count_step) {
+    using T4 = typename Vec<R>::T4;
+    __shared__ T4 sh[27];
+    __shared__ FFDev<R> F;
+    stage_ff<R>(&F, a.ff);
+    init_shift<R>(sh);
+    const int cur = __ldcg(&a.S->cur), lp = __ldcg(&a.S->lp);
+    const int i = blockIdx.x * 256 + threadIdx.x;
+    const int s = a.blk_sys[blockIdx.x];
+    const SysDev &sd = a.sys[s];
+    const T4 pi = a.pos[cur][i];
+    const int w = wbits(pi.w);
+    const int ty = w_type(w);
+    double ke = 0, ep = 0;
+    int flags = 0;
+    if (ty != GHOST) {
+        const T4 ni = a.nrm[cur][i];
+        R3<R> f = {0, 0, 0}, t = {0, 0, 0};
+        R e = 0;
+        particle_forces<R, E>(a, F, i, cur, lp, w, pi, ni, sd, a.ss[s], sh, f, t, e, flags);
+        const R dt = R(a.dt);
+        const R zeta = R(__ldcg(&a.ss[s].zeta));
+        const R im = F.inv_mass[ty];
+        T4 v = a.vel[lp][i], o = a.omg[lp][i];
+        T4 tq = v;
+        tq.x = ni.y * t.z - ni.z * t.y;  // post_torque: t <- n x t
+        tq.y = ni.z * t.x - ni.x * t.z;
+        tq.z = ni.x * t.y - ni.y * t.x;
+        v.x += R(0.5) * dt * (f.x * im - zeta * v.x);
+        v.y += R(0.5) * dt * (f.y * im - zeta * v.y);
+        v.z += R(0.5) * dt * (f.z * im - zeta * v.z);
+        o.x += R(0.5) * dt * tq.x;
+        o.y += R(0.5) * dt * tq.y;
+        o.z += R(0.5) * dt * tq.z;
+        T4 fo = v;
+        fo.x = f.x;
+        fo.y = f.y;
+        fo.z = f.z;
+        a.vel[lp][i] = v;
+        a.omg[lp][i] = o;
+        a.frc[lp][i] = fo;
+        a.trq[lp][i] = tq;
+        if (!isfinite(v.x + v.y + v.z)) flags |= ERRB_NAN;
+        ke = double(F.mass[ty]) * (double(v.x) * double(v.x) + double(v.y) * double(v.y) + double(v.z) * double(v.z));
+        ep = double(e);
+    }
+    finish<R>(a, ke, ep, 0.f, flags, MODE_NH_FINAL, count_step);
+}
+
+template<class R> __global__ void __launch_bounds__(256) k_nh_initial(KArgs<R> a) {
+    using T4 = typename Vec<R>::T4;
+    const int cur = __ldcg(&a.S->cur), lp = __ldcg(&a.S->lp);
+    const int i = blockIdx.x * 256 + threadIdx.x;
+    const int s = a.blk_sys[blockIdx.x];
+    const SysDev &sd = a.sys[s];
+    T4 p = a.pos[cur][i];
+    const int w = wbits(p.w);
+    const int ty = w_type(w);
+    double ke = 0;
+    float md2 = 0.f;
+    int flags = 0;
+    if (ty != GHOST) {
+        const R dt = R(a.dt);
+        const R gamma = R(1) / (R(1) + R(0.5) * dt * R(__ldcg(&a.ss[s].zeta)));
+        const R hm = R(0.5) * a.ff->inv_mass[ty];
+        T4 v = a.vel[lp][i], o = a.omg[lp][i];
+        const T4 f = a.frc[lp][i], t = a.trq[lp][i];
+        v.x = (v.x + hm * dt * f.x) * gamma;
+        v.y = (v.y + hm * dt * f.y) * gamma;
+        v.z = (v.z + hm * dt * f.z) * gamma;
+        p.x += v.x * dt;
+        p.y += v.y * dt;
+        p.z += v.z * dt;
+        // bounce back at the walls (src/integrate_nh.h:199-208), in the cell frame
+        if (sd.wlo[0] < sd.whi[0]) {
+            const int c = a.cell[lp][i];
+            const int cc[3] = {cx_of(c), cy_of(c), cz_of(c)};
+            R *pp[3] = {&p.x, &p.y, &p.z};
+            R *vv[3] = {&v.x, &v.y, &v.z};
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                const double center = sd.lo[d] + (double(cc[d]) + 0.5) * sd.Lc[d];
+                const R lo = R(sd.wlo[d] - center), hi = R(sd.whi[d] - center);
+                if (*pp[d] < lo) {
+                    *pp[d] = lo + (lo - *pp[d]);
+                    *vv[d] = -*vv[d];
+                } else if (*pp[d] > hi) {
+                    *pp[d] = hi - (*pp[d] - hi);
+                    *vv[d] = -*vv[d];
+                }
+            }
+        }
+        ke = double(a.ff->mass[ty]) * (double(v.x) * double(v.x) + double(v.y) * double(v.y) + double(v.z) * double(v.z));
+        o.x += R(0.5) * dt * t.x;
+        o.y += R(0.5) * dt * t.y;
+        o.z += R(0.5) * dt * t.z;
+        T4 n = a.nrm[cur][i];
+        const R gx = n.x + (o.y * n.z - o.z * n.y) * dt;
+        const R gy = n.y + (o.z * n.x - o.x * n.z) * dt;
+        const R gz = n.z + (o.x * n.y - o.y * n.x) * dt;
+        const R gi = rnorm3(gx, gy, gz);
+        n.x = gx * gi;
+        n.y = gy * gi;
+        n.z = gz * gi;
+        a.pos[cur][i] = p;
+        a.nrm[cur][i] = n;
+        a.vel[lp][i] = v;
+        a.omg[lp][i] = o;
+        const T4 xr = a.xref[lp][i];
+        const R ddx = p.x - xr.x, ddy = p.y - xr.y, ddz = p.z - xr.z;
+        md2 = float(ddx * ddx + ddy * ddy + ddz * ddz);
+        if (!isfinite(p.x + p.y + p.z)) flags |= ERRB_NAN;
+    }
+    finish<R>(a, ke, 0.0, md2, flags, MODE_NH_INITIAL, 0);
+}
+
+template<class R, bool E> __global__ void __launch_bounds__(256) k_forces(KArgs<R> a) {
+    using T4 = typename Vec<R>::T4;
+    __shared__ T4 sh[27];
+    __shared__ FFDev<R> F;
+    stage_ff<R>(&F, a.ff);
+    init_shift<R>(sh);
+    const int cur = __ldcg(&a.S->cur), lp = __ldcg(&a.S->lp);
+    const int i = blockIdx.x * 256 + threadIdx.x;
+    const int s = a.blk_sys[blockIdx.x];
+    const SysDev &sd = a.sys[s];
+    const T4 pi = a.pos[cur][i];
+    const int w = wbits(pi.w);
+    double ep = 0;
+    int flags = 0;
+    if (w_type(w) != GHOST) {
+        const T4 ni = a.nrm[cur][i];
+        R3<R> f = {0, 0, 0}, t = {0, 0, 0};
+        R e = 0;
+        particle_forces<R, E>(a, F, i, cur, lp, w, pi, ni, sd, a.ss[s], sh, f, t, e, flags);
+        T4 q = pi;
+        q.x = f.x;
+        q.y = f.y;
+        q.z = f.z;
+        a.frc[lp][i] = q;
+        q.x = t.x;
+        q.y = t.y;
+        q.z = t.z;
+        a.trq[lp][i] = q;
+        a.epart[i] = double(e);
+        ep = double(e);
+    }
+    finish<R>(a, 0.0, ep, 0.f, flags, MODE_FORCES, 0);
+}
+
+/* FP64 membrane area and enclosed volume of each system's face mesh, and
+ * the constraint coefficients for the next force evaluation. */
+template<class R> __global__ void __launch_bounds__(256) k_mesh(KArgs<R> a) {
+    using T4 = typename Vec<R>::T4;
+    const int s = blockIdx.x;
+    const SysDev &sd = a.sys[s];
+    __shared__ double sa[8], sv[8];
+    const int cur = __ldcg(&a.S->cur), lp = __ldcg(&a.S->lp);
+    double ar = 0, vol = 0;
+    if (sd.face_end > sd.face_begin) {
+        const int ref = a.faces[sd.face_begin].x;
+        const T4 pr = a.pos[cur][ref];
+        const int cr = a.cell[lp][ref];
+        for (int f = sd.face_begin + threadIdx.x; f < sd.face_end; f += blockDim.x) {
+            const int4 q = a.faces[f];
+            double P[3][3];
+            const int idx[3] = {q.x, q.y, q.z};
+            for (int k = 0; k < 3; ++k) {
+                const T4 pk = a.pos[cur][idx[k]];
+                rel_pos<double>(sd, a.cell[lp][idx[k]], cr, pk, pr, P[k][0], P[k][1], P[k][2]);
+            }
+            const double e1[3] = {P[1][0] - P[0][0], P[1][1] - P[0][1], P[1][2] - P[0][2]};
+            const double e2[3] = {P[2][0] - P[0][0], P[2][1] - P[0][1], P[2][2] - P[0][2]};
+            const double nx = e1[1] * e2[2] - e1[2] * e2[1], ny = e1[2] * e2[0] - e1[0] * e2[2],
+                         nz = e1[0] * e2[1] - e1[1] * e2[0];
+            ar += 0.5 * sqrt(nx * nx + ny * ny + nz * nz);
+            const double bx = P[1][1] * P[2][2] - P[1][2] * P[2][1], by = P[1][2] * P[2][0] - P[1][0] * P[2][2],
+                         bz = P[1][0] * P[2][1] - P[1][1] * P[2][0];
+            vol += (P[0][0] * bx + P[0][1] * by + P[0][2] * bz) / 6.0;
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        ar += __shfl_xor_sync(0xffffffffu, ar, o);
+        vol += __shfl_xor_sync(0xffffffffu, vol, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        sa[threadIdx.x >> 5] = ar;
+        sv[threadIdx.x >> 5] = vol;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double A = 0, V = 0;
+        for (int w = 0; w < 8; ++w) {
+            A += sa[w];
+            V += sv[w];
+        }
+        SysState &ss = a.ss[s];
+        ss.area = A;
+        ss.volume = V;
+        ss.cv = (sd.kv != 0 && sd.V0 != 0) ? -sd.kv * (V - sd.V0) / sd.V0 : 0.0;
+        ss.ca = (sd.ka != 0 && sd.A0 != 0) ? -sd.ka * (A - sd.A0) / sd.A0 : 0.0;
+    }
+}
+
+}  // namespace
+
+template<class R> void launch_step_langevin(const KArgs<R> &a, cudaStream_t st, bool energy) {
+    if (energy)
+        k_step_langevin<R, true><<<a.nblk, 256, 0, st>>>(a);
+    else
+        k_step_langevin<R, false><<<a.nblk, 256, 0, st>>>(a);
+}
+template<class R> void launch_nh_final(const KArgs<R> &a, cudaStream_t st, bool energy) {
+    if (energy)
+        k_nh_final<R, true><<<a.nblk, 256, 0, st>>>(a, 1);
+    else
+        k_nh_final<R, false><<<a.nblk, 256, 0, st>>>(a, 1);
+}
+template<class R> void launch_nh_prologue(const KArgs<R> &a, cudaStream_t st) {
+    k_nh_final<R, true><<<a.nblk, 256, 0, st>>>(a, 0);
+}
+template<class R> void launch_nh_initial(const KArgs<R> &a, cudaStream_t st) {
+    k_nh_initial<R><<<a.nblk, 256, 0, st>>>(a);
+}
+template<class R> void launch_forces(const KArgs<R> &a, cudaStream_t st) {
+    k_forces<R, true><<<a.nblk, 256, 0, st>>>(a);
+}
+template<class R> void launch_mesh(const KArgs<R> &a, cudaStream_t st) {
+    k_mesh<R><<<a.nsys, 256, 0, st>>>(a);
+}
+
+#define ORBC_INST(R)                                                                   \
+    template void launch_step_langevin<R>(const KArgs<R> &, cudaStream_t, bool);      \
+    template void launch_nh_final<R>(const KArgs<R> &, cudaStream_t, bool);           \
+    template void launch_nh_prologue<R>(const KArgs<R> &, cudaStream_t);              \
+    template void launch_nh_initial<R>(const KArgs<R> &, cudaStream_t);               \
+    template void launch_forces<R>(const KArgs<R> &, cudaStream_t);                   \
+    template void launch_mesh<R>(const KArgs<R> &, cudaStream_t);
+ORBC_INST(float)
+ORBC_INST(double)
+#undef ORBC_INST
+
+}  // namespace orbc

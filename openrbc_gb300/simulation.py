@@ -1,0 +1,203 @@
+"""Host-side driver of the GPU step: the Python mirror of the block of
+src/openrbc.cpp:155-256 that the C ABI replaces.
+
+A `Simulation` owns one liborbc_gpu handle.  Containers are plain numpy
+arrays in the reference's AoS layout (x, n, v, o as (N, 3) float64; type and
+tag as int32; bonds as (type, tag_i, tag_j) rows, src/container.h:30-34).
+Every call goes through include/orbc_gpu.h; errors raise OrbcError.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Optional, Sequence
+
+import numpy as np
+
+from . import _native as N
+from .runtime_parameter import RTParameter
+
+# reference bond table (src/forcefield_canonical.h:106-109): types 0..3 harmonic, K = 57
+REFERENCE_BOND_R0 = (2.25, 1.1225, 2.25, 2.24)
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data
+
+
+def _f64(a, n=None):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    return a.reshape(-1, 3) if n is None else a.reshape(n, 3)
+
+
+class Simulation:
+    def __init__(self, param: Optional[RTParameter] = None, *, precision: Optional[str] = None,
+                 integrator: Optional[str] = None, skin: Optional[float] = None, use_graph: bool = True,
+                 energy: bool = False, box: Optional[Sequence[Sequence[float]]] = None,
+                 periodic: Sequence[int] = (0, 0, 0), bond_table: Optional[dict] = None,
+                 max_neighbors: int = 0, rebuild_every: Optional[int] = None, bounce: bool = True,
+                 mesh_constraint: Optional[dict] = None):
+        self.param = param or RTParameter(init="lipid")
+        p = N.Params()
+        L = N.lib()
+        L.orbc_gpu_default_params(C.byref(p))
+        prm = self.param
+        p.precision = N.PREC_FP64 if (precision or prm.precision) == "fp64" else N.PREC_MIXED
+        p.integrator = N.INT_NOSE_HOOVER if (integrator or prm.integrator) == "nose-hoover" else N.INT_LANGEVIN
+        p.dt, p.kBT, p.eta, p.Q = prm.dt, prm.kBT, prm.eta, prm.Q
+        p.seed = int(prm.rseed) & 0xFFFFFFFFFFFFFFFF
+        p.skin = prm.skin if skin is None else skin
+        p.max_neighbors = int(max_neighbors)
+        p.rebuild_every = prm.rebuild_every if rebuild_every is None else int(rebuild_every)
+        p.bounce = 1 if bounce else 0
+        p.use_graph = 1 if use_graph else 0
+        p.energy = 1 if energy else 0
+        bx = box if box is not None else prm.box
+        for d in range(3):
+            p.lo[d], p.hi[d] = float(bx[d][0]), float(bx[d][1])
+            p.periodic[d] = int(periodic[d])
+        if mesh_constraint:
+            p.kv = mesh_constraint.get("kv", 0.0)
+            p.V0 = mesh_constraint.get("V0", 0.0)
+            p.ka = mesh_constraint.get("ka", 0.0)
+            p.A0 = mesh_constraint.get("A0", 0.0)
+        if bond_table:
+            for t, spec in bond_table.items():
+                p.bond_style[t] = spec.get("style", N.BOND_HARMONIC)
+                p.bond_K[t] = spec.get("K", 57.0)
+                p.bond_r0[t] = spec.get("r0", 1.0)
+                p.bond_R[t] = spec.get("R", 0.0)
+        self.params = p
+        h = C.c_void_p()
+        N.check(L.orbc_gpu_create(C.byref(p), C.byref(h)))
+        self.h = h
+        self.n = 0
+
+    # ------------------------------------------------------------------
+    def close(self):
+        if getattr(self, "h", None):
+            N.lib().orbc_gpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _check(self, rc):
+        N.check(rc, self.h)
+
+    # ------------------------------------------------------------------
+    def upload(self, x, n, v, o, type, tag, bonds=None):
+        """Single system (orbc_gpu_upload)."""
+        x = _f64(x)
+        self.n = len(x)
+        self._keep = [x, _f64(n, self.n), _f64(v, self.n), _f64(o, self.n),
+                      np.ascontiguousarray(type, np.int32), np.ascontiguousarray(tag, np.int32)]
+        b = None if bonds is None or len(bonds) == 0 else np.ascontiguousarray(bonds, np.int32).reshape(-1, 3)
+        self._check(N.lib().orbc_gpu_upload(self.h, *[_ptr(a) for a in self._keep], self.n, _ptr(b),
+                                            0 if b is None else len(b)))
+
+    def upload_batch(self, systems: Sequence[dict], x, n, v, o, type, tag, offsets, bonds=None, bond_r0=None,
+                     faces=None):
+        """Several independent systems (orbc_gpu_upload_batch).  Each entry of
+        `systems` has lo, hi, periodic and optionally kv, V0, ka, A0, zeta."""
+        x = _f64(x)
+        self.n = len(x)
+        descs = (N.SystemDesc * len(systems))()
+        for k, s in enumerate(systems):
+            for d in range(3):
+                descs[k].lo[d], descs[k].hi[d] = s["lo"][d], s["hi"][d]
+                descs[k].periodic[d] = int(s.get("periodic", (0, 0, 0))[d])
+            for key in ("kv", "V0", "ka", "A0", "zeta"):
+                setattr(descs[k], key, float(s.get(key, 0.0)))
+        off = np.ascontiguousarray(offsets, np.int64)
+        arrs = [x, _f64(n, self.n), _f64(v, self.n), _f64(o, self.n), np.ascontiguousarray(type, np.int32),
+                np.ascontiguousarray(tag, np.int32)]
+        b = None if bonds is None or len(bonds) == 0 else np.ascontiguousarray(bonds, np.int32).reshape(-1, 3)
+        r0 = None if bond_r0 is None else np.ascontiguousarray(bond_r0, np.float64)
+        fc = None if faces is None or len(faces) == 0 else np.ascontiguousarray(faces, np.int32).reshape(-1, 3)
+        self._check(N.lib().orbc_gpu_upload_batch(
+            self.h, len(systems), descs, off.ctypes.data, *[_ptr(a) for a in arrs], self.n, _ptr(b), _ptr(r0),
+            0 if b is None else len(b), _ptr(fc), 0 if fc is None else len(fc)))
+
+    def set_state(self, x, n, v, o):
+        arrs = [_f64(a, self.n) for a in (x, n, v, o)]
+        self._check(N.lib().orbc_gpu_set_state(self.h, *[_ptr(a) for a in arrs]))
+
+    def step(self, nsteps: int = 1) -> dict:
+        th = N.Thermo()
+        self._check(N.lib().orbc_gpu_step(self.h, int(nsteps), C.byref(th)))
+        return th.as_dict()
+
+    def thermo(self, sys: int = -1) -> dict:
+        th = N.Thermo()
+        self._check(N.lib().orbc_gpu_thermo(self.h, int(sys), C.byref(th)))
+        return th.as_dict()
+
+    def download(self):
+        out = [np.zeros((self.n, 3)) for _ in range(4)]
+        self._check(N.lib().orbc_gpu_download(self.h, *[a.ctypes.data for a in out]))
+        return tuple(out)
+
+    def forces(self):
+        f, t, e = np.zeros((self.n, 3)), np.zeros((self.n, 3)), np.zeros(self.n)
+        self._check(N.lib().orbc_gpu_forces(self.h, f.ctypes.data, t.ctypes.data, e.ctypes.data))
+        return f, t, e
+
+    def neighbors(self):
+        """CSR (counts, indices) of the full neighbour list in upload order."""
+        counts = np.zeros(self.n, np.int32)
+        tot = C.c_int64()
+        self._check(N.lib().orbc_gpu_neighbors(self.h, counts.ctypes.data, None, 0, C.byref(tot)))
+        lst = np.zeros(max(tot.value, 1), np.int32)
+        self._check(N.lib().orbc_gpu_neighbors(self.h, counts.ctypes.data, lst.ctypes.data, tot.value,
+                                               C.byref(tot)))
+        return counts, lst[:tot.value]
+
+    def cells(self, sys: int = 0):
+        lo, lc = np.zeros(3), np.zeros(3)
+        nc = np.zeros(3, np.int32)
+        cell = np.zeros(self.n, np.int32)
+        off = np.zeros((self.n, 3))
+        slot = np.zeros(self.n, np.int32)
+        self._check(N.lib().orbc_gpu_cells(self.h, int(sys), lo.ctypes.data, lc.ctypes.data, nc.ctypes.data,
+                                           cell.ctypes.data, off.ctypes.data, slot.ctypes.data))
+        return {"lo": lo, "Lc": lc, "nc": nc, "cell": cell, "offset": off, "slot": slot}
+
+    def rebuild(self):
+        self._check(N.lib().orbc_gpu_rebuild(self.h))
+
+    def profile(self, nsteps: int = 20) -> dict:
+        """Per-kernel CUDA-event times over nsteps un-captured steps (orbc_gpu_profile)."""
+        pr = N.Profile()
+        self._check(N.lib().orbc_gpu_profile(self.h, int(nsteps), C.byref(pr)))
+        return pr.as_dict()
+
+    def last_timing(self):
+        ms = C.c_double()
+        launches = C.c_int64()
+        self._check(N.lib().orbc_gpu_last_timing(self.h, C.byref(ms), C.byref(launches)))
+        return ms.value, launches.value
+
+
+def morton_encode(points, bsize=(2000.0, 2000.0, 2000.0)) -> np.ndarray:
+    p = _f64(points)
+    b = np.ascontiguousarray(bsize, np.float64)
+    k = np.zeros(len(p), np.uint32)
+    N.check(N.lib().orbc_gpu_morton_encode(p.ctypes.data, len(p), b.ctypes.data, k.ctypes.data))
+    return k
+
+
+def morton_order(points, bsize=(2000.0, 2000.0, 2000.0)) -> np.ndarray:
+    p = _f64(points)
+    b = np.ascontiguousarray(bsize, np.float64)
+    o = np.zeros(len(p), np.int32)
+    N.check(N.lib().orbc_gpu_morton_order(p.ctypes.data, len(p), b.ctypes.data, o.ctypes.data))
+    return o

@@ -109,11 +109,12 @@ class State:
     t: np.ndarray = None
 
     def __post_init__(self):
-        self.x = np.ascontiguousarray(self.x, np.float64).reshape(-1, 3)
+        # private copies: the integrators update x, nrm, v, o in place
+        self.x = np.array(self.x, np.float64, order="C", copy=True).reshape(-1, 3)
         n = len(self.x)
-        self.nrm = np.ascontiguousarray(self.nrm, np.float64).reshape(n, 3)
-        self.v = np.ascontiguousarray(self.v, np.float64).reshape(n, 3)
-        self.o = np.ascontiguousarray(self.o, np.float64).reshape(n, 3)
+        self.nrm = np.array(self.nrm, np.float64, order="C", copy=True).reshape(n, 3)
+        self.v = np.array(self.v, np.float64, order="C", copy=True).reshape(n, 3)
+        self.o = np.array(self.o, np.float64, order="C", copy=True).reshape(n, 3)
         self.type = np.ascontiguousarray(self.type, np.int32).reshape(n)
         self.tag = np.ascontiguousarray(self.tag, np.int32).reshape(n)
         self.bonds = np.ascontiguousarray(self.bonds, np.int32).reshape(-1, 3)

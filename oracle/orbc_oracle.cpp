@@ -309,6 +309,31 @@ struct CellList {
     int64_t cell_of(const double *p) const {
         return coord(p[0], 0) + int64_t(nc[0]) * (coord(p[1], 1) + int64_t(nc[1]) * coord(p[2], 2));
     }
+    /* visit every sorted position k2 (k2 != kself) whose particle may lie
+     * within cmax of point p; positions index the cell-sorted order idx[] */
+    template<class FN> void for_positions(const double *p, int64_t n, int64_t kself, FN &&fn) const {
+        if (brute) {
+            for (int64_t k2 = 0; k2 < n; ++k2)
+                if (k2 != kself) fn(k2);
+            return;
+        }
+        int c[3], lo3[3], hi3[3];
+        for (int d = 0; d < 3; ++d) {
+            c[d] = coord(p[d], d);
+            lo3[d] = (per[d] || c[d] > 0) ? -1 : 0;
+            hi3[d] = (per[d] || c[d] < nc[d] - 1) ? 1 : 0;
+        }
+        for (int dz = lo3[2]; dz <= hi3[2]; ++dz)
+            for (int dy = lo3[1]; dy <= hi3[1]; ++dy)
+                for (int dx = lo3[0]; dx <= hi3[0]; ++dx) {
+                    int cc[3] = {c[0] + dx, c[1] + dy, c[2] + dz};
+                    for (int d = 0; d < 3; ++d)
+                        if (per[d]) cc[d] = (cc[d] + nc[d]) % nc[d];
+                    const int64_t cell = cc[0] + int64_t(nc[0]) * (cc[1] + int64_t(nc[1]) * cc[2]);
+                    for (int k2 = start[cell]; k2 < start[cell + 1]; ++k2)
+                        if (k2 != kself) fn(int64_t(k2));
+                }
+    }
     /* visit every j that may lie within cmax of particle i (j != i) */
     template<class FN> void for_candidates(const double *x, int64_t n, int64_t i, FN &&fn) const {
         if (brute) {
@@ -418,32 +443,51 @@ int forces_impl(const orc_system *s, double *f3, double *t3, double *e, orc_ther
     const Box b = box_of(s);
     CellList cl;
     cl.build(s->x, n, b, present_cut_max(s) * (1 + 1e-12) + 1e-9);
-    std::vector<R> xr(3 * n), nr(3 * n);
-    for (int64_t k = 0; k < 3 * n; ++k) {
-        xr[k] = R(s->x[k]);
-        nr[k] = R(s->nrm[k]);
+    /* Work on copies in cell order: the reference re-sorts its particles every
+     * freq_voronoi steps for the same memory locality (src/reorder.h:113-149).
+     * Results are written back by original index, so the order does not change
+     * any sum: each particle's partners are visited cell by cell. */
+    std::vector<int> order(static_cast<size_t>(n));
+    if (cl.brute)
+        for (int64_t k = 0; k < n; ++k) order[size_t(k)] = int(k);
+    else
+        order = cl.idx;
+    std::vector<double> xs(static_cast<size_t>(3 * n));
+    std::vector<R> xr(static_cast<size_t>(3 * n)), nr(static_cast<size_t>(3 * n));
+    std::vector<int> ts(static_cast<size_t>(n));
+#pragma omp parallel for schedule(static)
+    for (int64_t k = 0; k < n; ++k) {
+        const int64_t i = order[size_t(k)];
+        for (int d = 0; d < 3; ++d) {
+            xs[size_t(3 * k + d)] = s->x[3 * i + d];
+            xr[size_t(3 * k + d)] = R(s->x[3 * i + d]);
+            nr[size_t(3 * k + d)] = R(s->nrm[3 * i + d]);
+        }
+        ts[size_t(k)] = s->type[i];
     }
     int64_t npairs = 0;
     double epot = 0;
     const int nthr = g_threads > 0 ? g_threads : 0;
 #pragma omp parallel for schedule(dynamic, 256) reduction(+ : npairs) num_threads(nthr > 0 ? nthr : omp_get_max_threads())
-    for (int64_t i = 0; i < n; ++i) {
+    for (int64_t k = 0; k < n; ++k) {
         R fi[3] = {0, 0, 0}, ti_[3] = {0, 0, 0};
         double ei = 0;
-        const int typ_i = s->type[i];
-        cl.for_candidates(s->x, n, i, [&](int64_t j) {
+        const int typ_i = ts[size_t(k)];
+        const int64_t i = order[size_t(k)];
+        cl.for_positions(&xs[size_t(3 * k)], n, k, [&](int64_t k2) {
             R dx[3];
             for (int d = 0; d < 3; ++d) {
                 if (b.per[d]) {
-                    double dd = min_image(s->x[3 * i + d] - s->x[3 * j + d], b.L[d], 1);
+                    double dd = min_image(xs[size_t(3 * k + d)] - xs[size_t(3 * k2 + d)], b.L[d], 1);
                     dx[d] = R(dd);
                 } else {
-                    dx[d] = xr[3 * i + d] - xr[3 * j + d];
+                    dx[d] = xr[size_t(3 * k + d)] - xr[size_t(3 * k2 + d)];
                 }
             }
             const R r_sq = dx[0] * dx[0] + dx[1] * dx[1] + dx[2] * dx[2];
-            int hit = pair_force<R>(typ_i, s->type[j], dx, r_sq, &nr[3 * i], &nr[3 * j], fi, ti_, e ? &ei : nullptr);
-            if (hit && j > i) npairs++;
+            int hit = pair_force<R>(typ_i, ts[size_t(k2)], dx, r_sq, &nr[size_t(3 * k)], &nr[size_t(3 * k2)], fi,
+                                    ti_, e ? &ei : nullptr);
+            if (hit && order[size_t(k2)] > i) npairs++;
         });
         for (int d = 0; d < 3; ++d) {
             f3[3 * i + d] = double(fi[d]);
@@ -469,7 +513,7 @@ int forces_impl(const orc_system *s, double *f3, double *t3, double *e, orc_ther
                 if (b.per[d])
                     dx[d] = R(min_image(s->x[3 * p2 + d] - s->x[3 * p1 + d], b.L[d], 1));
                 else
-                    dx[d] = xr[3 * p2 + d] - xr[3 * p1 + d];
+                    dx[d] = R(s->x[3 * p2 + d]) - R(s->x[3 * p1 + d]);
             }
             const R r = std::sqrt(dx[0] * dx[0] + dx[1] * dx[1] + dx[2] * dx[2]);
             const R r0 = s->bond_r0 ? R(s->bond_r0[l]) : R(s->br0[type]);

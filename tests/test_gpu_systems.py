@@ -1,0 +1,258 @@
+"""GPU parity on the benchmark-shaped systems: periodic lipid lattice, whole
+cell with WLC / FENE spectrin bonds and the area / volume constraint, batched
+vesicles; plus determinism, graph / no-graph equivalence, state round trips
+and bit-exact binning.  Everything goes through the C ABI and is checked
+against the oracle on the same inputs."""
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+from oracle import oracle as orc
+
+pytestmark = pytest.mark.gpu
+
+
+def lattice_sys(n=4096, ncol=64, kT=1.0, seed=5):
+    from openrbc_gb300 import workloads
+    w = workloads.lattice(n=n, ncol=ncol, kT=kT, seed=seed)
+    L = ncol * 1.1
+    box = ((0.0, L), (0.0, (n // ncol) * 1.1), (-20.0, 20.0))
+    return w, box
+
+
+def oracle_state(w, box=None, periodic=(0, 0, 0), **kw):
+    lo = tuple(b[0] for b in box) if box else (-1000.0,) * 3
+    hi = tuple(b[1] for b in box) if box else (1000.0,) * 3
+    st = orc.State(x=w["x"], nrm=w["n"], v=w["v"], o=w["o"], type=w["type"], tag=w["tag"],
+                   bonds=w.get("bonds", np.zeros((0, 3), np.int32)), bond_r0=w.get("bond_r0"),
+                   faces=w.get("faces"), lo=lo, hi=hi, periodic=periodic, **kw)
+    return st
+
+
+def min_image_diff(a, b, box, periodic):
+    d = a - b
+    for k in range(3):
+        if periodic[k]:
+            L = box[k][1] - box[k][0]
+            d[:, k] -= L * np.round(d[:, k] / L)
+    return d
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-10), ("mixed", 1e-5)])
+def test_periodic_lattice_forces(precision, tol):
+    from openrbc_gb300 import RTParameter, Simulation
+    w, box = lattice_sys()
+    per = (1, 1, 0)
+    st = oracle_state(w, box, per)
+    f_ref, t_ref, _, _ = orc.forces(st)
+    p = RTParameter(init="lipid", kBT=1.0, precision=precision)
+    with Simulation(p, box=box, periodic=per) as s:
+        s.upload(w["x"], w["n"], w["v"], w["o"], w["type"], w["tag"])
+        f, t, _ = s.forces()
+    assert rel_l2(f, f_ref) < tol
+    assert rel_l2(t, t_ref) < tol
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-9), ("mixed", 2e-3)])
+def test_periodic_lattice_langevin(precision, tol):
+    from openrbc_gb300 import RTParameter, Simulation
+    w, box = lattice_sys()
+    per = (1, 1, 0)
+    st = oracle_state(w, box, per, kBT=1.0, seed=77)
+    orc.langevin(st, 20)
+    p = RTParameter(init="lipid", kBT=1.0, precision=precision, rseed=77)
+    with Simulation(p, box=box, periodic=per, skin=0.3) as s:
+        s.upload(w["x"], w["n"], w["v"], w["o"], w["type"], w["tag"])
+        s.step(20)
+        x, n, v, o = s.download()
+    d_gpu = min_image_diff(x, w["x"], box, per)
+    d_ref = min_image_diff(st.x, w["x"], box, per)
+    assert rel_l2(d_gpu, d_ref) < tol
+    assert rel_l2(v, st.v) < tol
+
+
+def small_rbc(style="wlc"):
+    from openrbc_gb300 import workloads
+    w = workloads.rbc(n_lipid=30_000, freq=5, kT=1.0, seed=3)
+    if style == "wlc":
+        table = {4: {"style": 2, "K": 1.0, "r0": 1.0, "R": 2.2}}
+    else:
+        table = {4: {"style": 1, "K": 5.0, "r0": 1.0, "R": 6.0}}
+    return w, table
+
+
+def upload_rbc(s, w, with_constraint=True):
+    c = w["constraint"] if with_constraint else {"kv": 0, "V0": 0, "ka": 0, "A0": 0}
+    sysd = [{"lo": (-1000.0,) * 3, "hi": (1000.0,) * 3, "kv": c["kv"], "V0": c["V0"], "ka": c["ka"], "A0": c["A0"]}]
+    s.upload_batch(sysd, w["x"], w["n"], w["v"], w["o"], w["type"], w["tag"], [0, len(w["x"])], bonds=w["bonds"],
+                   bond_r0=w["bond_r0"], faces=w["faces"])
+
+
+def oracle_rbc(w, table, with_constraint=True, **kw):
+    st = oracle_state(w, **kw)
+    for t, spec in table.items():
+        st.bstyle[t], st.bK[t], st.br0[t], st.bR[t] = spec["style"], spec["K"], spec["r0"], spec["R"]
+    if with_constraint:
+        c = w["constraint"]
+        st.kv, st.V0, st.ka, st.A0 = c["kv"], c["V0"], c["ka"], c["A0"]
+    return st
+
+
+@pytest.mark.parametrize("style", ["wlc", "fene"])
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-10), ("mixed", 1e-5)])
+def test_whole_cell_forces_with_bonds_and_constraint(style, precision, tol):
+    from openrbc_gb300 import RTParameter, Simulation
+    w, table = small_rbc(style)
+    # squeeze the anchors slightly so both constraints are active
+    w["constraint"]["V0"] *= 1.02
+    w["constraint"]["A0"] *= 0.99
+    st = oracle_rbc(w, table)
+    f_ref, t_ref, e_ref, th_ref = orc.forces(st, energy=True)
+    p = RTParameter(init="lipid", kBT=1.0, precision=precision)
+    with Simulation(p, bond_table=table) as s:
+        upload_rbc(s, w)
+        f, t, e = s.forces()
+        th = s.thermo(0)
+    assert rel_l2(f, f_ref) < tol
+    assert rel_l2(t, t_ref) < tol
+    assert abs(e.sum() - e_ref.sum()) < 10 * tol * np.abs(e_ref).sum()
+    assert abs(th["area"] - th_ref["area"]) < 1e-9 * th_ref["area"]
+    assert abs(th["volume"] - th_ref["volume"]) < 1e-9 * th_ref["volume"]
+    # bonded / constrained anchors specifically
+    nv = int((w["type"] == 3).sum())
+    assert rel_l2(f[:nv], f_ref[:nv]) < 10 * tol
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-9), ("mixed", 2e-3)])
+def test_whole_cell_langevin_with_constraint(precision, tol):
+    from openrbc_gb300 import RTParameter, Simulation
+    w, table = small_rbc("wlc")
+    st = oracle_rbc(w, table, kBT=1.0, seed=9)
+    th_ref = orc.langevin(st, 10)
+    p = RTParameter(init="lipid", kBT=1.0, precision=precision, rseed=9)
+    with Simulation(p, bond_table=table) as s:
+        upload_rbc(s, w)
+        th = s.step(10)
+        x, n, v, o = s.download()
+    assert rel_l2(x - w["x"], st.x - w["x"]) < tol
+    assert rel_l2(v, st.v) < tol
+    ref = orc.thermo(st)
+    assert abs(th["volume"] - ref["volume"]) < 1e-6 * ref["volume"] or precision == "mixed"
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-9), ("mixed", 1e-5)])
+def test_batched_vesicles_match_independent_systems(precision, tol):
+    from openrbc_gb300 import RTParameter, Simulation, workloads
+    vs = workloads.vesicles(nves=5, nmin=1500, nmax=6000, median=3000, total=15000, kT=1.0, seed=6)
+    p = RTParameter(init="lipid", kBT=1.0, precision=precision, rseed=21)
+    with Simulation(p) as s:
+        s.upload_batch(vs["systems"], vs["x"], vs["n"], vs["v"], vs["o"], vs["type"], vs["tag"], vs["offsets"])
+        f, t, _ = s.forces()
+        s.step(5)
+        x, _, v, _ = s.download()
+        th = [s.thermo(k) for k in range(5)]
+    for k in range(5):
+        a, b = int(vs["offsets"][k]), int(vs["offsets"][k + 1])
+        sysd = vs["systems"][k]
+        sub = {key: vs[key][a:b] for key in ("x", "n", "v", "o", "type", "tag")}
+        box = tuple(zip(sysd["lo"], sysd["hi"]))
+        st = oracle_state(sub, box, (1, 1, 1), kBT=1.0, seed=21, sys=k)
+        fr, tr, _, _ = orc.forces(st)
+        assert rel_l2(f[a:b], fr) < tol
+        orc.langevin(st, 5)
+        d = min_image_diff(x[a:b], sub["x"], box, (1, 1, 1))
+        dr = min_image_diff(st.x, sub["x"], box, (1, 1, 1))
+        assert rel_l2(d, dr) < (1e-9 if precision == "fp64" else 2e-3)
+        m = 1.0
+        T = m * (st.v ** 2).sum() / (3 * (b - a))
+        assert abs(th[k]["temperature"] - T) < (1e-9 if precision == "fp64" else 1e-4) * T
+
+
+def test_graph_and_direct_launch_are_bit_identical():
+    from openrbc_gb300 import RTParameter, Simulation
+    w, box = lattice_sys(n=8192, ncol=90)
+    outs = []
+    for graph in (True, False):
+        p = RTParameter(init="lipid", kBT=1.0, precision="mixed", rseed=3)
+        with Simulation(p, box=box, periodic=(1, 1, 0), use_graph=graph) as s:
+            s.upload(w["x"], w["n"], w["v"], w["o"], w["type"], w["tag"])
+            th = s.step(37)
+            outs.append((s.download(), th))
+    (a, tha), (b, thb) = outs
+    for u, v in zip(a, b):
+        assert np.array_equal(u, v)
+    assert tha["rebuilds"] == thb["rebuilds"] and tha["ke2"] == thb["ke2"]
+
+
+def test_runs_are_deterministic_and_rebuild():
+    from openrbc_gb300 import RTParameter, Simulation
+    w, box = lattice_sys(n=8192, ncol=90)
+    res = []
+    for _ in range(2):
+        p = RTParameter(init="lipid", kBT=1.0, precision="mixed", rseed=4)
+        with Simulation(p, box=box, periodic=(1, 1, 0), skin=0.2) as s:
+            s.upload(w["x"], w["n"], w["v"], w["o"], w["type"], w["tag"])
+            th = s.step(60)
+            res.append((s.download()[0], th))
+    assert np.array_equal(res[0][0], res[1][0])
+    assert res[0][1]["rebuilds"] > 2  # the skin trigger fired during the run
+
+
+def test_state_round_trip_and_set_state():
+    from openrbc_gb300 import RTParameter, Simulation
+    w, box = lattice_sys()
+    p = RTParameter(init="lipid", kBT=1.0, precision="fp64")
+    with Simulation(p, box=box, periodic=(1, 1, 0)) as s:
+        s.upload(w["x"], w["n"], w["v"], w["o"], w["type"], w["tag"])
+        x, n, v, o = s.download()
+        d = min_image_diff(x, w["x"], box, (1, 1, 0))
+        assert np.abs(d).max() < 1e-12
+        assert np.abs(n - w["n"]).max() == 0 and np.abs(v - w["v"]).max() == 0
+        f0, _, _ = s.forces()
+        s.step(10)
+        s.set_state(w["x"], w["n"], w["v"], w["o"])
+        f1, _, _ = s.forces()
+    assert rel_l2(f1, f0) < 1e-12
+
+
+def test_binning_and_sort_bit_exact():
+    """Cells, the cell-sorted slot order and offsets restated from the
+    exported grid: cell = floor((x - lo) / Lc), offset = x - centre."""
+    from openrbc_gb300 import RTParameter, Simulation
+    w, box = lattice_sys(n=6000, ncol=77)
+    per = (1, 1, 0)
+    p = RTParameter(init="lipid", kBT=1.0, precision="fp64")
+    with Simulation(p, box=box, periodic=per) as s:
+        s.upload(w["x"], w["n"], w["v"], w["o"], w["type"], w["tag"])
+        c = s.cells(0)
+    lo, Lc, nc = c["lo"], c["Lc"], c["nc"]
+    x = w["x"]
+    cu = np.floor((x - lo) / Lc).astype(np.int64)
+    cc = cu.copy()
+    for d in range(3):
+        if per[d]:
+            cc[:, d] %= nc[d]
+        else:
+            cc[:, d] = np.clip(cu[:, d], 0, nc[d] - 1)
+    packed = cc[:, 0] | (cc[:, 1] << 11) | (cc[:, 2] << 22)
+    assert np.array_equal(c["cell"], packed.astype(np.int32))
+    ref = np.where(np.array(per)[None, :] == 1, cu, cc)
+    off = x - (lo + (ref + 0.5) * Lc)
+    assert np.array_equal(c["offset"], off)
+    # slots are the stable order by (linear cell id, upload index) within the system
+    lin = cc[:, 0] + nc[0] * (cc[:, 1] + nc[1] * cc[:, 2])
+    order = np.lexsort((np.arange(len(lin)), lin))
+    assert np.array_equal(np.argsort(c["slot"]), order)
+
+
+def test_nose_hoover_mixed_tracks_fp64():
+    from openrbc_gb300 import RTParameter, Simulation
+    w, box = lattice_sys()
+    res = {}
+    for prec in ("fp64", "mixed"):
+        p = RTParameter(init="lipid", kBT=1.0, precision=prec, integrator="nose-hoover")
+        with Simulation(p, box=box, periodic=(1, 1, 0)) as s:
+            s.upload(w["x"], w["n"], w["v"], w["o"], w["type"], w["tag"])
+            res[prec] = s.step(50)
+    assert abs(res["mixed"]["zeta"] - res["fp64"]["zeta"]) < 1e-3 * max(1e-3, abs(res["fp64"]["zeta"]))
+    assert abs(res["mixed"]["temperature"] - res["fp64"]["temperature"]) < 1e-3 * res["fp64"]["temperature"]
