@@ -47,9 +47,14 @@ BYTES_PER_PSTEP = 104.0
 FLOP_PER_PAIR = 106.0
 
 
-def workload():
+def workload(n_lipid=N_LIPID):
     from openrbc_gb300 import workloads
-    return workloads.rbc(n_lipid=N_LIPID, freq=FREQ, kT=KT, seed=2)
+    freq = FREQ if n_lipid == N_LIPID else max(4, int(round(FREQ * (n_lipid / N_LIPID) ** 0.5)))
+    return workloads.rbc(n_lipid=n_lipid, freq=freq, kT=KT, seed=2)
+
+
+def log(*a):
+    print("[bench]", *a, file=sys.stderr, flush=True)
 
 
 def make_sim(w, precision, **kw):
@@ -127,12 +132,13 @@ def cpu_baseline(w, nsteps=2, precision="f32"):
     threads = os.cpu_count() or 1
     orc.set_threads(threads)
     t0 = time.perf_counter()
-    orc.langevin(st, nsteps, precision)
+    orc.langevin(st, nsteps, precision, fast=True)
     dt = time.perf_counter() - t0
     n = len(w["x"])
     return {"value": n * nsteps / dt, "unit": "particle-steps/s", "cores": orc.get_threads(), "kind": "port",
             "sample": f"{nsteps} Langevin steps of the full {n}-particle membrane, FP32, oracle port of "
-                      f"src/compute_pairwise_fused.h + src/integrate_langevin.h"}
+                      f"src/compute_pairwise_fused.h + src/integrate_langevin.h built with the reference's "
+                      f"-O3 -ffast-math native flags"}
 
 
 def dist_setup():
@@ -163,7 +169,7 @@ def allreduce_max(v, ws):
 def run_reference(args, rank, ws):
     if rank != 0:
         return 0
-    w = workload()
+    w = workload(args.n_lipid)
     from oracle import oracle as orc
     orc.build()
     n = len(w["x"])
@@ -190,6 +196,9 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--fp64-steps", type=int, default=10)
+    ap.add_argument("--n-lipid", type=int, default=N_LIPID, help="smaller membranes for profiling runs")
+    ap.add_argument("--skip-fp64", action="store_true")
+    ap.add_argument("--skip-e2e", action="store_true")
     args = ap.parse_args()
     rank, ws = dist_setup()
     if args.impl == "reference":
@@ -197,81 +206,93 @@ def main():
     if "LOCAL_RANK" in os.environ:
         os.environ.setdefault("CUDA_VISIBLE_DEVICES", os.environ["LOCAL_RANK"])
 
-    from openrbc_gb300 import _native
-    _native.lib()
-    w = workload()
+    from openrbc_gb300 import _native as N
+    L = N.lib()
+    t_gen = time.perf_counter()
+    w = workload(args.n_lipid)
     n = len(w["x"])
+    log(f"workload: {n} particles, {len(w['bonds'])} bonds, {len(w['faces'])} faces "
+        f"({time.perf_counter() - t_gen:.1f} s)")
 
     # ---- mixed precision, device-resident
     sim = make_sim(w, "mixed")
     f_mixed, _, _ = sim.forces()
     sim.step(args.warmup)
     barrier(ws)
+    th0 = sim.thermo()
     with ClockSampler() as clk:
         th = sim.step(args.steps)
         ms, launches = sim.last_timing()
     ms = allreduce_max(ms, ws)
     value = ws * n * args.steps / (ms * 1e-3)
+    log(f"mixed: {ms / args.steps:.4f} ms/step, {value:.4e} particle-steps/s, "
+        f"rebuilds {th['rebuilds'] - th0['rebuilds']}, T = {th['temperature']:.4f}")
 
-    # ---- dominant kernel timing (profiled pass: events around each launch group)
+    # ---- dominant kernel timing (profiled pass: CUDA events around each launch group)
     prof = sim.profile(20)
+    log(f"profile: {prof}")
 
     # ---- plain FP64 on the same workload
-    sim64 = make_sim(w, "fp64")
-    f64, _, _ = sim64.forces()
-    sim64.step(2)
-    sim64.step(args.fp64_steps)
-    ms64, _ = sim64.last_timing()
-    value64 = n * args.fp64_steps / (ms64 * 1e-3)
-    sim64.close()
-    ferr = float(np.linalg.norm(f_mixed - f64) / np.linalg.norm(f64))
+    fp64 = None
+    ferr = None
+    if not args.skip_fp64 and args.fp64_steps > 0:
+        sim64 = make_sim(w, "fp64")
+        f64, _, _ = sim64.forces()
+        sim64.step(2)
+        sim64.step(args.fp64_steps)
+        ms64, _ = sim64.last_timing()
+        value64 = n * args.fp64_steps / (ms64 * 1e-3)
+        sim64.close()
+        ferr = float(np.linalg.norm(f_mixed - f64) / np.linalg.norm(f64))
+        fp64 = {"value": value64, "ms_per_step": ms64 / args.fp64_steps, "steps": args.fp64_steps}
+        log(f"fp64: {ms64 / args.fp64_steps:.4f} ms/step; mixed force rel err vs fp64 {ferr:.3e}")
 
     # ---- end to end through the C ABI with pinned host buffers
-    import torch
-    host = [torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy() for _ in range(4)]
-    sim.download()
-    x, nn, v, o = sim.download()
-    for h, a in zip(host, (x, nn, v, o)):
-        h[:] = a
-    e2e_steps = max(3, args.steps // 20)
-    import ctypes as C
-    from openrbc_gb300 import _native as N
-    L = N.lib()
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        N.check(L.orbc_gpu_set_state(sim.h, *[h.ctypes.data for h in host]), sim.h)
-        N.check(L.orbc_gpu_step(sim.h, 1, None), sim.h)
-        N.check(L.orbc_gpu_download(sim.h, *[h.ctypes.data for h in host]), sim.h)
-    e2e_s = allreduce_max(time.perf_counter() - t0, ws)
-    e2e = {"value": ws * n * e2e_steps / e2e_s, "unit": "particle-steps/s",
-           "h2d_bytes_per_step": 4 * 3 * 8 * n, "d2h_bytes_per_step": 4 * 3 * 8 * n,
-           "note": "per step: orbc_gpu_set_state (pinned H2D, forces a neighbour rebuild) + orbc_gpu_step(1) + "
-                   "orbc_gpu_download (D2H)"}
+    e2e = None
+    if not args.skip_e2e:
+        import torch
+        host = [torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy() for _ in range(4)]
+        for h, arr in zip(host, sim.download()):
+            h[:] = arr
+        e2e_steps = max(3, args.steps // 20)
+        barrier(ws)
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            N.check(L.orbc_gpu_set_state(sim.h, *[h.ctypes.data for h in host]), sim.h)
+            N.check(L.orbc_gpu_step(sim.h, 1, None), sim.h)
+            N.check(L.orbc_gpu_download(sim.h, *[h.ctypes.data for h in host]), sim.h)
+        e2e_s = allreduce_max(time.perf_counter() - t0, ws)
+        e2e = {"value": ws * n * e2e_steps / e2e_s, "unit": "particle-steps/s",
+               "h2d_bytes_per_step": 4 * 3 * 8 * n, "d2h_bytes_per_step": 4 * 3 * 8 * n, "steps": e2e_steps,
+               "note": "per step: orbc_gpu_set_state (pinned H2D of x, n, v, o; forces a neighbour rebuild) + "
+                       "orbc_gpu_step(1) + orbc_gpu_download (D2H of x, n, v, o)"}
+        log(f"e2e: {e2e['value']:.4e} particle-steps/s")
 
     peak, peak_kind = measured_peaks()
     kt = prof["step_kernel_ms"]
     achieved = BYTES_PER_PSTEP * n / (kt * 1e-3) / 1e9
-    k_mean = prof.get("mean_neighbors", None)
-    flops = 0.5 * (th["max_neighbors"] if k_mean is None else k_mean) * FLOP_PER_PAIR * n
+    pairs = prof["pairs_in_cutoff"]
+    flops = 0.5 * pairs * FLOP_PER_PAIR * n
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "traffic": None, "kernel": "k_step_langevin<float>", "kernel_ms": kt,
-            "peak_source": peak_kind,
-            "alu": {"achieved_tflops": flops / (kt * 1e-3) / 1e12, "unit": "TFLOP/s (FP32, algorithmic)"}}
+            "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
+            "alu": {"achieved_tflops": flops / (kt * 1e-3) / 1e12,
+                    "unit": "TFLOP/s (FP32, algorithmic: 106 flop per pair, half the list partners inside rc)"}}
     line = {"metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": f"rbc-evans-fung-{n}", "n_particles": n, "n_lipid": N_LIPID,
-                       "anchors": n - N_LIPID, "bonds": int(len(w["bonds"])), "faces": int(len(w["faces"])),
+            "config": {"workload": f"rbc-evans-fung-{n}", "n_particles": n, "n_lipid": args.n_lipid,
+                       "anchors": n - args.n_lipid, "bonds": int(len(w["bonds"])), "faces": int(len(w["faces"])),
                        "integrator": "langevin", "dt": DT, "kT": KT, "skin": SKIN, "precision": "mixed",
                        "l2": "inputs larger than L2 (state + neighbour list > 1 GB)",
                        "parallelism": f"replicas x{ws}"},
-            "fp64": {"value": value64, "ms_per_step": ms64 / args.fp64_steps, "steps": args.fp64_steps},
-            "mixed_over_fp64": value / ws / value64, "force_rel_err_mixed_vs_fp64": ferr,
-            "rebuilds_in_timed_region": None, "roofline": roof, "e2e": e2e, "gpu_launches": launches,
-            "clocks": clk.summary(), "profile": prof}
+            "fp64": fp64, "mixed_over_fp64": (value / ws / fp64["value"]) if fp64 else None,
+            "force_rel_err_mixed_vs_fp64": ferr, "rebuilds_in_timed_region": th["rebuilds"] - th0["rebuilds"],
+            "roofline": roof, "e2e": e2e, "gpu_launches": launches, "clocks": clk.summary(), "profile": prof}
+    sim.close()
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(w)
-    sim.close()
+        log(f"cpu baseline: {line['cpu_baseline']}")
     if rank == 0:
         print(json.dumps(line), flush=True)
     return 0

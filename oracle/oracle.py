@@ -19,6 +19,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "liborbc_oracle.so")
+LIB_FAST = os.path.join(HERE, "liborbc_oracle_fast.so")
 REF_DIR = os.path.join(HERE, "_ref")
 DEFAULT_REF_SRC = "/root/reference/src"
 
@@ -27,12 +28,13 @@ MAX_BOND_TYPES = 8
 
 _lock = threading.Lock()
 _lib = None
+_lib_fast = None
 _ref = {}
 
 
 def build(ref_src: Optional[str] = None) -> None:
     """Compile the oracle (and the reference harness when its source exists)."""
-    subprocess.run(["make", "-s", "-C", HERE, "liborbc_oracle.so"], check=True)
+    subprocess.run(["make", "-s", "-C", HERE, "liborbc_oracle.so", "liborbc_oracle_fast.so"], check=True)
     src = ref_src or os.environ.get("ORBC_REF_SRC", DEFAULT_REF_SRC)
     if os.path.isdir(src):
         subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={src}"], check=True,
@@ -160,13 +162,16 @@ class State:
         return s
 
 
-def lib():
-    global _lib
+def lib(fast: bool = False):
+    """The checker (strict IEEE build) or, with fast=True, the same source
+    built with the reference's optimisation flags for the timed baseline."""
+    global _lib, _lib_fast
     with _lock:
-        if _lib is None:
-            if not os.path.exists(LIB):
+        if (_lib_fast if fast else _lib) is None:
+            path = LIB_FAST if fast else LIB
+            if not os.path.exists(path):
                 build()
-            L = C.CDLL(LIB)
+            L = C.CDLL(path)
             P = C.POINTER
             for name in ("orc_forces_f64", "orc_forces_f32"):
                 getattr(L, name).argtypes = [P(OrcSystemC), C.c_void_p, C.c_void_p, C.c_void_p, P(OrcThermoC)]
@@ -182,8 +187,11 @@ def lib():
             L.orc_ff_tables.argtypes = [C.c_void_p] * 4
             L.orc_set_threads.argtypes = [C.c_int]
             L.orc_get_threads.restype = C.c_int
-            _lib = L
-    return _lib
+            if fast:
+                _lib_fast = L
+            else:
+                _lib = L
+    return _lib_fast if fast else _lib
 
 
 def _thermo(th: OrcThermoC) -> dict:
@@ -192,6 +200,11 @@ def _thermo(th: OrcThermoC) -> dict:
 
 def set_threads(n: int) -> None:
     lib().orc_set_threads(int(n))
+    lib(True).orc_set_threads(int(n))
+
+
+def get_threads() -> int:
+    return int(lib().orc_get_threads())
 
 
 def forces(st: State, precision: str = "f64", energy: bool = False):
@@ -211,8 +224,8 @@ def _sync_back(st: State, c: OrcSystemC):
     st.zeta, st.Q, st.step = c.zeta, c.Q, c.step
 
 
-def langevin(st: State, nsteps: int, precision: str = "f64") -> dict:
-    L = lib()
+def langevin(st: State, nsteps: int, precision: str = "f64", fast: bool = False) -> dict:
+    L = lib(fast)
     c = st._c()
     th = OrcThermoC()
     fn = L.orc_step_langevin_f64 if precision == "f64" else L.orc_step_langevin_f32

@@ -139,10 +139,11 @@ template<class R> inline void cross3(const R *u, const R *v, R *w) {  // math_ve
 
 /* Anisotropic poly 4-8 pair: src/pairwise_kernel.h:30-68 (lipid-lipid) and
  * src/pairwise_kernel_fused.h:22-61 (protein-lipid), same formula with the
- * lipid-protein table row of the protein type.  Adds force/torque on i. */
+ * lipid-protein table row of the protein type.  Adds force/torque on i and,
+ * when fj is given (Newton on), the opposite force and j's torque on j. */
 template<class R>
 inline void aniso(const R *dx, R r_sq, const R *mu1, const R *mu2, R cut, R rep, R att, R alpha, R *f,
-                  R *t, double *e) {
+                  R *t, double *e, R *fj, R *tj, double *ej) {
     const R r = std::sqrt(r_sq);
     const R rinv = R(1) / r;
     R u[3];
@@ -166,24 +167,36 @@ inline void aniso(const R *dx, R r_sq, const R *mu1, const R *mu2, R cut, R rep,
     const R alphauar = alphaua / r;
     const R fra = R(8.0) * rep * rc7 + A * R(4.0) * att * rc3;
     for (int k = 0; k < 3; ++k) {
-        f[k] += fra * u[k] + (nju * pni[k] + niu * pnj[k]) * alphauar;
+        const R fk = fra * u[k] + (nju * pni[k] + niu * pnj[k]) * alphauar;
+        f[k] += fk;
         t[k] -= alphaua * pnj[k];
+        if (fj) {
+            fj[k] -= fk;
+            tj[k] -= alphaua * pni[k];
+        }
     }
-    if (e) *e += 0.5 * (double(rep) * double(rc4) * double(rc4) + double(A) * double(att) * double(rc4));
+    const double u2 = 0.5 * (double(rep) * double(rc4) * double(rc4) + double(A) * double(att) * double(rc4));
+    if (e) *e += u2;
+    if (ej) *ej += u2;
 }
 
 /* Lennard-Jones (WCA cut): src/pairwise_kernel_fused.h:63-77. */
-template<class R> inline void lj(const R *dx, R rsq, R lj1, R lj2, R *f, double *e) {
+template<class R> inline void lj(const R *dx, R rsq, R lj1, R lj2, R *f, double *e, R *fj, double *ej) {
     const R r2inv = R(1) / rsq;
     const R r6inv = r2inv * r2inv * r2inv;
     const R forcelj = r6inv * (lj1 * r6inv - lj2);
     const R fpair = forcelj * r2inv;
-    for (int k = 0; k < 3; ++k) f[k] += dx[k] * fpair;
-    if (e) *e += 0.5 * (double(r6inv) * (double(lj1) / 12.0 * double(r6inv) - double(lj2) / 6.0));
+    for (int k = 0; k < 3; ++k) {
+        f[k] += dx[k] * fpair;
+        if (fj) fj[k] -= dx[k] * fpair;
+    }
+    const double u2 = 0.5 * (double(r6inv) * (double(lj1) / 12.0 * double(r6inv) - double(lj2) / 6.0));
+    if (e) *e += u2;
+    if (ej) *ej += u2;
 }
 
 /* Protein-protein repulsion: src/pairwise_kernel_fused.h:79-97. */
-template<class R> inline void prep(const R *dx, R r_sq, R cut, R rep, R *f, double *e) {
+template<class R> inline void prep(const R *dx, R r_sq, R cut, R rep, R *f, double *e, R *fj, double *ej) {
     const R r = std::sqrt(r_sq);
     R u[3];
     for (int k = 0; k < 3; ++k) u[k] = dx[k] / r;
@@ -192,8 +205,13 @@ template<class R> inline void prep(const R *dx, R r_sq, R cut, R rep, R *f, doub
     const R rc4 = rc * rc3;
     const R rc7 = rc3 * rc4;
     const R fr = R(8.0) * rep * rc7;
-    for (int k = 0; k < 3; ++k) f[k] += fr * u[k];
-    if (e) *e += 0.5 * double(rep) * double(rc4) * double(rc4);
+    for (int k = 0; k < 3; ++k) {
+        f[k] += fr * u[k];
+        if (fj) fj[k] -= fr * u[k];
+    }
+    const double u2 = 0.5 * double(rep) * double(rc4) * double(rc4);
+    if (e) *e += u2;
+    if (ej) *ej += u2;
 }
 
 /* Dispatch of src/compute_pairwise_fused.h:91-236: lipid-lipid
@@ -201,26 +219,27 @@ template<class R> inline void prep(const R *dx, R r_sq, R cut, R rep, R *f, doub
  * table index (:168-171), protein-protein with type12 = t1 + 6 t2 (:199-203,
  * :226-230).  Returns 1 if the pair interacted. */
 template<class R>
-inline int pair_force(int ti, int tj, const R *dx, R r_sq, const R *mui, const R *muj, R *f, R *t, double *e) {
+inline int pair_force(int ti, int tj, const R *dx, R r_sq, const R *mui, const R *muj, R *f, R *t, double *e,
+                      R *fj = nullptr, R *tqj = nullptr, double *ej = nullptr) {
     const FF<R> &F = ff<R>();
     if (!(r_sq > R(1e-5))) return 0;
     if (ti == 0 || tj == 0) {
         const int p = ti > tj ? ti : tj;
         if (r_sq < F.cutsqlp[p]) {
-            aniso<R>(dx, r_sq, mui, muj, F.cutlp[p], F.replp[p], F.attlp[p], F.alphalp[p], f, t, e);
+            aniso<R>(dx, r_sq, mui, muj, F.cutlp[p], F.replp[p], F.attlp[p], F.alphalp[p], f, t, e, fj, tqj, ej);
             return 1;
         } else if (r_sq < F.lj_cutsq[p]) {
-            lj<R>(dx, r_sq, F.lj1[p], F.lj2[p], f, e);
+            lj<R>(dx, r_sq, F.lj1[p], F.lj2[p], f, e, fj, ej);
             return 1;
         }
         return 0;
     }
     const int k = ti + NT * tj;
     if (r_sq < F.cutsqpp[k]) {
-        prep<R>(dx, r_sq, F.cutpp[k], F.reppp[k], f, e);
+        prep<R>(dx, r_sq, F.cutpp[k], F.reppp[k], f, e, fj, ej);
         return 1;
     } else if (r_sq < F.lj_cutsq[k]) {
-        lj<R>(dx, r_sq, F.lj1[k], F.lj2[k], f, e);
+        lj<R>(dx, r_sq, F.lj1[k], F.lj2[k], f, e, fj, ej);
         return 1;
     }
     return 0;
@@ -465,35 +484,56 @@ int forces_impl(const orc_system *s, double *f3, double *t3, double *e, orc_ther
         }
         ts[size_t(k)] = s->type[i];
     }
+    /* Newton's third law inside each thread's contiguous range of sorted
+     * particles, evaluated once per pair; pairs that cross ranges are
+     * evaluated from both sides (src/compute_pairwise_fused.h:262-275). */
+    std::vector<R> fs(static_cast<size_t>(3 * n), R(0)), tq(static_cast<size_t>(3 * n), R(0));
+    std::vector<double> es(e ? static_cast<size_t>(n) : 0, 0.0);
     int64_t npairs = 0;
     double epot = 0;
-    const int nthr = g_threads > 0 ? g_threads : 0;
-#pragma omp parallel for schedule(dynamic, 256) reduction(+ : npairs) num_threads(nthr > 0 ? nthr : omp_get_max_threads())
-    for (int64_t k = 0; k < n; ++k) {
-        R fi[3] = {0, 0, 0}, ti_[3] = {0, 0, 0};
-        double ei = 0;
-        const int typ_i = ts[size_t(k)];
-        const int64_t i = order[size_t(k)];
-        cl.for_positions(&xs[size_t(3 * k)], n, k, [&](int64_t k2) {
-            R dx[3];
-            for (int d = 0; d < 3; ++d) {
-                if (b.per[d]) {
-                    double dd = min_image(xs[size_t(3 * k + d)] - xs[size_t(3 * k2 + d)], b.L[d], 1);
-                    dx[d] = R(dd);
-                } else {
-                    dx[d] = xr[size_t(3 * k + d)] - xr[size_t(3 * k2 + d)];
+    const int nthr = g_threads > 0 ? g_threads : omp_get_max_threads();
+#pragma omp parallel num_threads(nthr) reduction(+ : npairs)
+    {
+        const int64_t T = omp_get_num_threads(), tid = omp_get_thread_num();
+        const int64_t beg = n * tid / T, end = n * (tid + 1) / T;
+        for (int64_t k = beg; k < end; ++k) {
+            const int typ_i = ts[size_t(k)];
+            const int64_t i = order[size_t(k)];
+            R *fi = &fs[size_t(3 * k)], *ti_ = &tq[size_t(3 * k)];
+            double *ei = e ? &es[size_t(k)] : nullptr;
+            cl.for_positions(&xs[size_t(3 * k)], n, k, [&](int64_t k2) {
+                const bool inside = k2 >= beg && k2 < end;
+                if (inside && k2 < k) return;  // evaluated when k2 was the first particle
+                R dx[3];
+                for (int d = 0; d < 3; ++d) {
+                    if (b.per[d]) {
+                        double dd = min_image(xs[size_t(3 * k + d)] - xs[size_t(3 * k2 + d)], b.L[d], 1);
+                        dx[d] = R(dd);
+                    } else {
+                        dx[d] = xr[size_t(3 * k + d)] - xr[size_t(3 * k2 + d)];
+                    }
                 }
-            }
-            const R r_sq = dx[0] * dx[0] + dx[1] * dx[1] + dx[2] * dx[2];
-            int hit = pair_force<R>(typ_i, ts[size_t(k2)], dx, r_sq, &nr[size_t(3 * k)], &nr[size_t(3 * k2)], fi,
-                                    ti_, e ? &ei : nullptr);
-            if (hit && order[size_t(k2)] > i) npairs++;
-        });
-        for (int d = 0; d < 3; ++d) {
-            f3[3 * i + d] = double(fi[d]);
-            t3[3 * i + d] = double(ti_[d]);
+                const R r_sq = dx[0] * dx[0] + dx[1] * dx[1] + dx[2] * dx[2];
+                int hit;
+                if (inside)
+                    hit = pair_force<R>(typ_i, ts[size_t(k2)], dx, r_sq, &nr[size_t(3 * k)], &nr[size_t(3 * k2)], fi,
+                                        ti_, ei, &fs[size_t(3 * k2)], &tq[size_t(3 * k2)],
+                                        e ? &es[size_t(k2)] : nullptr);
+                else
+                    hit = pair_force<R>(typ_i, ts[size_t(k2)], dx, r_sq, &nr[size_t(3 * k)], &nr[size_t(3 * k2)], fi,
+                                        ti_, ei);
+                if (hit && (inside || order[size_t(k2)] > i)) npairs++;
+            });
         }
-        if (e) e[i] = ei;
+    }
+#pragma omp parallel for schedule(static)
+    for (int64_t k = 0; k < n; ++k) {
+        const int64_t i = order[size_t(k)];
+        for (int d = 0; d < 3; ++d) {
+            f3[3 * i + d] = double(fs[size_t(3 * k + d)]);
+            t3[3 * i + d] = double(tq[size_t(3 * k + d)]);
+        }
+        if (e) e[i] = es[size_t(k)];
     }
     if (e)
         for (int64_t i = 0; i < n; ++i) epot += e[i];
