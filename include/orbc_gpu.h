@@ -194,6 +194,27 @@ int orbc_gpu_profile(orbc_handle *h, int nsteps, orbc_profile *out);
 int orbc_gpu_morton_encode(const double *p3, int64_t n, const double *bsize3, uint32_t *keys);
 int orbc_gpu_morton_order(const double *p3, int64_t n, const double *bsize3, int32_t *order);
 
+/* orbc_gpu_morton_order for callers that cannot allocate device memory.
+ * No counterpart in the reference.  Some callers may not call cudaMalloc /
+ * cudaFree: programs whose device memory belongs to another allocator (for
+ * example a framework's caching pool that must be the only allocator), and
+ * latency-bound loops that cannot afford the device synchronisation those
+ * calls imply.  Here the caller passes device pointers: d_p3 holds n points
+ * (AoS double[3n]) and d_order receives the stable (key, index) order;
+ * bsize3 is host memory.  The sort's scratch lives in one fixed array of
+ * about 3.1 MB in the library's device memory, present on every GPU that
+ * loads the library until the process exits; nothing is allocated per call.
+ * n above ORBC_NOALLOC_MAX_POINTS returns ORBC_ERR_ARG.  The first call on a
+ * device looks up that array's device address (with the device current);
+ * make that first call before any stream capture.  Work is queued on
+ * `stream` (a cudaStream_t, NULL for the default stream) and the call returns
+ * without waiting.  All calls share the one scratch array: calls whose work
+ * overlaps on the GPU (other streams, other host threads) race and corrupt
+ * each other's results, so order them on one stream. */
+#define ORBC_NOALLOC_MAX_POINTS 262144
+int orbc_gpu_morton_order_noalloc(const double *d_p3, int64_t n, const double *bsize3, int32_t *d_order,
+                                  void *stream);
+
 int orbc_gpu_destroy(orbc_handle *h);
 const char *orbc_gpu_error(orbc_handle *h);   /* NULL handle -> last create/standalone error */
 const char *orbc_gpu_version(void);

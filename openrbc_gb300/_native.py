@@ -19,6 +19,7 @@ PREC_FP64, PREC_MIXED = 0, 1
 INT_LANGEVIN, INT_NOSE_HOOVER = 0, 1
 BOND_HARMONIC, BOND_FENE, BOND_WLC_POW = 0, 1, 2
 MAX_BOND_TYPES = 8
+NOALLOC_MAX_POINTS = 262144
 
 # Every symbol include/*.h declares (checked by the CPU test suite).
 EXPORTS = [
@@ -26,7 +27,7 @@ EXPORTS = [
     "orbc_gpu_set_state", "orbc_gpu_step", "orbc_gpu_download", "orbc_gpu_forces", "orbc_gpu_thermo",
     "orbc_gpu_neighbors", "orbc_gpu_cells", "orbc_gpu_rebuild", "orbc_gpu_last_timing",
     "orbc_gpu_morton_encode", "orbc_gpu_morton_order", "orbc_gpu_destroy", "orbc_gpu_error",
-    "orbc_gpu_version", "orbc_gpu_profile",
+    "orbc_gpu_version", "orbc_gpu_profile", "orbc_gpu_morton_order_noalloc",
     "orbc_gen_lattice", "orbc_gen_rbc_counts", "orbc_gen_rbc", "orbc_gen_vesicle_sizes", "orbc_gen_vesicle",
 ]
 
@@ -112,6 +113,7 @@ def lib():
         L.orbc_gpu_morton_encode.argtypes = [vp, i64, vp, vp]
         L.orbc_gpu_morton_order.argtypes = [vp, i64, vp, vp]
         L.orbc_gpu_profile.argtypes = [H, i32, P(Profile)]
+        L.orbc_gpu_morton_order_noalloc.argtypes = [vp, i64, vp, vp, vp]
         L.orbc_gpu_destroy.argtypes = [H]
         L.orbc_gpu_error.argtypes = [H]
         L.orbc_gpu_error.restype = C.c_char_p
