@@ -199,6 +199,7 @@ def main():
     ap.add_argument("--n-lipid", type=int, default=N_LIPID, help="smaller membranes for profiling runs")
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default skin / kernel form")
     args = ap.parse_args()
     rank, ws = dist_setup()
     if args.impl == "reference":
@@ -217,6 +218,14 @@ def main():
     # ---- mixed precision, device-resident
     sim = make_sim(w, "mixed")
     f_mixed, _, _ = sim.forces()
+    tune = None
+    if not args.no_autotune:
+        t_tune = time.perf_counter()
+        trials = sim.autotune(trial_steps=20)
+        best = min(trials, key=lambda r: r["ms_per_step"])
+        tune = {"chosen": best, "trials": trials, "seconds": time.perf_counter() - t_tune}
+        log(f"autotune: skin {best['skin']}, form {best['variant']}, {best['ms_per_step']:.4f} ms/step "
+            f"({len(trials)} trials, {tune['seconds']:.1f} s)")
     sim.step(args.warmup)
     barrier(ws)
     th0 = sim.thermo()
@@ -283,12 +292,15 @@ def main():
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": f"rbc-evans-fung-{n}", "n_particles": n, "n_lipid": args.n_lipid,
                        "anchors": n - args.n_lipid, "bonds": int(len(w["bonds"])), "faces": int(len(w["faces"])),
-                       "integrator": "langevin", "dt": DT, "kT": KT, "skin": SKIN, "precision": "mixed",
+                       "integrator": "langevin", "dt": DT, "kT": KT,
+                       "skin": tune["chosen"]["skin"] if tune else SKIN,
+                       "kernel_form": tune["chosen"]["variant"] if tune else 0, "precision": "mixed",
                        "l2": "inputs larger than L2 (state + neighbour list > 1 GB)",
                        "parallelism": f"replicas x{ws}"},
             "fp64": fp64, "mixed_over_fp64": (value / ws / fp64["value"]) if fp64 else None,
             "force_rel_err_mixed_vs_fp64": ferr, "rebuilds_in_timed_region": th["rebuilds"] - th0["rebuilds"],
-            "roofline": roof, "e2e": e2e, "gpu_launches": launches, "clocks": clk.summary(), "profile": prof}
+            "roofline": roof, "e2e": e2e, "gpu_launches": launches, "clocks": clk.summary(), "profile": prof,
+            "autotune": tune}
     sim.close()
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(w)

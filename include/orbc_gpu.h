@@ -83,6 +83,11 @@ typedef struct {
     double bond_K[ORBC_MAX_BOND_TYPES];
     double bond_r0[ORBC_MAX_BOND_TYPES];
     double bond_R[ORBC_MAX_BOND_TYPES];
+    /* force-kernel form 0..3: bit 0 = software-pipelined neighbour pass
+       (else 2-way unrolled), bit 1 = non-lipid pair path inlined (else
+       called); orbc_gpu_autotune picks it per workload */
+    int kernel_variant;
+    int pad_params;
 } orbc_params;
 
 /* One independent system of a batched upload (its own box and constraint). */
@@ -185,8 +190,25 @@ typedef struct {
     double mesh_ms;           /* mean time of the area / volume kernel            */
     double mean_neighbors;    /* mean neighbour-list length per particle          */
     double pairs_in_cutoff;   /* mean partners inside the interaction range       */
+    double rebin_ms, sort_ms, gather_ms, nlist_ms;  /* rebuild stages (mean per rebuild) */
 } orbc_profile;
 int orbc_gpu_profile(orbc_handle *h, int nsteps, orbc_profile *out);
+
+/* Autotuner: times trial_steps graph-captured steps for each candidate
+ * neighbour-list skin (0.3, 0.45, 0.6, 0.8, 1.0) and force-kernel form (0..3)
+ * from a snapshot of the current state, keeps the fastest, and restores the
+ * snapshot (state, step counter, thermostat), so the simulation does not
+ * advance.  trials (may be NULL) receives up to max_trials rows.  No
+ * reference counterpart (the reference's cadences are fixed command-line
+ * values, src/runtime_parameter.h:57-60). */
+typedef struct {
+    double skin;
+    int variant;
+    int pad;
+    double ms_per_step;
+    double rebuilds_per_step;
+} orbc_tune_trial;
+int orbc_gpu_autotune(orbc_handle *h, int trial_steps, orbc_tune_trial *trials, int max_trials, int *ntrials);
 
 /* Reference Morton key of n points (src/reorder_morton.h:25-42; bsize3 is
  * RTParameter::bsize, 2000 per axis) and the stable order by (key, index)

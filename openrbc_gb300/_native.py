@@ -27,7 +27,7 @@ EXPORTS = [
     "orbc_gpu_set_state", "orbc_gpu_step", "orbc_gpu_download", "orbc_gpu_forces", "orbc_gpu_thermo",
     "orbc_gpu_neighbors", "orbc_gpu_cells", "orbc_gpu_rebuild", "orbc_gpu_last_timing",
     "orbc_gpu_morton_encode", "orbc_gpu_morton_order", "orbc_gpu_destroy", "orbc_gpu_error",
-    "orbc_gpu_version", "orbc_gpu_profile", "orbc_gpu_morton_order_noalloc",
+    "orbc_gpu_version", "orbc_gpu_profile", "orbc_gpu_morton_order_noalloc", "orbc_gpu_autotune",
     "orbc_gen_lattice", "orbc_gen_rbc_counts", "orbc_gen_rbc", "orbc_gen_vesicle_sizes", "orbc_gen_vesicle",
 ]
 
@@ -49,6 +49,7 @@ class Params(C.Structure):
         ("kv", C.c_double), ("V0", C.c_double), ("ka", C.c_double), ("A0", C.c_double),
         ("bond_style", C.c_int * MAX_BOND_TYPES), ("bond_K", C.c_double * MAX_BOND_TYPES),
         ("bond_r0", C.c_double * MAX_BOND_TYPES), ("bond_R", C.c_double * MAX_BOND_TYPES),
+        ("kernel_variant", C.c_int), ("pad_params", C.c_int),
     ]
 
 
@@ -71,10 +72,16 @@ class Thermo(C.Structure):
 class Profile(C.Structure):
     _fields_ = [("steps", C.c_int64), ("rebuilds", C.c_int64), ("step_kernel_ms", C.c_double),
                 ("rebuild_ms", C.c_double), ("gate_ms", C.c_double), ("mesh_ms", C.c_double),
-                ("mean_neighbors", C.c_double), ("pairs_in_cutoff", C.c_double)]
+                ("mean_neighbors", C.c_double), ("pairs_in_cutoff", C.c_double), ("rebin_ms", C.c_double),
+                ("sort_ms", C.c_double), ("gather_ms", C.c_double), ("nlist_ms", C.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class TuneTrial(C.Structure):
+    _fields_ = [("skin", C.c_double), ("variant", C.c_int), ("pad", C.c_int), ("ms_per_step", C.c_double),
+                ("rebuilds_per_step", C.c_double)]
 
 
 _lib = None
@@ -114,6 +121,7 @@ def lib():
         L.orbc_gpu_morton_order.argtypes = [vp, i64, vp, vp]
         L.orbc_gpu_profile.argtypes = [H, i32, P(Profile)]
         L.orbc_gpu_morton_order_noalloc.argtypes = [vp, i64, vp, vp, vp]
+        L.orbc_gpu_autotune.argtypes = [H, i32, P(TuneTrial), i32, P(i32)]
         L.orbc_gpu_destroy.argtypes = [H]
         L.orbc_gpu_error.argtypes = [H]
         L.orbc_gpu_error.restype = C.c_char_p

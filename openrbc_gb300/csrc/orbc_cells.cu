@@ -224,8 +224,7 @@ template<class R> __global__ void __launch_bounds__(256) k_rebin(KArgs<R> a, int
             p.x = o[0];
             p.y = o[1];
             p.z = o[2];
-            a.pos[cur][i] = p;
-            a.xref[lp][i] = p;
+            a.pos[cur][i] = p;  // the gather that follows sets the displacement reference
             a.cell[lp][i] = cpack(cc[0], cc[1], cc[2]);
             key = sd.cell_base + cell_lin(sd, cc[0], cc[1], cc[2]);
         }
@@ -255,9 +254,11 @@ template<class R> __global__ void __launch_bounds__(256) k_ranges_gather(KArgs<R
         a.nrm[nc][p] = a.nrm[cur][src];
         a.vel[nl][p] = a.vel[lp][src];
         a.omg[nl][p] = a.omg[lp][src];
-        a.frc[nl][p] = a.frc[lp][src];
-        a.trq[nl][p] = a.trq[lp][src];
-        a.xref[nl][p] = a.xref[lp][src];
+        if (a.carry_forces) {  // Nose-Hoover carries f and t from one half-step to the next
+            a.frc[nl][p] = a.frc[lp][src];
+            a.trq[nl][p] = a.trq[lp][src];
+        }
+        a.xref[nl][p] = ps;  // the list about to be built is referenced to these positions
         a.cell[nl][p] = a.cell[lp][src];
         a.tag[nl][p] = a.tag[lp][src];
         const int h = a.home[lp][src];
@@ -297,62 +298,105 @@ template<class R> __global__ void __launch_bounds__(256) k_nlist(KArgs<R> a, int
     const int cur = 1 - __ldcg(&a.S->cur), lp = 1 - __ldcg(&a.S->lp);
     const int n = a.npad;
     int maxc = 0;
+    // n is a multiple of the block size, so whole warps stay in the loop together
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const T4 p = a.pos[cur][i];
         const int ty = w_type(wbits(p.w));
-        if (ty == GHOST) {
-            a.nnb[i] = 0;
-            continue;
-        }
-        const SysDev &sd = a.sys[a.blk_sys[i / SYS_PAD]];
+        const bool real = ty != GHOST;
+        const SysDev &sd = a.sys[a.blk_sys[i / SYS_PAD]];  // one system per warp (SYS_PAD-aligned)
         const int c = a.cell[lp][i];
         const int cc[3] = {cx_of(c), cy_of(c), cz_of(c)};
         const R L[3] = {R(sd.Lc[0]), R(sd.Lc[1]), R(sd.Lc[2])};
         int count = 0;
-        for (int dz = -1; dz <= 1; ++dz) {
-            int z = cc[2] + dz;
-            if (sd.per[2]) {
-                z = z < 0 ? z + sd.nc[2] : (z >= sd.nc[2] ? z - sd.nc[2] : z);
-            } else if (z < 0 || z >= sd.nc[2]) {
-                continue;
+        auto test = [&](int j, int dx, int dy, int dz) {
+            const T4 q = a.pos[cur][j];
+            const int tj = w_type(wbits(q.w));
+            const float rl2 = rl2s[ty * 16 + tj];
+            if (!(rl2 > 0.f)) return;
+            // x_i - x_j = (o_i - o_j) - d * Lc
+            const R ex = add_rn(sub_rn(p.x, q.x), mul_rn(R(-dx), L[0]));
+            const R ey = add_rn(sub_rn(p.y, q.y), mul_rn(R(-dy), L[1]));
+            const R ez = add_rn(sub_rn(p.z, q.z), mul_rn(R(-dz), L[2]));
+            const R r2 = add_rn(add_rn(mul_rn(ex, ex), mul_rn(ey, ey)), mul_rn(ez, ez));
+            if (r2 < R(rl2)) {
+                const uint32_t code = uint32_t((dx + 1) + 3 * (dy + 1) + 9 * (dz + 1));
+                if (count < a.cap) a.nbr[nbr_index(i, count, a.cap)] = uint32_t(j) | (code << NB_SHIFT);
+                ++count;
             }
-            for (int dy = -1; dy <= 1; ++dy) {
-                int y = cc[1] + dy;
-                if (sd.per[1]) {
-                    y = y < 0 ? y + sd.nc[1] : (y >= sd.nc[1] ? y - sd.nc[1] : y);
-                } else if (y < 0 || y >= sd.nc[1]) {
+        };
+        // Bounding box of the warp's cells.  Consecutive slots sit in a few
+        // neighbouring cells, so one sweep of the box (grown by one cell) with
+        // every lane testing every candidate replaces 32 diverging 27-cell
+        // sweeps; a wide box (row or periodic seam) falls back to them.
+        const bool any_real = __any_sync(0xffffffffu, real);
+        int lo[3], hi[3], vol = any_real ? 1 : 0;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            // cells are < 2048 per axis; ghost lanes get neutral bounds
+            lo[d] = __reduce_min_sync(0xffffffffu, real ? cc[d] : 4096) - 1;
+            hi[d] = __reduce_max_sync(0xffffffffu, real ? cc[d] : -4096) + 1;
+            vol *= max(hi[d] - lo[d] + 1, 0);
+        }
+        if (vol > 0 && vol <= 64) {
+            for (int bz = lo[2]; bz <= hi[2]; ++bz) {
+                int z = bz;
+                if (sd.per[2]) {
+                    z = z < 0 ? z + sd.nc[2] : (z >= sd.nc[2] ? z - sd.nc[2] : z);
+                } else if (z < 0 || z >= sd.nc[2]) {
                     continue;
                 }
-                for (int dx = -1; dx <= 1; ++dx) {
-                    int x = cc[0] + dx;
-                    if (sd.per[0]) {
-                        x = x < 0 ? x + sd.nc[0] : (x >= sd.nc[0] ? x - sd.nc[0] : x);
-                    } else if (x < 0 || x >= sd.nc[0]) {
+                for (int by = lo[1]; by <= hi[1]; ++by) {
+                    int y = by;
+                    if (sd.per[1]) {
+                        y = y < 0 ? y + sd.nc[1] : (y >= sd.nc[1] ? y - sd.nc[1] : y);
+                    } else if (y < 0 || y >= sd.nc[1]) {
                         continue;
                     }
-                    const uint32_t code = uint32_t((dx + 1) + 3 * (dy + 1) + 9 * (dz + 1));
-                    // x_i - x_j = (o_i - o_j) - d * Lc
-                    const R sx = mul_rn(R(-dx), L[0]), sy = mul_rn(R(-dy), L[1]), sz = mul_rn(R(-dz), L[2]);
-                    const int2 rg = a.ranges[sd.cell_base + cell_lin(sd, x, y, z)];
-                    for (int j = rg.x; j < rg.y; ++j) {
-                        if (j == i) continue;
-                        const T4 q = a.pos[cur][j];
-                        const int tj = w_type(wbits(q.w));
-                        const float rl2 = rl2s[ty * 16 + tj];
-                        if (!(rl2 > 0.f)) continue;
-                        const R ex = add_rn(sub_rn(p.x, q.x), sx);
-                        const R ey = add_rn(sub_rn(p.y, q.y), sy);
-                        const R ez = add_rn(sub_rn(p.z, q.z), sz);
-                        const R r2 = add_rn(add_rn(mul_rn(ex, ex), mul_rn(ey, ey)), mul_rn(ez, ez));
-                        if (r2 < R(rl2)) {
-                            if (count < a.cap) a.nbr[int64_t(count) * n + i] = uint32_t(j) | (code << NB_SHIFT);
-                            ++count;
+                    for (int bx = lo[0]; bx <= hi[0]; ++bx) {
+                        int x = bx;
+                        if (sd.per[0]) {
+                            x = x < 0 ? x + sd.nc[0] : (x >= sd.nc[0] ? x - sd.nc[0] : x);
+                        } else if (x < 0 || x >= sd.nc[0]) {
+                            continue;
                         }
+                        const int dx = bx - cc[0], dy = by - cc[1], dz = bz - cc[2];
+                        const bool mine = real && dx >= -1 && dx <= 1 && dy >= -1 && dy <= 1 && dz >= -1 && dz <= 1;
+                        const int2 rg = a.ranges[sd.cell_base + cell_lin(sd, x, y, z)];
+                        for (int j = rg.x; j < rg.y; ++j)
+                            if (mine && j != i) test(j, dx, dy, dz);
+                    }
+                }
+            }
+        } else if (real) {
+            for (int dz = -1; dz <= 1; ++dz) {
+                int z = cc[2] + dz;
+                if (sd.per[2]) {
+                    z = z < 0 ? z + sd.nc[2] : (z >= sd.nc[2] ? z - sd.nc[2] : z);
+                } else if (z < 0 || z >= sd.nc[2]) {
+                    continue;
+                }
+                for (int dy = -1; dy <= 1; ++dy) {
+                    int y = cc[1] + dy;
+                    if (sd.per[1]) {
+                        y = y < 0 ? y + sd.nc[1] : (y >= sd.nc[1] ? y - sd.nc[1] : y);
+                    } else if (y < 0 || y >= sd.nc[1]) {
+                        continue;
+                    }
+                    for (int dx = -1; dx <= 1; ++dx) {
+                        int x = cc[0] + dx;
+                        if (sd.per[0]) {
+                            x = x < 0 ? x + sd.nc[0] : (x >= sd.nc[0] ? x - sd.nc[0] : x);
+                        } else if (x < 0 || x >= sd.nc[0]) {
+                            continue;
+                        }
+                        const int2 rg = a.ranges[sd.cell_base + cell_lin(sd, x, y, z)];
+                        for (int j = rg.x; j < rg.y; ++j)
+                            if (j != i) test(j, dx, dy, dz);
                     }
                 }
             }
         }
-        a.nnb[i] = min(count, a.cap);
+        a.nnb[i] = real ? min(count, a.cap) : 0;
         maxc = max(maxc, count);
     }
     // block max -> global max; last block finalises the rebuild
@@ -390,14 +434,27 @@ static int grid_for(int64_t n, int per_block = 256) {
     return int(g < 1 ? 1 : (g > cap ? cap : g));
 }
 
-template<class R> void launch_rebuild(const KArgs<R> &a, cudaStream_t st, bool gated) {
+template<class R> void launch_rebuild_stage(const KArgs<R> &a, cudaStream_t st, bool gated, int stage) {
     const int g = grid_for(a.npad);
-    k_rebin<R><<<g, 256, 0, st>>>(a, gated ? 1 : 0);
-    const int fin = radix_sort_pairs(const_cast<uint32_t **>(a.skey), const_cast<int **>(a.sval), a.counts,
-                                     a.digit_total, a.inv, a.npad, a.sort_passes, a.ntiles,
-                                     gated ? &a.S->rebuild : nullptr, st);
-    k_ranges_gather<R><<<g, 256, 0, st>>>(a, fin, gated ? 1 : 0);
-    k_nlist<R><<<grid_for(a.npad, 128), 128, 0, st>>>(a, gated ? 1 : 0);
+    switch (stage) {
+        case 0:
+            k_rebin<R><<<(a.npad + 255) / 256, 256, 0, st>>>(a, gated ? 1 : 0);
+            break;
+        case 1:
+            radix_sort_pairs(const_cast<uint32_t **>(a.skey), const_cast<int **>(a.sval), a.counts, a.digit_total,
+                             a.inv, a.npad, a.sort_passes, a.ntiles, gated ? &a.S->rebuild : nullptr, st);
+            break;
+        case 2:
+            k_ranges_gather<R><<<g, 256, 0, st>>>(a, a.sort_passes % 2, gated ? 1 : 0);
+            break;
+        default:
+            k_nlist<R><<<(a.npad + 127) / 128, 128, 0, st>>>(a, gated ? 1 : 0);
+            break;
+    }
+}
+
+template<class R> void launch_rebuild(const KArgs<R> &a, cudaStream_t st, bool gated) {
+    for (int k = 0; k < 4; ++k) launch_rebuild_stage<R>(a, st, gated, k);
 }
 
 /* ------------------------------------------------------------------------- */
@@ -533,6 +590,8 @@ void launch_morton(const double *p3, int64_t n, const double *b, uint32_t *keys,
 }
 
 template void launch_rebuild<float>(const KArgs<float> &, cudaStream_t, bool);
+template void launch_rebuild_stage<float>(const KArgs<float> &, cudaStream_t, bool, int);
+template void launch_rebuild_stage<double>(const KArgs<double> &, cudaStream_t, bool, int);
 template void launch_rebuild<double>(const KArgs<double> &, cudaStream_t, bool);
 template void launch_set_state<float>(const KArgs<float> &, const double *, const double *, const double *,
                                       const double *, int64_t, cudaStream_t);

@@ -20,13 +20,15 @@ namespace orbc {
 
 constexpr int NT = 6;            // particle types (src/forcefield_canonical.h:31-37)
 constexpr int GHOST = 15;        // type of padding slots
-constexpr int SYS_PAD = 256;     // slot padding per system == step-kernel block
+constexpr int SYS_PAD = 256;     // slot padding per system
+constexpr int STEP_BS = 128;     // threads per block of the force / integrator kernels (divides SYS_PAD)
 constexpr int MAX_BT = 8;        // bond types
 constexpr int MAX_DEG = 15;      // bonds / faces per particle (4-bit fields)
 constexpr uint32_t NB_MASK = (1u << 27) - 1u;
 constexpr int NB_SHIFT = 27;
 constexpr int MAX_SLOTS = 1 << 27;
 constexpr int NPART = 4;         // per-block partial sums: ke2, epot, maxd2, flags
+constexpr int MESH_CHUNK = 1024; // faces per block of the area / volume kernel
 
 enum : int {
     ERRB_NBR_OVERFLOW = 1,  // a neighbour list overflowed its capacity
@@ -66,6 +68,13 @@ __host__ __device__ inline int cy_of(int c) { return (c >> 11) & 2047; }
 __host__ __device__ inline int cz_of(int c) { return (c >> 22) & 1023; }
 constexpr int MAX_NC_XY = 2047, MAX_NC_Z = 1023;
 
+/* Neighbour list layout: warp-blocked ELL.  The entries of the 32 slots of a
+ * warp form one contiguous block of cap rows x 32 entries, so entry k of slot
+ * i is at nbr_index(i, k, cap); a warp's whole list is cap * 128 contiguous bytes. */
+__host__ __device__ inline int64_t nbr_index(int i, int k, int cap) {
+    return ((int64_t(i >> 5) * cap + k) << 5) | int64_t(i & 31);
+}
+
 struct BondSlot {
     int partner;  // slot of the other end
     int type;     // bond type (table index)
@@ -73,7 +82,8 @@ struct BondSlot {
 };
 
 template<class R> struct PairP {
-    R cutsq, cut, rep8, att4, alpha, aatt, ljcutsq, lj1, lj2, rep, att, pad;
+    R cutsq, cut, rep8, att4, alpha, aatt, ljcutsq, lj1, lj2, rep, att;
+    R anysq;  // max(cutsq, ljcutsq): the pair interacts somehow inside it
     int kind;
     int pad2;
 };
@@ -97,7 +107,7 @@ struct SysDev {
     unsigned cell_base;             // first global cell id; ncell + 1 ids (last = ghost cell)
     int off, npad, nreal;
     int face_begin, face_end;
-    int pad0;
+    int mblk_begin, mblk_end;       // blocks of the area / volume kernel (MESH_CHUNK faces each)
     double kv, V0, ka, A0, Q;
 };
 
@@ -113,7 +123,7 @@ struct SysState {
 struct Scalars {
     int cur, lp, rebuild, error;
     int max_nnb, out_of_grid, cond_hint, pad0;
-    unsigned int blk_counter, pad1, pad2, pad3;
+    unsigned int blk_counter, mesh_counter, pad2, pad3;
     long long step, rebuilds, since_rebuild, pad4;
 };
 
@@ -127,7 +137,10 @@ template<class R> struct KArgs {
     double *epart;           // per-slot energy (forces hook)
     int4 *faces;             // (a, b, c, sys) slots of the area/volume mesh
     int nfaces;
-    uint32_t *nbr;           // ELL neighbour list [cap][npad]
+    int nmblk;               // blocks of the area / volume kernel
+    int *mesh_blk_sys;       // system of each of those blocks
+    double *mesh_partial;    // [nmblk][2] area, volume
+    uint32_t *nbr;           // warp-blocked ELL neighbour list (nbr_index)
     int *nnb;
     int cap;
     int2 *ranges;            // cell -> [begin, end) of its slots
@@ -137,7 +150,7 @@ template<class R> struct KArgs {
     Scalars *S;
     SysDev *sys;
     SysState *ss;
-    int nsys, npad, nblk;
+    int nsys, npad, nblk;    // nblk: STEP_BS-slot blocks of the force / integrator kernels
     // radix sort scratch
     uint32_t *skey[2];
     int *sval[2];
@@ -148,18 +161,22 @@ template<class R> struct KArgs {
     R skin_half2;
     uint64_t seed;
     int rebuild_every;
-    int pad_i;
+    int variant;             // force-kernel form (see launch_step_langevin)
+    int carry_forces;        // forces / torques persist between kernels (Nose-Hoover)
     const FFDev<R> *ff;      // force-field tables (global; staged into shared memory per block)
 };
 
 // host-side launchers (explicitly instantiated for float and double)
 template<class R> void launch_rebuild(const KArgs<R> &a, cudaStream_t st, bool gated);
+// stage 0 rebin, 1 radix sort, 2 ranges + gather, 3 neighbour list
+template<class R> void launch_rebuild_stage(const KArgs<R> &a, cudaStream_t st, bool gated, int stage);
 template<class R> void launch_mesh(const KArgs<R> &a, cudaStream_t st);
 template<class R> void launch_step_langevin(const KArgs<R> &a, cudaStream_t st, bool energy);
 template<class R> void launch_nh_final(const KArgs<R> &a, cudaStream_t st, bool energy);
 template<class R> void launch_nh_initial(const KArgs<R> &a, cudaStream_t st);
 template<class R> void launch_nh_prologue(const KArgs<R> &a, cudaStream_t st);
 template<class R> void launch_forces(const KArgs<R> &a, cudaStream_t st);
+
 template<class R> void launch_set_state(const KArgs<R> &a, const double *x, const double *n, const double *v,
                                         const double *o, int64_t nhome, cudaStream_t st);
 template<class R> void launch_download(const KArgs<R> &a, double *x, double *n, double *v, double *o, double *f,

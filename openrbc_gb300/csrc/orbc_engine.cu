@@ -140,6 +140,7 @@ class EngineBase {
     virtual int cells(int sys, double *lo3, double *lc3, int *nc3, int *cell, double *off3, int *slot) = 0;
     virtual int rebuild() = 0;
     virtual int profile(int nsteps, orbc_profile *out) = 0;
+    virtual int autotune(int trial_steps, orbc_tune_trial *trials, int max_trials, int *ntrials) = 0;
     double last_ms = 0;
     int64_t last_launches = 0;
 };
@@ -202,6 +203,15 @@ template<class R> class Engine : public EngineBase {
         }
         drop_graph();
         nh_primed = false;
+        if (!relayout_in_progress) {  // topology copy for re-layouts (autotune)
+            topo.descs.assign(descs, descs + nsys);
+            topo.offsets.assign(offsets, offsets + nsys + 1);
+            topo.type.assign(type, type + n);
+            topo.tag.assign(tag, tag + n);
+            topo.bonds.assign(bonds3 ? bonds3 : nullptr, bonds3 ? bonds3 + 3 * nb : nullptr);
+            topo.bond_r0.assign(bond_r0 ? bond_r0 : nullptr, bond_r0 ? bond_r0 + nb : nullptr);
+            topo.faces.assign(faces3 ? faces3 : nullptr, faces3 ? faces3 + 3 * nf : nullptr);
+        }
         this->nsys = nsys;
         nhome = n;
         const FFHost &F = ffh();
@@ -287,14 +297,15 @@ template<class R> class Engine : public EngineBase {
         if (off >= MAX_SLOTS) return fail(ORBC_ERR_ARG, "upload: more than 2^27 particle slots");
         if (cbase >= (uint64_t(1) << 32) - 1) return fail(ORBC_ERR_ARG, "upload: more than 2^32 cells");
         npad = int(off);
-        nblk = npad / SYS_PAD;
+        nblk = npad / STEP_BS;
+        const int nb256 = npad / SYS_PAD;
         total_cells = cbase;
 
         // ---- slots
         std::vector<T4> hpos(static_cast<size_t>(npad)), hnrm(static_cast<size_t>(npad)), hvel(static_cast<size_t>(npad)), homg(static_cast<size_t>(npad)),
             hzero(static_cast<size_t>(npad));
         std::vector<int> hcell(size_t(npad), 0), htag(size_t(npad), -1), hhome(size_t(npad), -1),
-            hsoh(static_cast<size_t>(n)), hbs(static_cast<size_t>(nblk));
+            hsoh(static_cast<size_t>(n)), hbs(static_cast<size_t>(nb256));
         std::vector<int> wbitsv(size_t(npad), GHOST);
         std::memset(hzero.data(), 0, hzero.size() * sizeof(T4));
         for (int s = 0; s < nsys; ++s) {
@@ -370,6 +381,16 @@ template<class R> class Engine : public EngineBase {
             }
             hsys[size_t(s)].face_end = int(hfaces.size());
         }
+        // blocks of the area / volume kernel: MESH_CHUNK faces of one system each
+        std::vector<int> hmbs;
+        for (int s = 0; s < nsys; ++s) {
+            SysDev &sd = hsys[size_t(s)];
+            const int nfs = sd.face_end - sd.face_begin;
+            sd.mblk_begin = int(hmbs.size());
+            for (int k = 0; k < (nfs + MESH_CHUNK - 1) / MESH_CHUNK; ++k) hmbs.push_back(s);
+            sd.mblk_end = int(hmbs.size());
+        }
+        nmblk = int(hmbs.size());
         maxf = 0;
         for (int d : fdeg) maxf = std::max(maxf, d);
         if (maxf > MAX_DEG) return fail(ORBC_ERR_ARG, "upload: more than 15 faces on one vertex");
@@ -398,12 +419,13 @@ template<class R> class Engine : public EngineBase {
         }
         ntiles = sort_tiles(npad);
         if (epart.alloc(size_t(npad)) || faces.alloc(hfaces.size()) || ranges.alloc(size_t(total_cells)) ||
-            soh.alloc(size_t(n)) || blk_sys.alloc(size_t(nblk)) || partial.alloc(size_t(nblk) * NPART) ||
+            soh.alloc(size_t(n)) || blk_sys.alloc(size_t(nb256)) || partial.alloc(size_t(nblk) * NPART) ||
             Sd.alloc(1) || sysd.alloc(size_t(nsys)) || ssd.alloc(size_t(nsys)) || counts.alloc(size_t(256) * ntiles) ||
             dtot.alloc(256) || invd.alloc(size_t(npad)) || ffd.alloc(1) || nnb.alloc(size_t(npad)) ||
-            stage.alloc(size_t(n) * 12))
+            stage.alloc(size_t(n) * 12) || mesh_bs.alloc(hmbs.size()) || mesh_part.alloc(hmbs.size() * 2 + 2))
             return fail(ORBC_ERR_NOMEM, "upload: device allocation failed");
         cap = P.max_neighbors > 0 ? P.max_neighbors : 64;
+
         if (nbr.alloc(size_t(cap) * size_t(npad))) return fail(ORBC_ERR_NOMEM, "upload: neighbour list allocation failed");
 
         CK(cudaMemcpyAsync(pos[0].p, hpos.data(), hpos.size() * sizeof(T4), cudaMemcpyHostToDevice, st));
@@ -420,6 +442,8 @@ template<class R> class Engine : public EngineBase {
         CK(cudaMemcpyAsync(fslot[0].p, hfs.data(), hfs.size() * sizeof(int2), cudaMemcpyHostToDevice, st));
         if (!hfaces.empty())
             CK(cudaMemcpyAsync(faces.p, hfaces.data(), hfaces.size() * sizeof(int4), cudaMemcpyHostToDevice, st));
+        if (!hmbs.empty())
+            CK(cudaMemcpyAsync(mesh_bs.p, hmbs.data(), hmbs.size() * sizeof(int), cudaMemcpyHostToDevice, st));
         CK(cudaMemcpyAsync(soh.p, hsoh.data(), hsoh.size() * sizeof(int), cudaMemcpyHostToDevice, st));
         CK(cudaMemcpyAsync(blk_sys.p, hbs.data(), hbs.size() * sizeof(int), cudaMemcpyHostToDevice, st));
         CK(cudaMemcpyAsync(sysd.p, hsys.data(), hsys.size() * sizeof(SysDev), cudaMemcpyHostToDevice, st));
@@ -726,7 +750,7 @@ template<class R> class Engine : public EngineBase {
             const int h = hh[size_t(p)];
             if (h < 0) continue;
             for (int k = 0; k < hn[size_t(p)]; ++k) {
-                const uint32_t ent = hl[size_t(k) * npad + size_t(p)];
+                const uint32_t ent = hl[size_t(nbr_index(p, k, cap))];
                 per[size_t(h)].push_back(hh[size_t(ent & NB_MASK)]);
             }
             std::sort(per[size_t(h)].begin(), per[size_t(h)].end());
@@ -787,9 +811,10 @@ template<class R> class Engine : public EngineBase {
             int rc = step(0, nullptr);
             if (rc) return rc;
         }
-        cudaEvent_t ev[5];
+        cudaEvent_t ev[5], er[5];
         for (auto &e : ev) CK(cudaEventCreate(&e));
-        double t_step = 0, t_reb = 0, t_gate = 0, t_mesh = 0;
+        for (auto &e : er) CK(cudaEventCreate(&e));
+        double t_step = 0, t_reb = 0, t_gate = 0, t_mesh = 0, t_stage[4] = {0, 0, 0, 0};
         int64_t nreb = 0;
         for (int k = 0; k < nsteps; ++k) {
             Scalars b4;
@@ -797,7 +822,11 @@ template<class R> class Engine : public EngineBase {
             CK(cudaEventRecord(ev[0], st));
             if (P.integrator == ORBC_INT_NOSE_HOOVER) launch_nh_initial<R>(a, st);
             CK(cudaEventRecord(ev[1], st));
-            launch_rebuild<R>(a, st, true);
+            for (int g = 0; g < 4; ++g) {
+                CK(cudaEventRecord(er[g], st));
+                launch_rebuild_stage<R>(a, st, true, g);
+            }
+            CK(cudaEventRecord(er[4], st));
             CK(cudaEventRecord(ev[2], st));
             if (has_mesh) launch_mesh<R>(a, st);
             CK(cudaEventRecord(ev[3], st));
@@ -818,12 +847,18 @@ template<class R> class Engine : public EngineBase {
             if (af.rebuilds > b4.rebuilds) {
                 t_reb += m12;
                 ++nreb;
+                for (int g = 0; g < 4; ++g) {
+                    float mg;
+                    CK(cudaEventElapsedTime(&mg, er[g], er[g + 1]));
+                    t_stage[g] += mg;
+                }
             } else {
                 t_gate += m12;
             }
             t_mesh += m23;
             t_step += m34 + m01;
         }
+        for (auto &e : er) cudaEventDestroy(e);
         for (auto &e : ev) cudaEventDestroy(e);
         out->steps = nsteps;
         out->rebuilds = nreb;
@@ -831,6 +866,10 @@ template<class R> class Engine : public EngineBase {
         out->rebuild_ms = nreb ? t_reb / nreb : 0.0;
         out->gate_ms = nsteps > nreb ? t_gate / double(nsteps - nreb) : 0.0;
         out->mesh_ms = t_mesh / nsteps;
+        out->rebin_ms = nreb ? t_stage[0] / nreb : 0.0;
+        out->sort_ms = nreb ? t_stage[1] / nreb : 0.0;
+        out->gather_ms = nreb ? t_stage[2] / nreb : 0.0;
+        out->nlist_ms = nreb ? t_stage[3] / nreb : 0.0;
         // neighbour statistics of the current list
         Scalars hs;
         CK(cudaMemcpy(&hs, Sd.p, sizeof(Scalars), cudaMemcpyDeviceToHost));
@@ -852,7 +891,86 @@ template<class R> class Engine : public EngineBase {
         return ORBC_OK;
     }
 
+    /* Pick the neighbour-list skin and the force-kernel form by timing short
+     * trials from one snapshot of the state; the snapshot (positions,
+     * orientations, velocities, angular velocities, step counter, thermostat)
+     * is restored afterwards, so tuning does not advance the simulation. */
+    int autotune(int trial_steps, orbc_tune_trial *trials, int max_trials, int *ntrials) override {
+        if (!uploaded) return fail(ORBC_ERR_STATE, "autotune before upload");
+        if (trial_steps < 1) return fail(ORBC_ERR_ARG, "autotune: need trial_steps >= 1");
+        const size_t m = size_t(nhome) * 3;
+        std::vector<double> x(m), nv(m), v(m), o(m);
+        int rc = download(x.data(), nv.data(), v.data(), o.data());
+        if (rc) return rc;
+        Scalars hs;
+        CK(cudaMemcpy(&hs, Sd.p, sizeof(Scalars), cudaMemcpyDeviceToHost));
+        std::vector<SysState> hss(topo.descs.size());
+        CK(cudaMemcpy(hss.data(), ssd.p, hss.size() * sizeof(SysState), cudaMemcpyDeviceToHost));
+        for (size_t k = 0; k < hss.size(); ++k) topo.descs[k].zeta = hss[k].zeta;
+        const double skins[] = {0.3, 0.45, 0.6, 0.8, 1.0};
+        const int variants[] = {0, 1, 2, 3};
+        double best_ms = 1e300, best_skin = P.skin;
+        int best_var = P.kernel_variant, nt = 0;
+        for (double sk : skins) {
+            for (int var : variants) {
+                P.skin = sk;
+                P.kernel_variant = var;
+                rc = relayout(x, nv, v, o, hs.step);
+                if (rc) return rc;
+                rc = step(3, nullptr);  // warm: builds the graph
+                if (rc) return rc;
+                Scalars b4;
+                CK(cudaMemcpy(&b4, Sd.p, sizeof(Scalars), cudaMemcpyDeviceToHost));
+                rc = step(trial_steps, nullptr);
+                if (rc) return rc;
+                Scalars af;
+                CK(cudaMemcpy(&af, Sd.p, sizeof(Scalars), cudaMemcpyDeviceToHost));
+                const double ms = last_ms / trial_steps;
+                if (trials && nt < max_trials) {
+                    trials[nt].skin = sk;
+                    trials[nt].variant = var;
+                    trials[nt].ms_per_step = ms;
+                    trials[nt].rebuilds_per_step = double(af.rebuilds - b4.rebuilds) / trial_steps;
+                }
+                ++nt;
+                if (ms < best_ms) {
+                    best_ms = ms;
+                    best_skin = sk;
+                    best_var = var;
+                }
+            }
+        }
+        if (ntrials) *ntrials = nt;
+        P.skin = best_skin;
+        P.kernel_variant = best_var;
+        return relayout(x, nv, v, o, hs.step);
+    }
+
    private:
+    struct Topology {
+        std::vector<orbc_system_desc> descs;
+        std::vector<int64_t> offsets;
+        std::vector<int> type, tag, bonds, faces;
+        std::vector<double> bond_r0;
+    } topo;
+    bool relayout_in_progress = false;
+
+    /* Rebuild the whole device layout for the current parameters from a host
+     * snapshot of the state, then restore the step counter. */
+    int relayout(const std::vector<double> &x, const std::vector<double> &nv, const std::vector<double> &v,
+                 const std::vector<double> &o, long long step_counter) {
+        relayout_in_progress = true;
+        const size_t nb = topo.bonds.size() / 3, nf = topo.faces.size() / 3;
+        int rc = upload(int(topo.descs.size()), topo.descs.data(), topo.offsets.data(), x.data(), nv.data(), v.data(),
+                        o.data(), topo.type.data(), topo.tag.data(), topo.type.size(),
+                        nb ? topo.bonds.data() : nullptr, topo.bond_r0.empty() ? nullptr : topo.bond_r0.data(), nb,
+                        nf ? topo.faces.data() : nullptr, nf);
+        relayout_in_progress = false;
+        if (rc) return rc;
+        CK(cudaMemcpy(&Sd.p->step, &step_counter, sizeof(step_counter), cudaMemcpyHostToDevice));
+        return ORBC_OK;
+    }
+
     static T4 mk4(R x, R y, R z) {
         T4 v;
         v.x = x;
@@ -901,6 +1019,7 @@ template<class R> class Engine : public EngineBase {
             q.ljcutsq = R(F.ljcutsq[k]);
             q.lj1 = R(F.lj1[k]);
             q.lj2 = R(F.lj2[k]);
+            q.anysq = R(std::max(F.cutsq[k], F.ljcutsq[k]));
         }
         for (int t = 0; t < NT; ++t) {
             const double gam = 6.0 * M_PI * P.eta * F.radius[t];  // src/integrate_langevin.h:110-114
@@ -947,6 +1066,9 @@ template<class R> class Engine : public EngineBase {
         a.epart = epart.p;
         a.faces = faces.p;
         a.nfaces = nfaces;
+        a.nmblk = nmblk;
+        a.mesh_blk_sys = mesh_bs.p;
+        a.mesh_partial = mesh_part.p;
         a.nbr = nbr.p;
         a.nnb = nnb.p;
         a.cap = cap;
@@ -970,6 +1092,8 @@ template<class R> class Engine : public EngineBase {
         a.skin_half2 = R(0.25 * P.skin * P.skin);
         a.seed = P.seed;
         a.rebuild_every = P.rebuild_every;
+        a.variant = P.kernel_variant;
+        a.carry_forces = P.integrator == ORBC_INT_NOSE_HOOVER ? 1 : 0;
         a.ff = ffd.p;
     }
 
@@ -1002,6 +1126,7 @@ template<class R> class Engine : public EngineBase {
     int grow_capacity(int need, bool rebuild_now = true) {
         int nc = std::max(cap, int(std::ceil(need * 1.3 / 8.0)) * 8);
         if (nc <= cap) nc = cap + 16;
+
         drop_graph();
         if (nbr.alloc(size_t(nc) * size_t(npad))) return fail(ORBC_ERR_NOMEM, "neighbour list allocation failed");
         cap = nc;
@@ -1029,7 +1154,7 @@ template<class R> class Engine : public EngineBase {
     bool graph_cond = false;
     int graph_steps = 0;
     bool uploaded = false, nh_primed = false, has_mesh = false;
-    int nsys = 0, npad = 0, nblk = 0, cap = 0, passes = 4, ntiles = 1, maxb = 0, maxf = 0, nfaces = 0;
+    int nsys = 0, npad = 0, nblk = 0, cap = 0, passes = 4, ntiles = 1, maxb = 0, maxf = 0, nfaces = 0, nmblk = 0;
     int64_t nhome = 0;
     uint64_t total_cells = 0;
     std::vector<SysDev> hsys;
@@ -1042,7 +1167,8 @@ template<class R> class Engine : public EngineBase {
     DevBuf<double> epart, partial, stage;
     DevBuf<int4> faces;
     DevBuf<int2> ranges;
-    DevBuf<int> soh, blk_sys, counts, dtot, invd, nnb;
+    DevBuf<int> soh, blk_sys, counts, dtot, invd, nnb, mesh_bs;
+    DevBuf<double> mesh_part;
     DevBuf<uint32_t> nbr;
     DevBuf<Scalars> Sd;
     DevBuf<SysDev> sysd;
@@ -1098,7 +1224,8 @@ int orbc_gpu_create(const orbc_params *p, orbc_handle **out) {
     }
     *out = nullptr;
     if (!(p->dt > 0) || p->skin < 0 || (p->precision != ORBC_PREC_FP64 && p->precision != ORBC_PREC_MIXED) ||
-        (p->integrator != ORBC_INT_LANGEVIN && p->integrator != ORBC_INT_NOSE_HOOVER)) {
+        (p->integrator != ORBC_INT_LANGEVIN && p->integrator != ORBC_INT_NOSE_HOOVER) ||
+        (p->kernel_variant < 0 || p->kernel_variant > 3)) {
         g_last_error = "create: invalid parameters";
         return ORBC_ERR_ARG;
     }
@@ -1185,6 +1312,10 @@ int orbc_gpu_last_timing(orbc_handle *h, double *ms, int64_t *launches) {
 
 int orbc_gpu_profile(orbc_handle *h, int nsteps, orbc_profile *out) {
     return h ? h->e->profile(nsteps, out) : ORBC_ERR_ARG;
+}
+
+int orbc_gpu_autotune(orbc_handle *h, int trial_steps, orbc_tune_trial *trials, int max_trials, int *ntrials) {
+    return h ? h->e->autotune(trial_steps, trials, max_trials, ntrials) : ORBC_ERR_ARG;
 }
 
 int orbc_gpu_destroy(orbc_handle *h) {

@@ -108,8 +108,8 @@ __device__ __forceinline__ void repf(const PairP<R> &P, R dx, R dy, R dz, R r2, 
 
 /* Dispatch of src/compute_pairwise_fused.h:91-236 for a non lipid-lipid pair. */
 template<class R, bool E>
-__device__ __noinline__ void pair_general(const PairP<R> &P, R dx, R dy, R dz, R r2, R nix, R niy, R niz, R njx,
-                                          R njy, R njz, R3<R> &f, R3<R> &t, R &e) {
+__device__ __forceinline__ void pair_general_body(const PairP<R> &P, R dx, R dy, R dz, R r2, R nix, R niy, R niz,
+                                                  R njx, R njy, R njz, R3<R> &f, R3<R> &t, R &e) {
     if (!(r2 > R(1e-5))) return;
     if (r2 < P.cutsq) {
         if (P.kind == PAIR_ANISO)
@@ -119,6 +119,20 @@ __device__ __noinline__ void pair_general(const PairP<R> &P, R dx, R dy, R dz, R
     } else if (r2 < P.ljcutsq) {
         ljf<R, E>(P, dx, dy, dz, r2, f, e);
     }
+}
+template<class R, bool E>
+__device__ __noinline__ void pair_general_call(const PairP<R> &P, R dx, R dy, R dz, R r2, R nix, R niy, R niz,
+                                               R njx, R njy, R njz, R3<R> &f, R3<R> &t, R &e) {
+    pair_general_body<R, E>(P, dx, dy, dz, r2, nix, niy, niz, njx, njy, njz, f, t, e);
+}
+/* INL: inline the rare non-lipid path (more registers, no call) or call it. */
+template<class R, bool E, bool INL>
+__device__ __forceinline__ void pair_general(const PairP<R> &P, R dx, R dy, R dz, R r2, R nix, R niy, R niz, R njx,
+                                             R njy, R njz, R3<R> &f, R3<R> &t, R &e) {
+    if (INL)
+        pair_general_body<R, E>(P, dx, dy, dz, r2, nix, niy, niz, njx, njy, njz, f, t, e);
+    else
+        pair_general_call<R, E>(P, dx, dy, dz, r2, nix, niy, niz, njx, njy, njz, f, t, e);
 }
 
 __device__ __forceinline__ int wrap_delta(int d, int n) {
@@ -177,6 +191,16 @@ __device__ __forceinline__ R bond_kappa(const BondP<R> &B, R r0, R r, R &e, int 
     }
 }
 
+/* Bring this warp's block of neighbour entries (cap rows of 128 B, read
+ * once per step) into L1 ahead of the pair loop, so the loop's entry loads do
+ * not wait on DRAM.  All 32 lanes must call it. */
+__device__ __forceinline__ void prefetch_warp_list(const uint32_t *nbr, int i, int cap, int cnt) {
+    const int rows = __reduce_max_sync(0xffffffffu, unsigned(cnt));
+    const uint32_t *base = nbr + nbr_index(i & ~31, 0, cap);
+    for (int r = int(threadIdx.x & 31); r < rows; r += 32)
+        asm volatile("prefetch.global.L1 [%0];" ::"l"(base + 32 * r));
+}
+
 template<class R> __device__ __forceinline__ void stage_ff(FFDev<R> *dst, const FFDev<R> *src) {
     const int nw = int(sizeof(FFDev<R>) / sizeof(int));
     const int *s = reinterpret_cast<const int *>(src);
@@ -197,8 +221,9 @@ template<class R> __device__ __forceinline__ void init_shift(typename Vec<R>::T4
     __syncthreads();
 }
 
-/* All forces and torques on particle slot i. */
-template<class R, bool E>
+/* All forces and torques on particle slot i: pair terms over its neighbour
+ * list (variant V, see launch_step_langevin), bonds, mesh constraint. */
+template<class R, bool E, int V>
 __device__ __forceinline__ void particle_forces(const KArgs<R> &a, const FFDev<R> &F, int i, int cur, int lp, int w,
                                                 const typename Vec<R>::T4 &pi, const typename Vec<R>::T4 &ni,
                                                 const SysDev &sd, const SysState &ss,
@@ -209,38 +234,83 @@ __device__ __forceinline__ void particle_forces(const KArgs<R> &a, const FFDev<R
     const R Lx = R(sd.Lc[0]), Ly = R(sd.Lc[1]), Lz = R(sd.Lc[2]);
     const T4 *__restrict__ pos = a.pos[cur];
     const T4 *__restrict__ nrm = a.nrm[cur];
-    const uint32_t *__restrict__ nb = a.nbr + i;
+    const uint32_t *__restrict__ nb = a.nbr + nbr_index(i, 0, a.cap);
     const int cnt = a.nnb[i];
-    const int64_t stride = a.npad;
+    const int64_t stride = 32;
     const PairP<R> &LL = F.pair[0];
     const R ll_cutsq = LL.cutsq, ll_cut = LL.cut, ll_alpha = LL.alpha, ll_aatt = LL.aatt;
     const R ll_rep8 = LL.rep8, ll_att4 = LL.att4, ll_rep = LL.rep, ll_att = LL.att;
-#pragma unroll 2
-    for (int k = 0; k < cnt; ++k) {
-        const uint32_t ent = __ldg(nb + int64_t(k) * stride);
-        const int j = int(ent & NB_MASK);
-        const T4 s = sh[ent >> NB_SHIFT];
-        const T4 pj = ldg4<R>(pos + j);
-        const T4 nj = ldg4<R>(nrm + j);
-        const R dx = (pi.x - pj.x) + s.x * Lx;
-        const R dy = (pi.y - pj.y) + s.y * Ly;
-        const R dz = (pi.z - pj.z) + s.z * Lz;
-        const R r2 = dx * dx + dy * dy + dz * dz;
-        const int tj = w_type(wbits(pj.w));
-        if ((ty | tj) == 0) {
-            if (r2 < ll_cutsq && r2 > R(1e-5)) {
-                PairP<R> P;
-                P.cut = ll_cut;
-                P.alpha = ll_alpha;
-                P.aatt = ll_aatt;
-                P.rep8 = ll_rep8;
-                P.att4 = ll_att4;
-                P.rep = ll_rep;
-                P.att = ll_att;
-                aniso<R, E>(P, dx, dy, dz, r2, ni.x, ni.y, ni.z, nj.x, nj.y, nj.z, f, t, e);
+    if (V & 1) {
+        /* software-pipelined pass: the entry two ahead and the gathers one
+         * ahead are in flight while the current pair is evaluated */
+        uint32_t e1 = cnt > 0 ? __ldg(nb) : 0u;
+        uint32_t e2 = cnt > 1 ? __ldg(nb + stride) : 0u;
+        T4 pn, nn;
+        if (cnt > 0) {
+            pn = ldg4<R>(pos + int(e1 & NB_MASK));
+            nn = ldg4<R>(nrm + int(e1 & NB_MASK));
+        }
+        for (int k = 0; k < cnt; ++k) {
+            const uint32_t ent = e1;
+            const T4 pj = pn, nj = nn;
+            e1 = e2;
+            if (k + 2 < cnt) e2 = __ldg(nb + int64_t(k + 2) * stride);
+            if (k + 1 < cnt) {
+                pn = ldg4<R>(pos + int(e1 & NB_MASK));
+                nn = ldg4<R>(nrm + int(e1 & NB_MASK));
             }
-        } else {
-            pair_general<R, E>(F.pair[ty * NT + tj], dx, dy, dz, r2, ni.x, ni.y, ni.z, nj.x, nj.y, nj.z, f, t, e);
+            const T4 s = sh[ent >> NB_SHIFT];
+            const R dx = (pi.x - pj.x) + s.x * Lx;
+            const R dy = (pi.y - pj.y) + s.y * Ly;
+            const R dz = (pi.z - pj.z) + s.z * Lz;
+            const R r2 = dx * dx + dy * dy + dz * dz;
+            const int tj = w_type(wbits(pj.w));
+            if ((ty | tj) == 0) {
+                if (r2 < ll_cutsq && r2 > R(1e-5)) {
+                    PairP<R> P;
+                    P.cut = ll_cut;
+                    P.alpha = ll_alpha;
+                    P.aatt = ll_aatt;
+                    P.rep8 = ll_rep8;
+                    P.att4 = ll_att4;
+                    P.rep = ll_rep;
+                    P.att = ll_att;
+                    aniso<R, E>(P, dx, dy, dz, r2, ni.x, ni.y, ni.z, nj.x, nj.y, nj.z, f, t, e);
+                }
+            } else {
+                pair_general<R, E, (V & 2) != 0>(F.pair[ty * NT + tj], dx, dy, dz, r2, ni.x, ni.y, ni.z, nj.x, nj.y, nj.z, f, t,
+                                   e);
+            }
+        }
+    } else {
+#pragma unroll 2
+        for (int k = 0; k < cnt; ++k) {
+            const uint32_t ent = __ldg(nb + int64_t(k) * stride);
+            const int j = int(ent & NB_MASK);
+            const T4 s = sh[ent >> NB_SHIFT];
+            const T4 pj = ldg4<R>(pos + j);
+            const T4 nj = ldg4<R>(nrm + j);
+            const R dx = (pi.x - pj.x) + s.x * Lx;
+            const R dy = (pi.y - pj.y) + s.y * Ly;
+            const R dz = (pi.z - pj.z) + s.z * Lz;
+            const R r2 = dx * dx + dy * dy + dz * dz;
+            const int tj = w_type(wbits(pj.w));
+            if ((ty | tj) == 0) {
+                if (r2 < ll_cutsq && r2 > R(1e-5)) {
+                    PairP<R> P;
+                    P.cut = ll_cut;
+                    P.alpha = ll_alpha;
+                    P.aatt = ll_aatt;
+                    P.rep8 = ll_rep8;
+                    P.att4 = ll_att4;
+                    P.rep = ll_rep;
+                    P.att = ll_att;
+                    aniso<R, E>(P, dx, dy, dz, r2, ni.x, ni.y, ni.z, nj.x, nj.y, nj.z, f, t, e);
+                }
+            } else {
+                pair_general<R, E, (V & 2) != 0>(F.pair[ty * NT + tj], dx, dy, dz, r2, ni.x, ni.y, ni.z, nj.x, nj.y, nj.z, f, t,
+                                   e);
+            }
         }
     }
     // bonds
@@ -248,7 +318,7 @@ __device__ __forceinline__ void particle_forces(const KArgs<R> &a, const FFDev<R
     if (bd) {
         const int ci = a.cell[lp][i];
         for (int b = 0; b < bd; ++b) {
-            const BondSlot bs = a.bond[lp][int64_t(b) * stride + i];
+            const BondSlot bs = a.bond[lp][int64_t(b) * a.npad + i];
             const T4 pj = pos[bs.partner];
             R dx, dy, dz;
             rel_pos<R>(sd, a.cell[lp][bs.partner], ci, pj, pi, dx, dy, dz);
@@ -265,7 +335,7 @@ __device__ __forceinline__ void particle_forces(const KArgs<R> &a, const FFDev<R
         const int ci = a.cell[lp][i];
         const R cv = R(ss.cv) * R(1.0 / 6.0), ca = R(ss.ca) * R(0.5);
         for (int b = 0; b < fd; ++b) {
-            const int2 fs = a.fslot[lp][int64_t(b) * stride + i];
+            const int2 fs = a.fslot[lp][int64_t(b) * a.npad + i];
             R bx, by, bz, cx, cy, cz;
             rel_pos<R>(sd, a.cell[lp][fs.x], ci, pos[fs.x], pi, bx, by, bz);
             rel_pos<R>(sd, a.cell[lp][fs.y], ci, pos[fs.y], pi, cx, cy, cz);
@@ -301,6 +371,8 @@ __device__ __forceinline__ void philox3(uint32_t c0, uint32_t c1, uint32_t c2, u
 }
 template<class R> __device__ __forceinline__ R u11(uint32_t u) { return R(u >> 8) * R(1.0 / 8388608.0) - R(1); }
 
+constexpr int STEP_WARPS = STEP_BS / 32;
+
 enum { MODE_LANGEVIN = 0, MODE_NH_FINAL = 1, MODE_NH_INITIAL = 2, MODE_FORCES = 3 };
 
 /* Block partial sums -> per-system totals in the last block (fixed order). */
@@ -330,7 +402,7 @@ __device__ __forceinline__ void finish(const KArgs<R> &a, double ke, double ep, 
         double k = 0, e = 0;
         float m = 0;
         int fl = 0;
-        for (int w = 0; w < 8; ++w) {
+        for (int w = 0; w < STEP_WARPS; ++w) {
             k += sk[w];
             e += se[w];
             m = fmaxf(m, sm[w]);
@@ -349,9 +421,9 @@ __device__ __forceinline__ void finish(const KArgs<R> &a, double ke, double ep, 
     if (!last) return;
     __threadfence();
     // per system: one warp per system, lanes stride over the system's blocks
-    for (int s = warp; s < a.nsys; s += 8) {
+    for (int s = warp; s < a.nsys; s += STEP_WARPS) {
         const SysDev &sd = a.sys[s];
-        const int b0 = sd.off / SYS_PAD, b1 = (sd.off + sd.npad) / SYS_PAD;
+        const int b0 = sd.off / STEP_BS, b1 = (sd.off + sd.npad) / STEP_BS;
         double k = 0, e = 0;
         for (int b = b0 + lane; b < b1; b += 32) {
             k += __ldcg(a.partial + int64_t(b) * NPART);
@@ -396,7 +468,7 @@ __device__ __forceinline__ void finish(const KArgs<R> &a, double ke, double ep, 
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        for (int w = 0; w < 8; ++w) {
+        for (int w = 0; w < STEP_WARPS; ++w) {
             m = fmaxf(m, sm[w]);
             fl |= sf[w];
         }
@@ -417,7 +489,7 @@ __device__ __forceinline__ void finish(const KArgs<R> &a, double ke, double ep, 
     }
 }
 
-template<class R, bool E> __global__ void __launch_bounds__(256) k_step_langevin(KArgs<R> a) {
+template<class R, bool E, int V> __global__ void __launch_bounds__(STEP_BS, (V & 2) ? 6 : 8) k_step_langevin(KArgs<R> a) {
     using T4 = typename Vec<R>::T4;
     __shared__ T4 sh[27];
     __shared__ FFDev<R> F;
@@ -425,10 +497,11 @@ template<class R, bool E> __global__ void __launch_bounds__(256) k_step_langevin
     init_shift<R>(sh);
     const int cur = __ldcg(&a.S->cur), lp = __ldcg(&a.S->lp);
     const long long step = __ldcg(&a.S->step);
-    const int i = blockIdx.x * 256 + threadIdx.x;
-    const int s = a.blk_sys[blockIdx.x];
+    const int i = blockIdx.x * STEP_BS + threadIdx.x;
+    const int s = a.blk_sys[(blockIdx.x * STEP_BS) / SYS_PAD];
     const SysDev &sd = a.sys[s];
     const T4 pi = a.pos[cur][i];
+    prefetch_warp_list(a.nbr, i, a.cap, a.nnb[i]);
     const int w = wbits(pi.w);
     const int ty = w_type(w);
     double ke = 0, ep = 0;
@@ -438,7 +511,7 @@ template<class R, bool E> __global__ void __launch_bounds__(256) k_step_langevin
         const T4 ni = a.nrm[cur][i];
         R3<R> f = {0, 0, 0}, t = {0, 0, 0};
         R e = 0;
-        particle_forces<R, E>(a, F, i, cur, lp, w, pi, ni, sd, a.ss[s], sh, f, t, e, flags);
+        particle_forces<R, E, V>(a, F, i, cur, lp, w, pi, ni, sd, a.ss[s], sh, f, t, e, flags);
         const R dt = R(a.dt);
         T4 v = a.vel[lp][i], o = a.omg[lp][i];
         // ROTATION: t <- n x t; o += dt t; n <- normalize(n + (o x n) dt)
@@ -484,17 +557,18 @@ template<class R, bool E> __global__ void __launch_bounds__(256) k_step_langevin
     finish<R>(a, ke, ep, md2, flags, MODE_LANGEVIN, 1);
 }
 
-template<class R, bool E> __global__ void __launch_bounds__(256) k_nh_final(KArgs<R> a, int count_step) {
+template<class R, bool E, int V> __global__ void __launch_bounds__(STEP_BS, (V & 2) ? 6 : 8) k_nh_final(KArgs<R> a, int count_step) {
     using T4 = typename Vec<R>::T4;
     __shared__ T4 sh[27];
     __shared__ FFDev<R> F;
     stage_ff<R>(&F, a.ff);
     init_shift<R>(sh);
     const int cur = __ldcg(&a.S->cur), lp = __ldcg(&a.S->lp);
-    const int i = blockIdx.x * 256 + threadIdx.x;
-    const int s = a.blk_sys[blockIdx.x];
+    const int i = blockIdx.x * STEP_BS + threadIdx.x;
+    const int s = a.blk_sys[(blockIdx.x * STEP_BS) / SYS_PAD];
     const SysDev &sd = a.sys[s];
     const T4 pi = a.pos[cur][i];
+    prefetch_warp_list(a.nbr, i, a.cap, a.nnb[i]);
     const int w = wbits(pi.w);
     const int ty = w_type(w);
     double ke = 0, ep = 0;
@@ -503,7 +577,7 @@ template<class R, bool E> __global__ void __launch_bounds__(256) k_nh_final(KArg
         const T4 ni = a.nrm[cur][i];
         R3<R> f = {0, 0, 0}, t = {0, 0, 0};
         R e = 0;
-        particle_forces<R, E>(a, F, i, cur, lp, w, pi, ni, sd, a.ss[s], sh, f, t, e, flags);
+        particle_forces<R, E, V>(a, F, i, cur, lp, w, pi, ni, sd, a.ss[s], sh, f, t, e, flags);
         const R dt = R(a.dt);
         const R zeta = R(__ldcg(&a.ss[s].zeta));
         const R im = F.inv_mass[ty];
@@ -533,11 +607,11 @@ template<class R, bool E> __global__ void __launch_bounds__(256) k_nh_final(KArg
     finish<R>(a, ke, ep, 0.f, flags, MODE_NH_FINAL, count_step);
 }
 
-template<class R> __global__ void __launch_bounds__(256) k_nh_initial(KArgs<R> a) {
+template<class R> __global__ void __launch_bounds__(STEP_BS) k_nh_initial(KArgs<R> a) {
     using T4 = typename Vec<R>::T4;
     const int cur = __ldcg(&a.S->cur), lp = __ldcg(&a.S->lp);
-    const int i = blockIdx.x * 256 + threadIdx.x;
-    const int s = a.blk_sys[blockIdx.x];
+    const int i = blockIdx.x * STEP_BS + threadIdx.x;
+    const int s = a.blk_sys[(blockIdx.x * STEP_BS) / SYS_PAD];
     const SysDev &sd = a.sys[s];
     T4 p = a.pos[cur][i];
     const int w = wbits(p.w);
@@ -600,17 +674,18 @@ template<class R> __global__ void __launch_bounds__(256) k_nh_initial(KArgs<R> a
     finish<R>(a, ke, 0.0, md2, flags, MODE_NH_INITIAL, 0);
 }
 
-template<class R, bool E> __global__ void __launch_bounds__(256) k_forces(KArgs<R> a) {
+template<class R, bool E, int V> __global__ void __launch_bounds__(STEP_BS, (V & 2) ? 6 : 8) k_forces(KArgs<R> a) {
     using T4 = typename Vec<R>::T4;
     __shared__ T4 sh[27];
     __shared__ FFDev<R> F;
     stage_ff<R>(&F, a.ff);
     init_shift<R>(sh);
     const int cur = __ldcg(&a.S->cur), lp = __ldcg(&a.S->lp);
-    const int i = blockIdx.x * 256 + threadIdx.x;
-    const int s = a.blk_sys[blockIdx.x];
+    const int i = blockIdx.x * STEP_BS + threadIdx.x;
+    const int s = a.blk_sys[(blockIdx.x * STEP_BS) / SYS_PAD];
     const SysDev &sd = a.sys[s];
     const T4 pi = a.pos[cur][i];
+    prefetch_warp_list(a.nbr, i, a.cap, a.nnb[i]);
     const int w = wbits(pi.w);
     double ep = 0;
     int flags = 0;
@@ -618,7 +693,7 @@ template<class R, bool E> __global__ void __launch_bounds__(256) k_forces(KArgs<
         const T4 ni = a.nrm[cur][i];
         R3<R> f = {0, 0, 0}, t = {0, 0, 0};
         R e = 0;
-        particle_forces<R, E>(a, F, i, cur, lp, w, pi, ni, sd, a.ss[s], sh, f, t, e, flags);
+        particle_forces<R, E, V>(a, F, i, cur, lp, w, pi, ni, sd, a.ss[s], sh, f, t, e, flags);
         T4 q = pi;
         q.x = f.x;
         q.y = f.y;
@@ -635,19 +710,25 @@ template<class R, bool E> __global__ void __launch_bounds__(256) k_forces(KArgs<
 }
 
 /* FP64 membrane area and enclosed volume of each system's face mesh, and
- * the constraint coefficients for the next force evaluation. */
+ * the constraint coefficients for the next force evaluation.  Each block sums
+ * MESH_CHUNK faces of one system; the last block adds the block sums of each
+ * system in block order (deterministic). */
 template<class R> __global__ void __launch_bounds__(256) k_mesh(KArgs<R> a) {
     using T4 = typename Vec<R>::T4;
-    const int s = blockIdx.x;
+    const int b = blockIdx.x;
+    const int s = a.mesh_blk_sys[b];
     const SysDev &sd = a.sys[s];
     __shared__ double sa[8], sv[8];
+    __shared__ bool last;
     const int cur = __ldcg(&a.S->cur), lp = __ldcg(&a.S->lp);
     double ar = 0, vol = 0;
-    if (sd.face_end > sd.face_begin) {
+    const int f0 = sd.face_begin + (b - sd.mblk_begin) * MESH_CHUNK;
+    const int f1 = min(sd.face_end, f0 + MESH_CHUNK);
+    if (f1 > f0) {
         const int ref = a.faces[sd.face_begin].x;
         const T4 pr = a.pos[cur][ref];
         const int cr = a.cell[lp][ref];
-        for (int f = sd.face_begin + threadIdx.x; f < sd.face_end; f += blockDim.x) {
+        for (int f = f0 + int(threadIdx.x); f < f1; f += blockDim.x) {
             const int4 q = a.faces[f];
             double P[3][3];
             const int idx[3] = {q.x, q.y, q.z};
@@ -681,39 +762,83 @@ template<class R> __global__ void __launch_bounds__(256) k_mesh(KArgs<R> a) {
             A += sa[w];
             V += sv[w];
         }
-        SysState &ss = a.ss[s];
-        ss.area = A;
-        ss.volume = V;
-        ss.cv = (sd.kv != 0 && sd.V0 != 0) ? -sd.kv * (V - sd.V0) / sd.V0 : 0.0;
-        ss.ca = (sd.ka != 0 && sd.A0 != 0) ? -sd.ka * (A - sd.A0) / sd.A0 : 0.0;
+        a.mesh_partial[2 * b] = A;
+        a.mesh_partial[2 * b + 1] = V;
+        __threadfence();
+        last = atomicAdd(&a.S->mesh_counter, 1u) == gridDim.x - 1;
     }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    const int lane = threadIdx.x & 31;
+    for (int q = threadIdx.x >> 5; q < a.nsys; q += 8) {
+        const SysDev &sq = a.sys[q];
+        double A = 0, V = 0;
+        for (int k = sq.mblk_begin + lane; k < sq.mblk_end; k += 32) {
+            A += __ldcg(a.mesh_partial + 2 * k);
+            V += __ldcg(a.mesh_partial + 2 * k + 1);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            A += __shfl_xor_sync(0xffffffffu, A, o);
+            V += __shfl_xor_sync(0xffffffffu, V, o);
+        }
+        if (lane == 0) {
+            SysState &ss = a.ss[q];
+            ss.area = A;
+            ss.volume = V;
+            ss.cv = (sq.kv != 0 && sq.V0 != 0) ? -sq.kv * (V - sq.V0) / sq.V0 : 0.0;
+            ss.ca = (sq.ka != 0 && sq.A0 != 0) ? -sq.ka * (A - sq.A0) / sq.A0 : 0.0;
+        }
+    }
+    if (threadIdx.x == 0) a.S->mesh_counter = 0;
 }
 
 }  // namespace
 
-template<class R> void launch_step_langevin(const KArgs<R> &a, cudaStream_t st, bool energy) {
+/* Force-kernel forms (bit 0: software-pipelined list pass -- the next entry's
+ * gathers are issued before the current pair is evaluated -- instead of a
+ * 2-way unrolled loop; bit 1: the rare non-lipid pair path inlined, with up
+ * to 85 registers, instead of called).  The autotuner picks one per workload. */
+template<class R, int V> void step_langevin_v(const KArgs<R> &a, cudaStream_t st, bool energy) {
     if (energy)
-        k_step_langevin<R, true><<<a.nblk, 256, 0, st>>>(a);
+        k_step_langevin<R, true, V><<<a.nblk, STEP_BS, 0, st>>>(a);
     else
-        k_step_langevin<R, false><<<a.nblk, 256, 0, st>>>(a);
+        k_step_langevin<R, false, V><<<a.nblk, STEP_BS, 0, st>>>(a);
+}
+template<class R, int V> void nh_final_v(const KArgs<R> &a, cudaStream_t st, bool energy) {
+    if (energy)
+        k_nh_final<R, true, V><<<a.nblk, STEP_BS, 0, st>>>(a, 1);
+    else
+        k_nh_final<R, false, V><<<a.nblk, STEP_BS, 0, st>>>(a, 1);
+}
+template<class R> void launch_step_langevin(const KArgs<R> &a, cudaStream_t st, bool energy) {
+    switch (a.variant) {
+        case 1: step_langevin_v<R, 1>(a, st, energy); break;
+        case 2: step_langevin_v<R, 2>(a, st, energy); break;
+        case 3: step_langevin_v<R, 3>(a, st, energy); break;
+        default: step_langevin_v<R, 0>(a, st, energy); break;
+    }
 }
 template<class R> void launch_nh_final(const KArgs<R> &a, cudaStream_t st, bool energy) {
-    if (energy)
-        k_nh_final<R, true><<<a.nblk, 256, 0, st>>>(a, 1);
-    else
-        k_nh_final<R, false><<<a.nblk, 256, 0, st>>>(a, 1);
+    switch (a.variant) {
+        case 1: nh_final_v<R, 1>(a, st, energy); break;
+        case 2: nh_final_v<R, 2>(a, st, energy); break;
+        case 3: nh_final_v<R, 3>(a, st, energy); break;
+        default: nh_final_v<R, 0>(a, st, energy); break;
+    }
 }
 template<class R> void launch_nh_prologue(const KArgs<R> &a, cudaStream_t st) {
-    k_nh_final<R, true><<<a.nblk, 256, 0, st>>>(a, 0);
+    k_nh_final<R, true, 0><<<a.nblk, STEP_BS, 0, st>>>(a, 0);
 }
 template<class R> void launch_nh_initial(const KArgs<R> &a, cudaStream_t st) {
-    k_nh_initial<R><<<a.nblk, 256, 0, st>>>(a);
+    k_nh_initial<R><<<a.nblk, STEP_BS, 0, st>>>(a);
 }
 template<class R> void launch_forces(const KArgs<R> &a, cudaStream_t st) {
-    k_forces<R, true><<<a.nblk, 256, 0, st>>>(a);
+    k_forces<R, true, 0><<<a.nblk, STEP_BS, 0, st>>>(a);
 }
 template<class R> void launch_mesh(const KArgs<R> &a, cudaStream_t st) {
-    k_mesh<R><<<a.nsys, 256, 0, st>>>(a);
+    if (a.nmblk > 0) k_mesh<R><<<a.nmblk, 256, 0, st>>>(a);
 }
 
 #define ORBC_INST(R)                                                                   \

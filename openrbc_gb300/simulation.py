@@ -35,7 +35,7 @@ class Simulation:
                  energy: bool = False, box: Optional[Sequence[Sequence[float]]] = None,
                  periodic: Sequence[int] = (0, 0, 0), bond_table: Optional[dict] = None,
                  max_neighbors: int = 0, rebuild_every: Optional[int] = None, bounce: bool = True,
-                 mesh_constraint: Optional[dict] = None):
+                 mesh_constraint: Optional[dict] = None, kernel_variant: int = 0):
         self.param = param or RTParameter(init="lipid")
         p = N.Params()
         L = N.lib()
@@ -51,6 +51,7 @@ class Simulation:
         p.bounce = 1 if bounce else 0
         p.use_graph = 1 if use_graph else 0
         p.energy = 1 if energy else 0
+        p.kernel_variant = int(kernel_variant)
         bx = box if box is not None else prm.box
         for d in range(3):
             p.lo[d], p.hi[d] = float(bx[d][0]), float(bx[d][1])
@@ -179,6 +180,15 @@ class Simulation:
         pr = N.Profile()
         self._check(N.lib().orbc_gpu_profile(self.h, int(nsteps), C.byref(pr)))
         return pr.as_dict()
+
+    def autotune(self, trial_steps: int = 30):
+        """Pick skin and force-kernel form by timing trials (orbc_gpu_autotune);
+        the state is restored afterwards.  Returns the trial table."""
+        rows = (N.TuneTrial * 64)()
+        nt = C.c_int()
+        self._check(N.lib().orbc_gpu_autotune(self.h, int(trial_steps), rows, 64, C.byref(nt)))
+        return [{"skin": r.skin, "variant": r.variant, "ms_per_step": r.ms_per_step,
+                 "rebuilds_per_step": r.rebuilds_per_step} for r in rows[:nt.value]]
 
     def last_timing(self):
         ms = C.c_double()

@@ -256,3 +256,42 @@ def test_nose_hoover_mixed_tracks_fp64():
             res[prec] = s.step(50)
     assert abs(res["mixed"]["zeta"] - res["fp64"]["zeta"]) < 1e-3 * max(1e-3, abs(res["fp64"]["zeta"]))
     assert abs(res["mixed"]["temperature"] - res["fp64"]["temperature"]) < 1e-3 * res["fp64"]["temperature"]
+
+
+@pytest.mark.parametrize("variant", [1, 2, 3])
+def test_force_kernel_forms_agree(variant):
+    """The four force-kernel forms evaluate the same pairs in the same order."""
+    from openrbc_gb300 import RTParameter
+    from openrbc_gb300 import Simulation
+    w, table = small_rbc("wlc")
+    out = {}
+    for v in (0, variant):
+        p = RTParameter(init="lipid", kBT=1.0, precision="mixed", rseed=5)
+        with Simulation(p, bond_table=table, kernel_variant=v) as s:
+            upload_rbc(s, w)
+            f, t, _ = s.forces()
+            s.step(20)
+            out[v] = (f, s.download()[0])
+    assert rel_l2(out[variant][0], out[0][0]) < 1e-6
+    assert rel_l2(out[variant][1] - w["x"], out[0][1] - w["x"]) < 1e-4
+
+
+def test_autotune_restores_state_and_keeps_stepping():
+    from openrbc_gb300 import RTParameter, Simulation
+    w, box = lattice_sys(n=8192, ncol=90)
+    p = RTParameter(init="lipid", kBT=1.0, precision="mixed", rseed=8)
+    with Simulation(p, box=box, periodic=(1, 1, 0)) as s:
+        s.upload(w["x"], w["n"], w["v"], w["o"], w["type"], w["tag"])
+        s.step(5)
+        before = s.download()
+        step0 = s.thermo()["step"]
+        trials = s.autotune(trial_steps=4)
+        after = s.download()
+        assert len(trials) == 20 and all(t["ms_per_step"] > 0 for t in trials)
+        assert s.thermo()["step"] == step0
+        d = min_image_diff(after[0], before[0], box, (1, 1, 0))
+        assert np.abs(d).max() < 1e-5
+        for u, v in zip(after[1:], before[1:]):
+            assert np.abs(u - v).max() < 1e-6
+        th = s.step(10)
+        assert th["step"] == step0 + 10 and np.isfinite(th["temperature"])
