@@ -87,7 +87,11 @@ typedef struct {
        (else 2-way unrolled), bit 1 = non-lipid pair path inlined (else
        called); orbc_gpu_autotune picks it per workload */
     int kernel_variant;
-    int pad_params;
+    /* 1: remove each system's mean lipid velocity between the force
+       evaluation and the integrator every step, as the disabled call
+       integrate(zero_bulk_velocity(param), lipid) at src/openrbc.cpp:228 would
+       (src/zero_bulk_velocity.h:29-56); 0 (default): off, as in the reference */
+    int zero_bulk;
 } orbc_params;
 
 /* One independent system of a batched upload (its own box and constraint). */
@@ -172,6 +176,32 @@ int orbc_gpu_cells(orbc_handle *h, int sys, double *lo3, double *lc3, int *nc3, 
 
 /* Force a neighbour-list rebuild now (sort + bins + list). */
 int orbc_gpu_rebuild(orbc_handle *h);
+
+/* assign_temperature (src/assign_temperature.h:26-44, applied to lipids and
+ * proteins at src/openrbc.cpp:160): every particle's velocity becomes
+ * sqrt(2 kBT / m) g with g three unit Gaussians (the reference's factor 2 is
+ * kept; pass kBT * amplify for its amplify argument).  The Gaussians come from
+ * Box-Muller on one Philox4x32-10 block keyed by seed with counter (tag,
+ * 0x6B8B4567, 0x327B23C6, system index), so they do not depend on the thread
+ * count or the slot order (the reference draws from per-thread generators).
+ * Orientations and angular velocities are untouched. */
+int orbc_gpu_assign_temperature(orbc_handle *h, double kBT, uint64_t seed);
+
+/* rdf / rdf_1peak_r (src/rdf.h:26-81): histogram of the distances of all
+ * unordered pairs of system sys whose types match (type_a, type_b) in either
+ * order (-1 = any type): counts[(int)(r / dr)] += 1 for r < rcut (rcut <= 0:
+ * no cutoff) and bin < nbins; other pairs are counted in *dropped (the
+ * reference writes past its 10,000 bins instead).  The reference's `rdf` is
+ * type_a = type_b = -1 over one container, dr = 0.1, nbins = 10000;
+ * `rdf_1peak_r` is type 4 with itself, dr = 0.5, rcut = 25, 51 bins.
+ * Distances are evaluated in the handle's precision (FP32 for
+ * ORBC_PREC_MIXED, as the reference's default `real`; FP64 otherwise) from
+ * coordinates relative to the centre of the system's box, with the minimum
+ * image on periodic axes (the reference has none).  All pairs are visited
+ * (O(N^2), as in the reference).  The caller normalises: the reference writes
+ * r = dr i and counts[i] / (4 * 3.14 * r^2 * dr) to rdf.txt. */
+int orbc_gpu_rdf(orbc_handle *h, int sys, int type_a, int type_b, double dr, int nbins, double rcut,
+                 uint64_t *counts, int64_t *dropped);
 
 /* Milliseconds of device time of the last orbc_gpu_step call, and the number
  * of kernel launches it issued (graph nodes included). */

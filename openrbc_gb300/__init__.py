@@ -5,7 +5,8 @@ this package is its host-side mirror of the reference's interface
 (RTParameter, the containers, the step loop) and its build script.
 """
 from .runtime_parameter import ParameterError, RTParameter
-from .simulation import Simulation, morton_encode, morton_order
+from .simulation import Simulation, morton_encode, morton_order, rdf_table, write_rdf
 from ._native import OrbcError
 
-__all__ = ["RTParameter", "ParameterError", "Simulation", "OrbcError", "morton_encode", "morton_order"]
+__all__ = ["RTParameter", "ParameterError", "Simulation", "OrbcError", "morton_encode", "morton_order", "rdf_table",
+           "write_rdf"]

@@ -28,6 +28,7 @@ EXPORTS = [
     "orbc_gpu_neighbors", "orbc_gpu_cells", "orbc_gpu_rebuild", "orbc_gpu_last_timing",
     "orbc_gpu_morton_encode", "orbc_gpu_morton_order", "orbc_gpu_destroy", "orbc_gpu_error",
     "orbc_gpu_version", "orbc_gpu_profile", "orbc_gpu_morton_order_noalloc", "orbc_gpu_autotune",
+    "orbc_gpu_assign_temperature", "orbc_gpu_rdf",
     "orbc_gen_lattice", "orbc_gen_rbc_counts", "orbc_gen_rbc", "orbc_gen_vesicle_sizes", "orbc_gen_vesicle",
 ]
 
@@ -49,7 +50,7 @@ class Params(C.Structure):
         ("kv", C.c_double), ("V0", C.c_double), ("ka", C.c_double), ("A0", C.c_double),
         ("bond_style", C.c_int * MAX_BOND_TYPES), ("bond_K", C.c_double * MAX_BOND_TYPES),
         ("bond_r0", C.c_double * MAX_BOND_TYPES), ("bond_R", C.c_double * MAX_BOND_TYPES),
-        ("kernel_variant", C.c_int), ("pad_params", C.c_int),
+        ("kernel_variant", C.c_int), ("zero_bulk", C.c_int),
     ]
 
 
@@ -116,6 +117,8 @@ def lib():
         L.orbc_gpu_neighbors.argtypes = [H, vp, vp, i64, P(i64)]
         L.orbc_gpu_cells.argtypes = [H, i32, vp, vp, vp, vp, vp, vp]
         L.orbc_gpu_rebuild.argtypes = [H]
+        L.orbc_gpu_assign_temperature.argtypes = [H, d, C.c_uint64]
+        L.orbc_gpu_rdf.argtypes = [H, i32, i32, i32, d, i32, d, vp, P(i64)]
         L.orbc_gpu_last_timing.argtypes = [H, P(d), P(i64)]
         L.orbc_gpu_morton_encode.argtypes = [vp, i64, vp, vp]
         L.orbc_gpu_morton_order.argtypes = [vp, i64, vp, vp]

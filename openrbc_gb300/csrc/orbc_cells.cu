@@ -28,15 +28,6 @@ __device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(
 __device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
 
-__device__ __forceinline__ unsigned cell_lin(const SysDev &s, int x, int y, int z) {
-    return unsigned(x) + unsigned(s.nc[0]) * (unsigned(y) + unsigned(s.nc[1]) * unsigned(z));
-}
-__device__ __forceinline__ unsigned ncell_of(const SysDev &s) {
-    return unsigned(s.nc[0]) * unsigned(s.nc[1]) * unsigned(s.nc[2]);
-}
-
-template<class T4> __device__ __forceinline__ T4 ld4(const T4 *p) { return *p; }
-template<> __device__ __forceinline__ float4 ld4<float4>(const float4 *p) { return __ldg(p); }
 
 __device__ __forceinline__ int gate_closed(const int *gate) { return gate && !__ldcg(gate); }
 
@@ -197,11 +188,11 @@ template<class R> __global__ void __launch_bounds__(256) k_rebin(KArgs<R> a, int
         const int w = wbits(p.w);
         uint32_t key;
         if (w_type(w) == GHOST) {
-            key = sd.cell_base + ncell_of(sd);
+            key = sd.cell_base + ncell_ids(sd);
         } else {
             const int c = a.cell[lp][i];
             int cc[3] = {cx_of(c), cy_of(c), cz_of(c)};
-            a.ranges[sd.cell_base + cell_lin(sd, cc[0], cc[1], cc[2])] = make_int2(0, 0);
+            a.ranges[sd.cell_base + cell_code(sd, cc[0], cc[1], cc[2])] = make_int2(0, 0);
             R o[3] = {p.x, p.y, p.z};
 #pragma unroll
             for (int d = 0; d < 3; ++d) {
@@ -226,7 +217,7 @@ template<class R> __global__ void __launch_bounds__(256) k_rebin(KArgs<R> a, int
             p.z = o[2];
             a.pos[cur][i] = p;  // the gather that follows sets the displacement reference
             a.cell[lp][i] = cpack(cc[0], cc[1], cc[2]);
-            key = sd.cell_base + cell_lin(sd, cc[0], cc[1], cc[2]);
+            key = sd.cell_base + cell_code(sd, cc[0], cc[1], cc[2]);
         }
         a.skey[0][i] = key;
         a.sval[0][i] = i;
@@ -287,18 +278,29 @@ template<class R> __global__ void __launch_bounds__(256) k_ranges_gather(KArgs<R
     }
 }
 
-template<class R> __global__ void __launch_bounds__(256) k_nlist(KArgs<R> a, int gated) {
+template<class R> __global__ void __launch_bounds__(128) k_nlist(KArgs<R> a, int gated) {
     using T4 = typename Vec<R>::T4;
     if (gated && !__ldcg(&a.S->rebuild)) return;
-    __shared__ float rl2s[256];
-    rl2s[threadIdx.x] = __ldg(&a.ff->rlist2[threadIdx.x]);
-    if (blockDim.x < 256 && threadIdx.x + blockDim.x < 256)
-        rl2s[threadIdx.x + blockDim.x] = __ldg(&a.ff->rlist2[threadIdx.x + blockDim.x]);
+    constexpr int CAND = sizeof(T4) == 16 ? 256 : 160;  // staged candidates per warp
+    constexpr int NLW = 4;                                // warps per block
+    constexpr int NLBOX = 128;                            // largest box (cells) swept warp-wide
+    __shared__ float rl2s[256], ri2s[256];
+    __shared__ T4 s_pos[NLW][CAND];
+    __shared__ int2 s_jk[NLW][CAND];
+    __shared__ int s_off[NLW][NLBOX + 1], s_beg[NLW][NLBOX];
+    __shared__ unsigned char s_need[NLW][NLBOX];
+    constexpr bool STG = sizeof(T4) == 16;  // warp staging in the mixed-precision step kernels
+    const int warp = threadIdx.x >> 5;
+    for (int k = threadIdx.x; k < 256; k += blockDim.x) {
+        rl2s[k] = __ldg(&a.ff->rlist2[k]);
+        ri2s[k] = __ldg(&a.ff->rin2[k]);
+    }
     __syncthreads();
     const int cur = 1 - __ldcg(&a.S->cur), lp = 1 - __ldcg(&a.S->lp);
     const int n = a.npad;
     int maxc = 0;
     // n is a multiple of the block size, so whole warps stay in the loop together
+    const int lane = threadIdx.x & 31;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const T4 p = a.pos[cur][i];
         const int ty = w_type(wbits(p.w));
@@ -307,9 +309,10 @@ template<class R> __global__ void __launch_bounds__(256) k_nlist(KArgs<R> a, int
         const int c = a.cell[lp][i];
         const int cc[3] = {cx_of(c), cy_of(c), cz_of(c)};
         const R L[3] = {R(sd.Lc[0]), R(sd.Lc[1]), R(sd.Lc[2])};
-        int count = 0;
-        auto test = [&](int j, int dx, int dy, int dz) {
-            const T4 q = a.pos[cur][j];
+        // Entries inside the pair's interaction range fill rows 0, 1, ... of
+        // this slot's column; skin-shell entries fill rows cap-1, cap-2, ...
+        int nin = 0, nout = 0, total = 0;
+        auto test = [&](int j, const T4 &q, int dx, int dy, int dz) {
             const int tj = w_type(wbits(q.w));
             const float rl2 = rl2s[ty * 16 + tj];
             if (!(rl2 > 0.f)) return;
@@ -319,15 +322,31 @@ template<class R> __global__ void __launch_bounds__(256) k_nlist(KArgs<R> a, int
             const R ez = add_rn(sub_rn(p.z, q.z), mul_rn(R(-dz), L[2]));
             const R r2 = add_rn(add_rn(mul_rn(ex, ex), mul_rn(ey, ey)), mul_rn(ez, ez));
             if (r2 < R(rl2)) {
-                const uint32_t code = uint32_t((dx + 1) + 3 * (dy + 1) + 9 * (dz + 1));
-                if (count < a.cap) a.nbr[nbr_index(i, count, a.cap)] = uint32_t(j) | (code << NB_SHIFT);
-                ++count;
+                const uint32_t ent = uint32_t(j) | (uint32_t((dx + 1) + 3 * (dy + 1) + 9 * (dz + 1)) << NB_SHIFT);
+                if (nin + nout < a.cap) {
+                    if (r2 < R(ri2s[ty * 16 + tj]))
+                        a.nbr[nbr_index(i, nin++, a.cap)] = ent;
+                    else
+                        a.nbr[nbr_index(i, a.cap - 1 - nout++, a.cap)] = ent;
+                }
+                ++total;
             }
         };
         // Bounding box of the warp's cells.  Consecutive slots sit in a few
-        // neighbouring cells, so one sweep of the box (grown by one cell) with
-        // every lane testing every candidate replaces 32 diverging 27-cell
-        // sweeps; a wide box (row or periodic seam) falls back to them.
+        // neighbouring cells (cell ids follow tiles), so one sweep of the cells
+        // of the box (grown by one cell) that some lane's 27-cell neighbourhood
+        // covers, with every lane testing every candidate, replaces 32
+        // diverging 27-cell sweeps.  The ranges of those cells are fetched one
+        // per lane and scanned into candidate offsets; the candidates are then
+        // staged in shared memory (CAND at a time, all loads in flight
+        // together) and every lane reads them as broadcasts.  A wide box falls
+        // back to per-lane sweeps.  When the candidates form at most STG_RMAX
+        // contiguous slot ranges and number at most STG_CAND, the warp's
+        // entries hold the candidate's local index and the ranges go to
+        // wmeta, so the step kernels can copy the candidates to shared memory
+        // and read them there.
+        bool staged = false;
+        int nranges = 0, total_c = 0;
         const bool any_real = __any_sync(0xffffffffu, real);
         int lo[3], hi[3], vol = any_real ? 1 : 0;
 #pragma unroll
@@ -337,35 +356,94 @@ template<class R> __global__ void __launch_bounds__(256) k_nlist(KArgs<R> a, int
             hi[d] = __reduce_max_sync(0xffffffffu, real ? cc[d] : -4096) + 1;
             vol *= max(hi[d] - lo[d] + 1, 0);
         }
-        if (vol > 0 && vol <= 64) {
-            for (int bz = lo[2]; bz <= hi[2]; ++bz) {
-                int z = bz;
-                if (sd.per[2]) {
-                    z = z < 0 ? z + sd.nc[2] : (z >= sd.nc[2] ? z - sd.nc[2] : z);
-                } else if (z < 0 || z >= sd.nc[2]) {
-                    continue;
+        if (vol > 0 && vol <= NLBOX) {
+            const int bx_n = hi[0] - lo[0] + 1, by_n = hi[1] - lo[1] + 1;
+            int *off = s_off[warp];
+            int *beg = s_beg[warp];
+            unsigned char *need = s_need[warp];
+            // this lane's cell relative to the box corner (inside [1, n-2] per axis)
+            const int rx0 = cc[0] - lo[0], ry0 = cc[1] - lo[1], rz0 = cc[2] - lo[2];
+            for (int k = lane; k < vol; k += 32) need[k] = 0;
+            __syncwarp();
+            if (real)
+                for (int dz = -1; dz <= 1; ++dz)
+                    for (int dy = -1; dy <= 1; ++dy)
+                        for (int dx = -1; dx <= 1; ++dx)
+                            need[(rx0 + dx) + bx_n * ((ry0 + dy) + by_n * (rz0 + dz))] = 1;
+            __syncwarp();
+            int2 *meta = a.wmeta + int64_t(i >> 5) * 32;
+            int running = 0, carry_end = -1;
+            for (int base = 0; base < vol; base += 32) {
+                int2 rg = make_int2(0, 0);
+                const int cidx = base + lane;
+                if (cidx < vol && need[cidx]) {
+                    int x = lo[0] + cidx % bx_n, y = lo[1] + (cidx / bx_n) % by_n, z = lo[2] + cidx / (bx_n * by_n);
+                    bool ok = true;
+                    if (sd.per[0]) x = x < 0 ? x + sd.nc[0] : (x >= sd.nc[0] ? x - sd.nc[0] : x);
+                    else ok = ok && x >= 0 && x < sd.nc[0];
+                    if (sd.per[1]) y = y < 0 ? y + sd.nc[1] : (y >= sd.nc[1] ? y - sd.nc[1] : y);
+                    else ok = ok && y >= 0 && y < sd.nc[1];
+                    if (sd.per[2]) z = z < 0 ? z + sd.nc[2] : (z >= sd.nc[2] ? z - sd.nc[2] : z);
+                    else ok = ok && z >= 0 && z < sd.nc[2];
+                    if (ok) rg = a.ranges[sd.cell_base + cell_code(sd, x, y, z)];
                 }
-                for (int by = lo[1]; by <= hi[1]; ++by) {
-                    int y = by;
-                    if (sd.per[1]) {
-                        y = y < 0 ? y + sd.nc[1] : (y >= sd.nc[1] ? y - sd.nc[1] : y);
-                    } else if (y < 0 || y >= sd.nc[1]) {
-                        continue;
+                const int cnt = rg.y > rg.x ? rg.y - rg.x : 0;
+                int inc = cnt;  // inclusive warp scan
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int t = __shfl_up_sync(0xffffffffu, inc, o);
+                    if (lane >= o) inc += t;
+                }
+                const int my_off = running + inc - cnt;
+                if (cidx < vol) {
+                    off[cidx] = my_off;
+                    beg[cidx] = rg.x;
+                }
+                if (STG) {
+                    // a non-empty cell opens a new slot range unless the previous
+                    // non-empty cell (box order) ends where it begins
+                    const unsigned nem = __ballot_sync(0xffffffffu, cnt > 0);
+                    const unsigned below = nem & ((1u << lane) - 1u);
+                    const int pe = __shfl_sync(0xffffffffu, rg.y, below ? 31 - __clz(below) : 0);
+                    const bool newr = cnt > 0 && rg.x != (below ? pe : carry_end);
+                    const unsigned nm = __ballot_sync(0xffffffffu, newr);
+                    const int rid = nranges + __popc(nm & ((1u << lane) - 1u));
+                    if (newr && rid < STG_RMAX) meta[1 + rid] = make_int2(rg.x, my_off);
+                    nranges += __popc(nm);
+                    if (nem) carry_end = __shfl_sync(0xffffffffu, rg.y, 31 - __clz(nem));
+                }
+                running += __shfl_sync(0xffffffffu, inc, 31);
+            }
+            if (lane == 0) off[vol] = running;
+            __syncwarp();
+            total_c = running;
+            staged = STG && nranges <= STG_RMAX && total_c <= STG_CAND;
+            for (int c0 = 0; c0 < total_c; c0 += CAND) {
+                const int nch = min(CAND, total_c - c0);
+                for (int t = lane; t < nch; t += 32) {
+                    const int idx = c0 + t;
+                    int l = 0, h = vol;  // off[l] <= idx < off[h]
+                    while (h - l > 1) {
+                        const int mid = (l + h) >> 1;
+                        if (off[mid] <= idx) l = mid;
+                        else h = mid;
                     }
-                    for (int bx = lo[0]; bx <= hi[0]; ++bx) {
-                        int x = bx;
-                        if (sd.per[0]) {
-                            x = x < 0 ? x + sd.nc[0] : (x >= sd.nc[0] ? x - sd.nc[0] : x);
-                        } else if (x < 0 || x >= sd.nc[0]) {
+                    const int j = beg[l] + (idx - off[l]);
+                    s_pos[warp][t] = a.pos[cur][j];
+                    const int kx = l % bx_n, ky = (l / bx_n) % by_n, kz = l / (bx_n * by_n);
+                    s_jk[warp][t] = make_int2(j, kx | (ky << 8) | (kz << 16));
+                }
+                __syncwarp();
+                if (real) {
+                    for (int t = 0; t < nch; ++t) {
+                        const int2 jk = s_jk[warp][t];
+                        const int dx = (jk.y & 255) - rx0, dy = ((jk.y >> 8) & 255) - ry0, dz = (jk.y >> 16) - rz0;
+                        if (unsigned(dx + 1) > 2u || unsigned(dy + 1) > 2u || unsigned(dz + 1) > 2u || jk.x == i)
                             continue;
-                        }
-                        const int dx = bx - cc[0], dy = by - cc[1], dz = bz - cc[2];
-                        const bool mine = real && dx >= -1 && dx <= 1 && dy >= -1 && dy <= 1 && dz >= -1 && dz <= 1;
-                        const int2 rg = a.ranges[sd.cell_base + cell_lin(sd, x, y, z)];
-                        for (int j = rg.x; j < rg.y; ++j)
-                            if (mine && j != i) test(j, dx, dy, dz);
+                        test(staged ? c0 + t : jk.x, s_pos[warp][t], dx, dy, dz);
                     }
                 }
+                __syncwarp();
             }
         } else if (real) {
             for (int dz = -1; dz <= 1; ++dz) {
@@ -389,15 +467,16 @@ template<class R> __global__ void __launch_bounds__(256) k_nlist(KArgs<R> a, int
                         } else if (x < 0 || x >= sd.nc[0]) {
                             continue;
                         }
-                        const int2 rg = a.ranges[sd.cell_base + cell_lin(sd, x, y, z)];
+                        const int2 rg = a.ranges[sd.cell_base + cell_code(sd, x, y, z)];
                         for (int j = rg.x; j < rg.y; ++j)
-                            if (j != i) test(j, dx, dy, dz);
+                            if (j != i) test(j, a.pos[cur][j], dx, dy, dz);
                     }
                 }
             }
         }
-        a.nnb[i] = real ? min(count, a.cap) : 0;
-        maxc = max(maxc, count);
+        a.nnb[i] = real ? (nin | (nout << 16)) : 0;
+        if (lane == 0) a.wmeta[int64_t(i >> 5) * 32] = staged ? make_int2(nranges, total_c) : make_int2(0, 0);
+        maxc = max(maxc, total);
     }
     // block max -> global max; last block finalises the rebuild
     __shared__ int smax[8];
@@ -472,7 +551,7 @@ __global__ void k_set_state(KArgs<R> a, const double *x, const double *nv, const
         T4 q = a.pos[cur][p];
         {
             const int c0 = a.cell[lp][p];  // the next rebin clears only the new cells
-            a.ranges[sd.cell_base + cell_lin(sd, cx_of(c0), cy_of(c0), cz_of(c0))] = make_int2(0, 0);
+            a.ranges[sd.cell_base + cell_code(sd, cx_of(c0), cy_of(c0), cz_of(c0))] = make_int2(0, 0);
         }
         int cc[3];
         R off[3];

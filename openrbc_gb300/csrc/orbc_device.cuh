@@ -27,8 +27,14 @@ constexpr int MAX_DEG = 15;      // bonds / faces per particle (4-bit fields)
 constexpr uint32_t NB_MASK = (1u << 27) - 1u;
 constexpr int NB_SHIFT = 27;
 constexpr int MAX_SLOTS = 1 << 27;
-constexpr int NPART = 4;         // per-block partial sums: ke2, epot, maxd2, flags
+constexpr int NPART = 8;         // per-block partial sums: ke2, epot, maxd2, flags, lipid sum v (3), pad
 constexpr int MESH_CHUNK = 1024; // faces per block of the area / volume kernel
+// Warp staging (mixed precision): the union of the 27-cell neighbourhoods of
+// a warp's 32 slots is at most STG_RMAX contiguous slot ranges holding at most
+// STG_CAND particles; the step kernels copy their positions and orientations
+// to shared memory once and the warp's list entries index that copy.
+constexpr int STG_CAND = 304;
+constexpr int STG_RMAX = 31;
 
 enum : int {
     ERRB_NBR_OVERFLOW = 1,  // a neighbour list overflowed its capacity
@@ -98,18 +104,37 @@ template<class R> struct FFDev {
     R mass[NT], inv_mass[NT], gamma[NT], sigma[NT];
     BondP<R> bond[MAX_BT];
     float rlist2[16 * 16];          // neighbour-list cutoff^2 (cut + skin)^2, 0 = never
+    float rin2[16 * 16];            // interaction range^2: list entries inside it go to the inner rows
 };
 
 struct SysDev {
     double lo[3], Lc[3];            // grid origin and cell size
     double wlo[3], whi[3];          // reflective walls (Nose-Hoover bounce-back)
     int nc[3], per[3];
+    int ntile[3], pad0;             // 4 x 4 x 4 tiles of cells per axis (cell-id order)
     unsigned cell_base;             // first global cell id; ncell + 1 ids (last = ghost cell)
     int off, npad, nreal;
     int face_begin, face_end;
     int mblk_begin, mblk_end;       // blocks of the area / volume kernel (MESH_CHUNK faces each)
+    int nlipid, pad1;               // lipids in the system (bulk-velocity removal)
     double kv, V0, ka, A0, Q;
 };
+
+/* Cell id inside a system: 4 x 4 x 4 tiles of cells in row-major tile
+ * order, Morton (x, y, z interleaved) inside a tile.  Particles are sorted by
+ * cell id, so 32 consecutive slots sit in a compact clump of cells (a warp's
+ * neighbourhood), unlike row-major order where a warp strings along a row. */
+__host__ __device__ __forceinline__ unsigned tile_spread2(unsigned v) { return (v & 1u) | ((v & 2u) << 2); }
+__host__ __device__ __forceinline__ unsigned cell_code(const SysDev &s, int x, int y, int z) {
+    const unsigned tile =
+        unsigned(x >> 2) + unsigned(s.ntile[0]) * (unsigned(y >> 2) + unsigned(s.ntile[1]) * unsigned(z >> 2));
+    return (tile << 6) | tile_spread2(unsigned(x) & 3u) | (tile_spread2(unsigned(y) & 3u) << 1) |
+           (tile_spread2(unsigned(z) & 3u) << 2);
+}
+/* ids per system (tiles x 64); id cell_base + ncell_ids is the ghost id */
+__host__ __device__ __forceinline__ unsigned ncell_ids(const SysDev &s) {
+    return unsigned(s.ntile[0]) * unsigned(s.ntile[1]) * unsigned(s.ntile[2]) * 64u;
+}
 
 struct SysState {
     double zeta;        // Nose-Hoover thermostat variable
@@ -117,6 +142,7 @@ struct SysState {
     double epot;        // potential energy (when accumulated)
     double area, volume;
     double cv, ca;      // constraint coefficients -k (Q - Q0) / Q0 used by the next forces
+    double vcom[3];     // mean lipid velocity removed before the next integration
     double pad;
 };
 
@@ -141,7 +167,9 @@ template<class R> struct KArgs {
     int *mesh_blk_sys;       // system of each of those blocks
     double *mesh_partial;    // [nmblk][2] area, volume
     uint32_t *nbr;           // warp-blocked ELL neighbour list (nbr_index)
-    int *nnb;
+    int *nnb;                // inner count | shell count << 16 (see k_nlist)
+    int2 *wmeta;             // per warp of slots, 32 entries: {staged ranges (0 = not staged), candidates},
+                             // then {first slot, first local index} of each range
     int cap;
     int2 *ranges;            // cell -> [begin, end) of its slots
     int *slot_of_home;
@@ -163,6 +191,7 @@ template<class R> struct KArgs {
     int rebuild_every;
     int variant;             // force-kernel form (see launch_step_langevin)
     int carry_forces;        // forces / torques persist between kernels (Nose-Hoover)
+    int zero_bulk;           // remove the mean lipid velocity before integrating
     const FFDev<R> *ff;      // force-field tables (global; staged into shared memory per block)
 };
 
@@ -176,6 +205,12 @@ template<class R> void launch_nh_final(const KArgs<R> &a, cudaStream_t st, bool 
 template<class R> void launch_nh_initial(const KArgs<R> &a, cudaStream_t st);
 template<class R> void launch_nh_prologue(const KArgs<R> &a, cudaStream_t st);
 template<class R> void launch_forces(const KArgs<R> &a, cudaStream_t st);
+template<class R> void launch_vcom(const KArgs<R> &a, cudaStream_t st);
+template<class R>
+cudaError_t launch_rdf(const double *x3, const int *type, int n, const double centre[3], const double L[3], int ta,
+                       int tb, double dr, int nbins, double rcut, unsigned long long *counts,
+                       unsigned long long *dropped, void *work, cudaStream_t st);
+template<class R> void launch_assign_temperature(const KArgs<R> &a, double kT, uint64_t seed, cudaStream_t st);
 
 template<class R> void launch_set_state(const KArgs<R> &a, const double *x, const double *n, const double *v,
                                         const double *o, int64_t nhome, cudaStream_t st);

@@ -132,6 +132,7 @@ class EngineBase {
                        const double *n3, const double *v3, const double *o3, const int *type, const int *tag, size_t n,
                        const int *bonds3, const double *bond_r0, size_t nb, const int *faces3, size_t nf) = 0;
     virtual int set_state(const double *x3, const double *n3, const double *v3, const double *o3) = 0;
+    virtual int assign_temperature(double kT, uint64_t seed) = 0;
     virtual int step(int nsteps, orbc_thermo *out) = 0;
     virtual int download(double *x3, double *n3, double *v3, double *o3) = 0;
     virtual int forces(double *f3, double *t3, double *e) = 0;
@@ -139,6 +140,8 @@ class EngineBase {
     virtual int neighbors(int *counts, int *list, int64_t cap, int64_t *total) = 0;
     virtual int cells(int sys, double *lo3, double *lc3, int *nc3, int *cell, double *off3, int *slot) = 0;
     virtual int rebuild() = 0;
+    virtual int rdf(int sys, int ta, int tb, double dr, int nbins, double rcut, uint64_t *counts,
+                    int64_t *dropped) = 0;
     virtual int profile(int nsteps, orbc_profile *out) = 0;
     virtual int autotune(int trial_steps, orbc_tune_trial *trials, int max_trials, int *ntrials) = 0;
     double last_ms = 0;
@@ -203,6 +206,7 @@ template<class R> class Engine : public EngineBase {
         }
         drop_graph();
         nh_primed = false;
+        vcom_valid = false;
         if (!relayout_in_progress) {  // topology copy for re-layouts (autotune)
             topo.descs.assign(descs, descs + nsys);
             topo.offsets.assign(offsets, offsets + nsys + 1);
@@ -285,6 +289,8 @@ template<class R> class Engine : public EngineBase {
             sd.off = int(off);
             sd.npad = int(npad_s);
             sd.nreal = int(ns);
+            sd.nlipid = 0;
+            for (int64_t i = b; i < e; ++i) sd.nlipid += type[i] == 0 ? 1 : 0;
             sd.cell_base = unsigned(cbase);
             sd.kv = d.kv;
             sd.V0 = d.V0;
@@ -292,7 +298,8 @@ template<class R> class Engine : public EngineBase {
             sd.A0 = d.A0;
             sd.Q = P.Q;
             off += npad_s;
-            cbase += uint64_t(sd.nc[0]) * sd.nc[1] * sd.nc[2] + 1;
+            for (int dd = 0; dd < 3; ++dd) sd.ntile[dd] = (sd.nc[dd] + 3) / 4;
+            cbase += uint64_t(sd.ntile[0]) * uint64_t(sd.ntile[1]) * uint64_t(sd.ntile[2]) * 64u + 1;
         }
         if (off >= MAX_SLOTS) return fail(ORBC_ERR_ARG, "upload: more than 2^27 particle slots");
         if (cbase >= (uint64_t(1) << 32) - 1) return fail(ORBC_ERR_ARG, "upload: more than 2^32 cells");
@@ -421,7 +428,7 @@ template<class R> class Engine : public EngineBase {
         if (epart.alloc(size_t(npad)) || faces.alloc(hfaces.size()) || ranges.alloc(size_t(total_cells)) ||
             soh.alloc(size_t(n)) || blk_sys.alloc(size_t(nb256)) || partial.alloc(size_t(nblk) * NPART) ||
             Sd.alloc(1) || sysd.alloc(size_t(nsys)) || ssd.alloc(size_t(nsys)) || counts.alloc(size_t(256) * ntiles) ||
-            dtot.alloc(256) || invd.alloc(size_t(npad)) || ffd.alloc(1) || nnb.alloc(size_t(npad)) ||
+            dtot.alloc(256) || invd.alloc(size_t(npad)) || ffd.alloc(1) || nnb.alloc(size_t(npad)) || wmeta.alloc(size_t(npad)) ||
             stage.alloc(size_t(n) * 12) || mesh_bs.alloc(hmbs.size()) || mesh_part.alloc(hmbs.size() * 2 + 2))
             return fail(ORBC_ERR_NOMEM, "upload: device allocation failed");
         cap = P.max_neighbors > 0 ? P.max_neighbors : 64;
@@ -451,6 +458,7 @@ template<class R> class Engine : public EngineBase {
         CK(cudaMemsetAsync(partial.p, 0, size_t(nblk) * NPART * sizeof(double), st));
         CK(cudaMemsetAsync(epart.p, 0, size_t(npad) * sizeof(double), st));
         CK(cudaMemsetAsync(nnb.p, 0, size_t(npad) * sizeof(int), st));
+        CK(cudaMemsetAsync(wmeta.p, 0, size_t(npad) * sizeof(int2), st));
         // other parity copies start equal (gather overwrites them before use)
         Scalars hs;
         std::memset(&hs, 0, sizeof(hs));
@@ -472,11 +480,11 @@ template<class R> class Engine : public EngineBase {
         // first neighbour build; grow the capacity if the guess was short
         int rc = build_lists(true);
         if (rc) return rc;
-        if (has_mesh) {
-            launch_mesh<R>(a, st);
-            CK(cudaGetLastError());
-            CK(cudaStreamSynchronize(st));
-        }
+        if (has_mesh) launch_mesh<R>(a, st);
+        launch_vcom<R>(a, st);  // temperature and lipid mean of the uploaded velocities
+        CK(cudaGetLastError());
+        CK(cudaStreamSynchronize(st));
+        vcom_valid = true;
         return ORBC_OK;
     }
 
@@ -491,8 +499,22 @@ template<class R> class Engine : public EngineBase {
         CK(cudaMemcpyAsync(d + 6 * nhome, v3, bytes, cudaMemcpyHostToDevice, st));
         CK(cudaMemcpyAsync(d + 9 * nhome, o3, bytes, cudaMemcpyHostToDevice, st));
         launch_set_state<R>(a, d, d + 3 * nhome, d + 6 * nhome, d + 9 * nhome, nhome, st);
+        launch_vcom<R>(a, st);  // temperature and lipid mean of the new velocities
         CK(cudaGetLastError());
         nh_primed = false;
+        vcom_valid = true;
+        return ORBC_OK;
+    }
+
+    int assign_temperature(double kT, uint64_t seed) override {
+        if (!uploaded) return fail(ORBC_ERR_STATE, "assign_temperature before upload");
+        if (!(kT >= 0)) return fail(ORBC_ERR_ARG, "assign_temperature: kT must be >= 0");
+        launch_assign_temperature<R>(a, kT, seed, st);
+        launch_vcom<R>(a, st);  // temperature and lipid mean of the new velocities
+        CK(cudaGetLastError());
+        CK(cudaStreamSynchronize(st));
+        nh_primed = false;
+        vcom_valid = true;
         return ORBC_OK;
     }
 
@@ -609,6 +631,12 @@ template<class R> class Engine : public EngineBase {
         CK(cudaMemcpyAsync(&before, Sd.p, sizeof(Scalars), cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
         int64_t extra = 0;
+        if (P.zero_bulk && P.integrator == ORBC_INT_LANGEVIN && !vcom_valid) {
+            launch_vcom<R>(a, st);
+            CK(cudaGetLastError());
+            vcom_valid = true;
+            extra += 1;
+        }
         if (P.integrator == ORBC_INT_NOSE_HOOVER && !nh_primed) {
             launch_rebuild<R>(a, st, true);
             if (has_mesh) launch_mesh<R>(a, st);
@@ -745,13 +773,24 @@ template<class R> class Engine : public EngineBase {
         CK(cudaMemcpy(hn.data(), nnb.p, hn.size() * sizeof(int), cudaMemcpyDeviceToHost));
         CK(cudaMemcpy(hh.data(), home[hs.lp].p, hh.size() * sizeof(int), cudaMemcpyDeviceToHost));
         CK(cudaMemcpy(hl.data(), nbr.p, hl.size() * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+        std::vector<int2> hm(static_cast<size_t>(npad));
+        CK(cudaMemcpy(hm.data(), wmeta.p, hm.size() * sizeof(int2), cudaMemcpyDeviceToHost));
         std::vector<std::vector<int>> per(static_cast<size_t>(nhome));
         for (int p = 0; p < npad; ++p) {
             const int h = hh[size_t(p)];
             if (h < 0) continue;
-            for (int k = 0; k < hn[size_t(p)]; ++k) {
-                const uint32_t ent = hl[size_t(nbr_index(p, k, cap))];
-                per[size_t(h)].push_back(hh[size_t(ent & NB_MASK)]);
+            const int2 *m = hm.data() + size_t(p >> 5) * 32;  // staged warp: entries are local indices
+            const int nin = hn[size_t(p)] & 0xffff, nout = hn[size_t(p)] >> 16;
+            for (int k = 0; k < nin + nout; ++k) {
+                const int row = k < nin ? k : cap - 1 - (k - nin);
+                const uint32_t ent = hl[size_t(nbr_index(p, row, cap))];
+                int j = int(ent & NB_MASK);
+                if (m[0].x > 0) {
+                    int r = 0;
+                    while (r + 1 < m[0].x && m[2 + r].y <= j) ++r;
+                    j = m[1 + r].x + (j - m[1 + r].y);
+                }
+                per[size_t(h)].push_back(hh[size_t(j)]);
             }
             std::sort(per[size_t(h)].begin(), per[size_t(h)].end());
         }
@@ -801,6 +840,39 @@ template<class R> class Engine : public EngineBase {
     int rebuild() override {
         if (!uploaded) return fail(ORBC_ERR_STATE, "rebuild before upload");
         return build_lists(false);
+    }
+
+    int rdf(int s, int ta, int tb, double dr, int nbins, double rcut, uint64_t *counts, int64_t *dropped) override {
+        if (!uploaded) return fail(ORBC_ERR_STATE, "rdf before upload");
+        if (s < 0 || s >= nsys) return fail(ORBC_ERR_ARG, "rdf: no such system");
+        if (!(dr > 0) || nbins < 1 || nbins > (1 << 24) || !counts || ta < -1 || ta >= NT || tb < -1 || tb >= NT)
+            return fail(ORBC_ERR_ARG, "rdf: need dr > 0, 1 <= nbins <= 2^24, types in -1..5 and a counts array");
+        const int64_t b = topo.offsets[size_t(s)], e = topo.offsets[size_t(s) + 1];
+        const int n = int(e - b);
+        const orbc_system_desc &d = topo.descs[size_t(s)];
+        double centre[3], L[3];
+        for (int k = 0; k < 3; ++k) {
+            centre[k] = 0.5 * (d.lo[k] + d.hi[k]);
+            L[k] = d.periodic[k] ? d.hi[k] - d.lo[k] : 0.0;
+        }
+        launch_download<R>(a, stage.p, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, st);
+        CK(cudaGetLastError());
+        DevBuf<int> td;
+        DevBuf<T4> work;
+        DevBuf<unsigned long long> cnt;
+        CK(td.alloc(size_t(n)));
+        CK(work.alloc(size_t(n)));
+        CK(cnt.alloc(size_t(nbins) + 1));
+        CK(cudaMemcpyAsync(td.p, topo.type.data() + b, size_t(n) * sizeof(int), cudaMemcpyHostToDevice, st));
+        CK(cudaMemsetAsync(cnt.p, 0, (size_t(nbins) + 1) * sizeof(unsigned long long), st));
+        CK(launch_rdf<R>(stage.p + 3 * b, td.p, n, centre, L, ta, tb, dr, nbins, rcut, cnt.p, cnt.p + nbins, work.p,
+                         st));
+        std::vector<unsigned long long> h(size_t(nbins) + 1);
+        CK(cudaMemcpyAsync(h.data(), cnt.p, h.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        for (int k = 0; k < nbins; ++k) counts[k] = uint64_t(h[size_t(k)]);
+        if (dropped) *dropped = int64_t(h[size_t(nbins)]);
+        return ORBC_OK;
     }
 
     int profile(int nsteps, orbc_profile *out) override {
@@ -876,18 +948,16 @@ template<class R> class Engine : public EngineBase {
         std::vector<int> hn(static_cast<size_t>(npad)), hh(static_cast<size_t>(npad));
         CK(cudaMemcpy(hn.data(), nnb.p, hn.size() * sizeof(int), cudaMemcpyDeviceToHost));
         CK(cudaMemcpy(hh.data(), home[hs.lp].p, hh.size() * sizeof(int), cudaMemcpyDeviceToHost));
-        double tot = 0;
+        double tot = 0, tin = 0;
         int64_t cnt = 0;
         for (int p = 0; p < npad; ++p)
             if (hh[size_t(p)] >= 0) {
-                tot += hn[size_t(p)];
+                tot += (hn[size_t(p)] & 0xffff) + (hn[size_t(p)] >> 16);
+                tin += hn[size_t(p)] & 0xffff;
                 ++cnt;
             }
         out->mean_neighbors = cnt ? tot / double(cnt) : 0.0;
-        // fraction of list entries inside the interaction range, from the list cutoff geometry
-        // (a flat membrane: pairs scale with the square of the cutoff)
-        const double rc = 2.6, rl = 2.6 + P.skin;
-        out->pairs_in_cutoff = out->mean_neighbors * (rc * rc) / (rl * rl);
+        out->pairs_in_cutoff = cnt ? tin / double(cnt) : 0.0;  // inner entries at the last build
         return ORBC_OK;
     }
 
@@ -1037,11 +1107,14 @@ template<class R> class Engine : public EngineBase {
         for (int ti = 0; ti < 16; ++ti)
             for (int tj = 0; tj < 16; ++tj) {
                 float v = 0.f;
+                float vin = 0.f;
                 if (ti < NT && tj < NT && F.range[ti * NT + tj] > 0) {
                     const double rl = F.range[ti * NT + tj] + P.skin;
                     v = float(rl * rl);
+                    vin = float(F.range[ti * NT + tj] * F.range[ti * NT + tj]);
                 }
                 hff.rlist2[ti * 16 + tj] = v;
+                hff.rin2[ti * 16 + tj] = vin;
             }
     }
 
@@ -1071,6 +1144,7 @@ template<class R> class Engine : public EngineBase {
         a.mesh_partial = mesh_part.p;
         a.nbr = nbr.p;
         a.nnb = nnb.p;
+        a.wmeta = wmeta.p;
         a.cap = cap;
         a.ranges = ranges.p;
         a.slot_of_home = soh.p;
@@ -1094,6 +1168,7 @@ template<class R> class Engine : public EngineBase {
         a.rebuild_every = P.rebuild_every;
         a.variant = P.kernel_variant;
         a.carry_forces = P.integrator == ORBC_INT_NOSE_HOOVER ? 1 : 0;
+        a.zero_bulk = P.zero_bulk ? 1 : 0;
         a.ff = ffd.p;
     }
 
@@ -1153,7 +1228,7 @@ template<class R> class Engine : public EngineBase {
     cudaGraphExec_t gexec = nullptr;
     bool graph_cond = false;
     int graph_steps = 0;
-    bool uploaded = false, nh_primed = false, has_mesh = false;
+    bool uploaded = false, nh_primed = false, has_mesh = false, vcom_valid = false;
     int nsys = 0, npad = 0, nblk = 0, cap = 0, passes = 4, ntiles = 1, maxb = 0, maxf = 0, nfaces = 0, nmblk = 0;
     int64_t nhome = 0;
     uint64_t total_cells = 0;
@@ -1170,6 +1245,7 @@ template<class R> class Engine : public EngineBase {
     DevBuf<int> soh, blk_sys, counts, dtot, invd, nnb, mesh_bs;
     DevBuf<double> mesh_part;
     DevBuf<uint32_t> nbr;
+    DevBuf<int2> wmeta;
     DevBuf<Scalars> Sd;
     DevBuf<SysDev> sysd;
     DevBuf<SysState> ssd;
@@ -1225,7 +1301,7 @@ int orbc_gpu_create(const orbc_params *p, orbc_handle **out) {
     *out = nullptr;
     if (!(p->dt > 0) || p->skin < 0 || (p->precision != ORBC_PREC_FP64 && p->precision != ORBC_PREC_MIXED) ||
         (p->integrator != ORBC_INT_LANGEVIN && p->integrator != ORBC_INT_NOSE_HOOVER) ||
-        (p->kernel_variant < 0 || p->kernel_variant > 3)) {
+        (p->kernel_variant < 0 || p->kernel_variant > 3) || (p->zero_bulk != 0 && p->zero_bulk != 1)) {
         g_last_error = "create: invalid parameters";
         return ORBC_ERR_ARG;
     }
@@ -1303,6 +1379,13 @@ int orbc_gpu_cells(orbc_handle *h, int sys, double *lo3, double *lc3, int *nc3, 
     return h ? h->e->cells(sys, lo3, lc3, nc3, cell, offset3, slot) : ORBC_ERR_ARG;
 }
 int orbc_gpu_rebuild(orbc_handle *h) { return h ? h->e->rebuild() : ORBC_ERR_ARG; }
+int orbc_gpu_rdf(orbc_handle *h, int sys, int type_a, int type_b, double dr, int nbins, double rcut,
+                 uint64_t *counts, int64_t *dropped) {
+    return h ? h->e->rdf(sys, type_a, type_b, dr, nbins, rcut, counts, dropped) : ORBC_ERR_ARG;
+}
+int orbc_gpu_assign_temperature(orbc_handle *h, double kBT, uint64_t seed) {
+    return h ? h->e->assign_temperature(kBT, seed) : ORBC_ERR_ARG;
+}
 int orbc_gpu_last_timing(orbc_handle *h, double *ms, int64_t *launches) {
     if (!h) return ORBC_ERR_ARG;
     if (ms) *ms = h->e->last_ms;

@@ -1,0 +1,167 @@
+// Pair-distance histogram of one system (src/rdf.h:26-81: `rdf` over all
+// pairs with dr-wide bins, `rdf_1peak_r` with a type filter and a cutoff).
+//
+// The positions of the system's particles are packed once (caller order,
+// relative to the centre of the system's box, in the working precision) and
+// every unordered pair i < j is visited by a tiled all-pairs sweep: a block
+// owns 256 i-particles, stages 256 j-particles at a time in shared memory and
+// accumulates into a block-private shared-memory histogram that is added to
+// the global one at the end (integer atomics, so the counts do not depend on
+// the order).  Every floating-point operation is rounded once, in the same
+// order as the CPU restatement, so the histogram is bit-identical to it.
+#include "orbc_device.cuh"
+
+namespace orbc {
+
+namespace {
+
+template<class T> struct P4;
+template<> struct P4<float> {
+    using T4 = float4;
+};
+template<> struct P4<double> {
+    using T4 = double4a;
+};
+
+__device__ __forceinline__ float o_sub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ double o_sub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ float o_add(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double o_add(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float o_mul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double o_mul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float o_div(float a, float b) { return __fdiv_rn(a, b); }
+__device__ __forceinline__ double o_div(double a, double b) { return __ddiv_rn(a, b); }
+__device__ __forceinline__ float o_sqrt(float a) { return __fsqrt_rn(a); }
+__device__ __forceinline__ double o_sqrt(double a) { return __dsqrt_rn(a); }
+__device__ __forceinline__ float o_rint(float a) { return rintf(a); }
+__device__ __forceinline__ double o_rint(double a) { return rint(a); }
+
+constexpr int RDF_TILE = 256;
+constexpr int RDF_JT = 16;  // j-tiles per block
+
+template<class T>
+__global__ void k_rdf_pack(const double *x3, const int *type, int n, double c0, double c1, double c2,
+                           typename P4<T>::T4 *out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    typename P4<T>::T4 q;
+    q.x = T(__dsub_rn(x3[3 * int64_t(i)], c0));
+    q.y = T(__dsub_rn(x3[3 * int64_t(i) + 1], c1));
+    q.z = T(__dsub_rn(x3[3 * int64_t(i) + 2], c2));
+    q.w = T(type[i]);
+    out[i] = q;
+}
+
+struct RdfArgs {
+    int n, ta, tb, nbins, smem_hist;
+    double dr, rcut, L[3];
+    unsigned long long *counts, *dropped;
+};
+
+__device__ __forceinline__ bool tmatch(int t, int want) { return want < 0 || t == want; }
+
+template<class T> __global__ void __launch_bounds__(RDF_TILE) k_rdf(const typename P4<T>::T4 *p, RdfArgs ra) {
+    using T4 = typename P4<T>::T4;
+    extern __shared__ unsigned hist[];
+    __shared__ T4 tile[RDF_TILE];
+    __shared__ unsigned long long sdrop;
+    const int it = blockIdx.x;
+    const int ntile = (ra.n + RDF_TILE - 1) / RDF_TILE;
+    const int jt0 = blockIdx.y * RDF_JT, jt1 = min(ntile, jt0 + RDF_JT);
+    if (jt1 <= it) return;  // whole chunk below the diagonal (uniform per block)
+    if (ra.smem_hist)
+        for (int b = threadIdx.x; b < ra.nbins; b += blockDim.x) hist[b] = 0u;
+    if (threadIdx.x == 0) sdrop = 0ull;
+    const int i = it * RDF_TILE + threadIdx.x;
+    T4 pi;
+    pi.x = pi.y = pi.z = T(0);
+    pi.w = T(-1);
+    if (i < ra.n) pi = p[i];
+    const int ti = int(pi.w);
+    const T dr = T(ra.dr), rcut = T(ra.rcut);
+    const T L[3] = {T(ra.L[0]), T(ra.L[1]), T(ra.L[2])};
+    unsigned long long drop = 0;
+    for (int jt = max(jt0, it); jt < jt1; ++jt) {
+        __syncthreads();
+        const int jl = jt * RDF_TILE + threadIdx.x;
+        if (jl < ra.n) tile[threadIdx.x] = p[jl];
+        __syncthreads();
+        if (i >= ra.n) continue;
+        const int kend = min(RDF_TILE, ra.n - jt * RDF_TILE);
+        for (int k = (jt == it ? threadIdx.x + 1 : 0); k < kend; ++k) {
+            const T4 q = tile[k];
+            const int tj = int(q.w);
+            if (!((tmatch(ti, ra.ta) && tmatch(tj, ra.tb)) || (tmatch(ti, ra.tb) && tmatch(tj, ra.ta)))) continue;
+            T dd[3] = {o_sub(pi.x, q.x), o_sub(pi.y, q.y), o_sub(pi.z, q.z)};
+#pragma unroll
+            for (int d = 0; d < 3; ++d)
+                if (L[d] > T(0)) dd[d] = o_sub(dd[d], o_mul(L[d], o_rint(o_div(dd[d], L[d]))));
+            const T r = o_sqrt(o_add(o_add(o_mul(dd[0], dd[0]), o_mul(dd[1], dd[1])), o_mul(dd[2], dd[2])));
+            if (rcut > T(0) && !(r < rcut)) {
+                ++drop;
+                continue;
+            }
+            const T qb = o_div(r, dr);
+            const int b = qb < T(2147483647.0) ? int(qb) : 2147483647;
+            if (b >= ra.nbins) {
+                ++drop;
+                continue;
+            }
+            if (ra.smem_hist)
+                atomicAdd(&hist[b], 1u);
+            else
+                atomicAdd(&ra.counts[b], 1ull);
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) drop += __shfl_xor_sync(0xffffffffu, drop, o);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0 && drop) atomicAdd(&sdrop, drop);
+    __syncthreads();
+    if (threadIdx.x == 0 && sdrop) atomicAdd(ra.dropped, sdrop);
+    if (ra.smem_hist)
+        for (int b = threadIdx.x; b < ra.nbins; b += blockDim.x)
+            if (hist[b]) atomicAdd(&ra.counts[b], (unsigned long long)hist[b]);
+}
+
+}  // namespace
+
+/* Histogram of the n points x3 (device, AoS double, caller order) with types
+ * type (device); counts (device, nbins) and dropped (device, 1) must be
+ * zeroed by the caller; work (device) holds n packed points (16 or 32 B). */
+template<class R>
+cudaError_t launch_rdf(const double *x3, const int *type, int n, const double centre[3], const double L[3], int ta,
+                       int tb, double dr, int nbins, double rcut, unsigned long long *counts,
+                       unsigned long long *dropped, void *work, cudaStream_t st) {
+    using T4 = typename P4<R>::T4;
+    T4 *pk = static_cast<T4 *>(work);
+    k_rdf_pack<R><<<(n + 255) / 256, 256, 0, st>>>(x3, type, n, centre[0], centre[1], centre[2], pk);
+    RdfArgs ra;
+    ra.n = n;
+    ra.ta = ta;
+    ra.tb = tb;
+    ra.nbins = nbins;
+    ra.dr = dr;
+    ra.rcut = rcut;
+    for (int d = 0; d < 3; ++d) ra.L[d] = L[d];
+    ra.counts = counts;
+    ra.dropped = dropped;
+    const size_t hbytes = size_t(nbins) * sizeof(unsigned);
+    ra.smem_hist = hbytes <= size_t(160) * 1024 ? 1 : 0;
+    const size_t dyn = ra.smem_hist ? hbytes : 0;
+    cudaError_t e = cudaFuncSetAttribute(k_rdf<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(dyn));
+    if (e != cudaSuccess) return e;
+    const int ntile = (n + RDF_TILE - 1) / RDF_TILE;
+    const dim3 grid(unsigned(ntile), unsigned((ntile + RDF_JT - 1) / RDF_JT));
+    k_rdf<R><<<grid, RDF_TILE, dyn, st>>>(pk, ra);
+    return cudaGetLastError();
+}
+
+template cudaError_t launch_rdf<float>(const double *, const int *, int, const double *, const double *, int, int,
+                                       double, int, double, unsigned long long *, unsigned long long *, void *,
+                                       cudaStream_t);
+template cudaError_t launch_rdf<double>(const double *, const int *, int, const double *, const double *, int, int,
+                                        double, int, double, unsigned long long *, unsigned long long *, void *,
+                                        cudaStream_t);
+
+}  // namespace orbc

@@ -38,6 +38,60 @@ template<> __device__ __forceinline__ double4a ldg4<double>(const double4a *p) {
     return r;
 }
 
+/* Partner loads: read-only global path, or the warp's shared-memory copy. */
+template<class R, bool SM> __device__ __forceinline__ typename Vec<R>::T4 ldp(const typename Vec<R>::T4 *p) {
+    if (SM)
+        return *p;
+    else
+        return ldg4<R>(p);
+}
+
+/* Shared-memory copy of the warp's neighbourhood (mixed precision only). */
+template<class R> struct StageBuf {
+    static constexpr int N = sizeof(typename Vec<R>::T4) == 16 ? STG_CAND : 1;
+    typename Vec<R>::T4 pos[STEP_BS / 32][N], nrm[STEP_BS / 32][N];
+};
+
+/* Copy the positions and orientations of this warp's candidate ranges (wmeta)
+ * to shared memory with cp.async; returns whether the warp's list entries are
+ * local indices into that copy.  All 32 lanes must call it. */
+template<class R>
+__device__ __forceinline__ bool stage_warp(const KArgs<R> &a, int i, int cur, StageBuf<R> &sb) {
+    if constexpr (StageBuf<R>::N == 1) {
+        return false;
+    } else {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int2 m = a.wmeta[int64_t(i >> 5) * 32 + lane];
+    const int nr = __shfl_sync(0xffffffffu, m.x, 0);
+    if (nr == 0) return false;
+    const int ntot = __shfl_sync(0xffffffffu, m.y, 0);
+    const typename Vec<R>::T4 *pos = a.pos[cur], *nrm = a.nrm[cur];
+    for (int t0 = 0; t0 < ntot; t0 += 32) {
+        const int t = t0 + lane;
+        // range r holding candidate t: the last r < nr with first local index <= t
+        int r = 0;
+#pragma unroll
+        for (int step = 16; step > 0; step >>= 1) {
+            const int c = r + step;
+            const int oc = __shfl_sync(0xffffffffu, m.y, min(c + 1, 31));
+            if (c < nr && oc <= t) r = c;
+        }
+        const int first = __shfl_sync(0xffffffffu, m.x, r + 1);
+        const int loc = __shfl_sync(0xffffffffu, m.y, r + 1);
+        if (t < ntot) {
+            const int j = first + (t - loc);
+            const unsigned dp = unsigned(__cvta_generic_to_shared(&sb.pos[warp][t]));
+            const unsigned dn = unsigned(__cvta_generic_to_shared(&sb.nrm[warp][t]));
+            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dp), "l"(pos + j) : "memory");
+            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dn), "l"(nrm + j) : "memory");
+        }
+    }
+    asm volatile("cp.async.wait_all;" ::: "memory");
+    __syncwarp();
+    return true;
+    }
+}
+
 __device__ __forceinline__ void inv_sqrt(float r2, float &r, float &rinv) {
     rinv = rsqrtf(r2);
     r = r2 * rinv;
@@ -191,14 +245,18 @@ __device__ __forceinline__ R bond_kappa(const BondP<R> &B, R r0, R r, R &e, int 
     }
 }
 
-/* Bring this warp's block of neighbour entries (cap rows of 128 B, read
- * once per step) into L1 ahead of the pair loop, so the loop's entry loads do
- * not wait on DRAM.  All 32 lanes must call it. */
-__device__ __forceinline__ void prefetch_warp_list(const uint32_t *nbr, int i, int cap, int cnt) {
-    const int rows = __reduce_max_sync(0xffffffffu, unsigned(cnt));
+/* Bring the used rows of this warp's block of neighbour entries (read once
+ * per step) into L1 ahead of the pair loops, so the loops' entry loads do not
+ * wait on DRAM.  packed = inner count | shell count << 16.  All 32 lanes must
+ * call it. */
+__device__ __forceinline__ void prefetch_warp_list(const uint32_t *nbr, int i, int cap, int packed) {
+    const int rin = __reduce_max_sync(0xffffffffu, unsigned(packed & 0xffff));
+    const int rout = __reduce_max_sync(0xffffffffu, unsigned(packed >> 16));
     const uint32_t *base = nbr + nbr_index(i & ~31, 0, cap);
-    for (int r = int(threadIdx.x & 31); r < rows; r += 32)
-        asm volatile("prefetch.global.L1 [%0];" ::"l"(base + 32 * r));
+    for (int r = int(threadIdx.x & 31); r < rin + rout; r += 32) {
+        const int row = r < rin ? r : cap - 1 - (r - rin);
+        asm volatile("prefetch.global.L1 [%0];" ::"l"(base + 32 * row));
+    }
 }
 
 template<class R> __device__ __forceinline__ void stage_ff(FFDev<R> *dst, const FFDev<R> *src) {
@@ -223,95 +281,95 @@ template<class R> __device__ __forceinline__ void init_shift(typename Vec<R>::T4
 
 /* All forces and torques on particle slot i: pair terms over its neighbour
  * list (variant V, see launch_step_langevin), bonds, mesh constraint. */
-template<class R, bool E, int V>
+template<class R, bool E, int V, bool SM>
 __device__ __forceinline__ void particle_forces(const KArgs<R> &a, const FFDev<R> &F, int i, int cur, int lp, int w,
                                                 const typename Vec<R>::T4 &pi, const typename Vec<R>::T4 &ni,
                                                 const SysDev &sd, const SysState &ss,
-                                                const typename Vec<R>::T4 *sh, R3<R> &f, R3<R> &t, R &e,
+                                                const typename Vec<R>::T4 *sh, const typename Vec<R>::T4 *srcp,
+                                                const typename Vec<R>::T4 *srcn, R3<R> &f, R3<R> &t, R &e,
                                                 int &flags) {
     using T4 = typename Vec<R>::T4;
     const int ty = w_type(w);
     const R Lx = R(sd.Lc[0]), Ly = R(sd.Lc[1]), Lz = R(sd.Lc[2]);
-    const T4 *__restrict__ pos = a.pos[cur];
-    const T4 *__restrict__ nrm = a.nrm[cur];
+    const T4 *__restrict__ pos = a.pos[cur];  // bond and face partners (global slots)
     const uint32_t *__restrict__ nb = a.nbr + nbr_index(i, 0, a.cap);
-    const int cnt = a.nnb[i];
+    const int packed = a.nnb[i];
+    const int nin = packed & 0xffff, nout = packed >> 16;
+    const uint32_t *__restrict__ shell = nb + int64_t(a.cap - 1) * 32;  // shell rows run downwards
     const int64_t stride = 32;
     const PairP<R> &LL = F.pair[0];
     const R ll_cutsq = LL.cutsq, ll_cut = LL.cut, ll_alpha = LL.alpha, ll_aatt = LL.aatt;
     const R ll_rep8 = LL.rep8, ll_att4 = LL.att4, ll_rep = LL.rep, ll_att = LL.att;
-    if (V & 1) {
-        /* software-pipelined pass: the entry two ahead and the gathers one
-         * ahead are in flight while the current pair is evaluated */
-        uint32_t e1 = cnt > 0 ? __ldg(nb) : 0u;
-        uint32_t e2 = cnt > 1 ? __ldg(nb + stride) : 0u;
-        T4 pn, nn;
-        if (cnt > 0) {
-            pn = ldg4<R>(pos + int(e1 & NB_MASK));
-            nn = ldg4<R>(nrm + int(e1 & NB_MASK));
+    auto pair = [&](uint32_t ent, const T4 &pj, const T4 &nj) {
+        const T4 s = sh[ent >> NB_SHIFT];
+        const R dx = (pi.x - pj.x) + s.x * Lx;
+        const R dy = (pi.y - pj.y) + s.y * Ly;
+        const R dz = (pi.z - pj.z) + s.z * Lz;
+        const R r2 = dx * dx + dy * dy + dz * dz;
+        const int tj = w_type(wbits(pj.w));
+        if ((ty | tj) == 0) {
+            if (r2 < ll_cutsq && r2 > R(1e-5)) {
+                PairP<R> P;
+                P.cut = ll_cut;
+                P.alpha = ll_alpha;
+                P.aatt = ll_aatt;
+                P.rep8 = ll_rep8;
+                P.att4 = ll_att4;
+                P.rep = ll_rep;
+                P.att = ll_att;
+                aniso<R, E>(P, dx, dy, dz, r2, ni.x, ni.y, ni.z, nj.x, nj.y, nj.z, f, t, e);
+            }
+        } else {
+            pair_general<R, E, (V & 2) != 0>(F.pair[ty * NT + tj], dx, dy, dz, r2, ni.x, ni.y, ni.z, nj.x, nj.y,
+                                             nj.z, f, t, e);
         }
-        for (int k = 0; k < cnt; ++k) {
+    };
+    // Inner rows: partners that were inside the interaction range at the last
+    // build; almost all still are, so every lane does the pair arithmetic.
+    if (V & 1) {
+        /* software-pipelined: the entry two ahead and the gathers one ahead
+         * are in flight while the current pair is evaluated */
+        uint32_t e1 = nin > 0 ? __ldg(nb) : 0u;
+        uint32_t e2 = nin > 1 ? __ldg(nb + stride) : 0u;
+        T4 pn, nn;
+        if (nin > 0) {
+            pn = ldp<R, SM>(srcp + int(e1 & NB_MASK));
+            nn = ldp<R, SM>(srcn + int(e1 & NB_MASK));
+        }
+        for (int k = 0; k < nin; ++k) {
             const uint32_t ent = e1;
             const T4 pj = pn, nj = nn;
             e1 = e2;
-            if (k + 2 < cnt) e2 = __ldg(nb + int64_t(k + 2) * stride);
-            if (k + 1 < cnt) {
-                pn = ldg4<R>(pos + int(e1 & NB_MASK));
-                nn = ldg4<R>(nrm + int(e1 & NB_MASK));
+            if (k + 2 < nin) e2 = __ldg(nb + int64_t(k + 2) * stride);
+            if (k + 1 < nin) {
+                pn = ldp<R, SM>(srcp + int(e1 & NB_MASK));
+                nn = ldp<R, SM>(srcn + int(e1 & NB_MASK));
             }
-            const T4 s = sh[ent >> NB_SHIFT];
-            const R dx = (pi.x - pj.x) + s.x * Lx;
-            const R dy = (pi.y - pj.y) + s.y * Ly;
-            const R dz = (pi.z - pj.z) + s.z * Lz;
-            const R r2 = dx * dx + dy * dy + dz * dz;
-            const int tj = w_type(wbits(pj.w));
-            if ((ty | tj) == 0) {
-                if (r2 < ll_cutsq && r2 > R(1e-5)) {
-                    PairP<R> P;
-                    P.cut = ll_cut;
-                    P.alpha = ll_alpha;
-                    P.aatt = ll_aatt;
-                    P.rep8 = ll_rep8;
-                    P.att4 = ll_att4;
-                    P.rep = ll_rep;
-                    P.att = ll_att;
-                    aniso<R, E>(P, dx, dy, dz, r2, ni.x, ni.y, ni.z, nj.x, nj.y, nj.z, f, t, e);
-                }
-            } else {
-                pair_general<R, E, (V & 2) != 0>(F.pair[ty * NT + tj], dx, dy, dz, r2, ni.x, ni.y, ni.z, nj.x, nj.y, nj.z, f, t,
-                                   e);
-            }
+            pair(ent, pj, nj);
         }
     } else {
 #pragma unroll 2
-        for (int k = 0; k < cnt; ++k) {
+        for (int k = 0; k < nin; ++k) {
             const uint32_t ent = __ldg(nb + int64_t(k) * stride);
             const int j = int(ent & NB_MASK);
-            const T4 s = sh[ent >> NB_SHIFT];
-            const T4 pj = ldg4<R>(pos + j);
-            const T4 nj = ldg4<R>(nrm + j);
-            const R dx = (pi.x - pj.x) + s.x * Lx;
-            const R dy = (pi.y - pj.y) + s.y * Ly;
-            const R dz = (pi.z - pj.z) + s.z * Lz;
-            const R r2 = dx * dx + dy * dy + dz * dz;
-            const int tj = w_type(wbits(pj.w));
-            if ((ty | tj) == 0) {
-                if (r2 < ll_cutsq && r2 > R(1e-5)) {
-                    PairP<R> P;
-                    P.cut = ll_cut;
-                    P.alpha = ll_alpha;
-                    P.aatt = ll_aatt;
-                    P.rep8 = ll_rep8;
-                    P.att4 = ll_att4;
-                    P.rep = ll_rep;
-                    P.att = ll_att;
-                    aniso<R, E>(P, dx, dy, dz, r2, ni.x, ni.y, ni.z, nj.x, nj.y, nj.z, f, t, e);
-                }
-            } else {
-                pair_general<R, E, (V & 2) != 0>(F.pair[ty * NT + tj], dx, dy, dz, r2, ni.x, ni.y, ni.z, nj.x, nj.y, nj.z, f, t,
-                                   e);
-            }
+            pair(ent, ldp<R, SM>(srcp + j), ldp<R, SM>(srcn + j));
         }
+    }
+    // Shell rows: partners in the skin at the last build, mostly still outside
+    // the range; the orientation is only gathered for the few that came in.
+#pragma unroll 2
+    for (int k = 0; k < nout; ++k) {
+        const uint32_t ent = __ldg(shell - int64_t(k) * stride);
+        const int j = int(ent & NB_MASK);
+        const T4 pj = ldp<R, SM>(srcp + j);
+        const T4 s = sh[ent >> NB_SHIFT];
+        const R dx = (pi.x - pj.x) + s.x * Lx;
+        const R dy = (pi.y - pj.y) + s.y * Ly;
+        const R dz = (pi.z - pj.z) + s.z * Lz;
+        const R r2 = dx * dx + dy * dy + dz * dz;
+        const int tj = w_type(wbits(pj.w));
+        const R lim = ((ty | tj) == 0) ? ll_cutsq : F.pair[ty * NT + tj].anysq;
+        if (r2 < lim) pair(ent, pj, ldp<R, SM>(srcn + j));
     }
     // bonds
     const int bd = w_bdeg(w);
@@ -351,8 +409,8 @@ __device__ __forceinline__ void particle_forces(const KArgs<R> &a, const FFDev<R
     }
 }
 
-__device__ __forceinline__ void philox3(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t k0, uint32_t k1,
-                                        uint32_t &o0, uint32_t &o1, uint32_t &o2) {
+__device__ __forceinline__ void philox4(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t k0, uint32_t k1,
+                                        uint32_t o[4]) {
 #pragma unroll
     for (int r = 0; r < 10; ++r) {
         const uint32_t lo0 = 0xD2511F53u * c0, hi0 = __umulhi(0xD2511F53u, c0);
@@ -365,21 +423,52 @@ __device__ __forceinline__ void philox3(uint32_t c0, uint32_t c1, uint32_t c2, u
         k0 += 0x9E3779B9u;
         k1 += 0xBB67AE85u;
     }
-    o0 = c0;
-    o1 = c1;
-    o2 = c2;
+    o[0] = c0;
+    o[1] = c1;
+    o[2] = c2;
+    o[3] = c3;
+}
+__device__ __forceinline__ void philox3(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t k0, uint32_t k1,
+                                        uint32_t &o0, uint32_t &o1, uint32_t &o2) {
+    uint32_t o[4];
+    philox4(c0, c1, c2, c3, k0, k1, o);
+    o0 = o[0];
+    o1 = o[1];
+    o2 = o[2];
 }
 template<class R> __device__ __forceinline__ R u11(uint32_t u) { return R(u >> 8) * R(1.0 / 8388608.0) - R(1); }
 
 constexpr int STEP_WARPS = STEP_BS / 32;
 
-enum { MODE_LANGEVIN = 0, MODE_NH_FINAL = 1, MODE_NH_INITIAL = 2, MODE_FORCES = 3 };
+/* particle_forces with the partners read from the warp's shared-memory copy
+ * (stg) or from global memory. */
+template<class R, bool E, int V>
+__device__ __forceinline__ void forces_of(bool stg, const StageBuf<R> &sb, const KArgs<R> &a, const FFDev<R> &F,
+                                          int i, int cur, int lp, int w, const typename Vec<R>::T4 &pi,
+                                          const typename Vec<R>::T4 &ni, const SysDev &sd, const SysState &ss,
+                                          const typename Vec<R>::T4 *sh, R3<R> &f, R3<R> &t, R &e, int &flags) {
+    if constexpr (StageBuf<R>::N > 1) {
+        if (stg) {
+            const int warp = threadIdx.x >> 5;
+            particle_forces<R, E, V, true>(a, F, i, cur, lp, w, pi, ni, sd, ss, sh, sb.pos[warp], sb.nrm[warp], f, t,
+                                           e, flags);
+            return;
+        }
+    }
+    particle_forces<R, E, V, false>(a, F, i, cur, lp, w, pi, ni, sd, ss, sh, a.pos[cur], a.nrm[cur], f, t, e, flags);
+}
+
+// resident blocks per SM the force kernels are compiled for: the mixed form
+// is limited by its shared-memory stage to 5 blocks
+#define STEP_MINB(R, V) (sizeof(R) == 4 ? 5 : (((V) & 2) ? 6 : 8))
+
+enum { MODE_LANGEVIN = 0, MODE_NH_FINAL = 1, MODE_NH_INITIAL = 2, MODE_FORCES = 3, MODE_VCOM = 4 };
 
 /* Block partial sums -> per-system totals in the last block (fixed order). */
 template<class R>
 __device__ __forceinline__ void finish(const KArgs<R> &a, double ke, double ep, float md2, int flags, int mode,
-                                       int count_step) {
-    __shared__ double sk[8], se[8];
+                                       int count_step, double vx = 0, double vy = 0, double vz = 0) {
+    __shared__ double sk[8], se[8], sv[8][3];
     __shared__ float sm[8];
     __shared__ int sf[8];
     __shared__ bool last;
@@ -390,16 +479,22 @@ __device__ __forceinline__ void finish(const KArgs<R> &a, double ke, double ep, 
         ep += __shfl_xor_sync(0xffffffffu, ep, o);
         md2 = fmaxf(md2, __shfl_xor_sync(0xffffffffu, md2, o));
         flags |= __shfl_xor_sync(0xffffffffu, flags, o);
+        vx += __shfl_xor_sync(0xffffffffu, vx, o);
+        vy += __shfl_xor_sync(0xffffffffu, vy, o);
+        vz += __shfl_xor_sync(0xffffffffu, vz, o);
     }
     if (lane == 0) {
         sk[warp] = ke;
         se[warp] = ep;
         sm[warp] = md2;
         sf[warp] = flags;
+        sv[warp][0] = vx;
+        sv[warp][1] = vy;
+        sv[warp][2] = vz;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        double k = 0, e = 0;
+        double k = 0, e = 0, v0 = 0, v1 = 0, v2 = 0;
         float m = 0;
         int fl = 0;
         for (int w = 0; w < STEP_WARPS; ++w) {
@@ -407,12 +502,18 @@ __device__ __forceinline__ void finish(const KArgs<R> &a, double ke, double ep, 
             e += se[w];
             m = fmaxf(m, sm[w]);
             fl |= sf[w];
+            v0 += sv[w][0];
+            v1 += sv[w][1];
+            v2 += sv[w][2];
         }
         double *p = a.partial + int64_t(blockIdx.x) * NPART;
         p[0] = k;
         p[1] = e;
         p[2] = double(m);
         p[3] = double(fl);
+        p[4] = v0;
+        p[5] = v1;
+        p[6] = v2;
         __threadfence();
         const unsigned ticket = atomicAdd(&a.S->blk_counter, 1u);
         last = (ticket == gridDim.x - 1);
@@ -424,19 +525,32 @@ __device__ __forceinline__ void finish(const KArgs<R> &a, double ke, double ep, 
     for (int s = warp; s < a.nsys; s += STEP_WARPS) {
         const SysDev &sd = a.sys[s];
         const int b0 = sd.off / STEP_BS, b1 = (sd.off + sd.npad) / STEP_BS;
-        double k = 0, e = 0;
+        double k = 0, e = 0, v0 = 0, v1 = 0, v2 = 0;
         for (int b = b0 + lane; b < b1; b += 32) {
             k += __ldcg(a.partial + int64_t(b) * NPART);
             e += __ldcg(a.partial + int64_t(b) * NPART + 1);
+            v0 += __ldcg(a.partial + int64_t(b) * NPART + 4);
+            v1 += __ldcg(a.partial + int64_t(b) * NPART + 5);
+            v2 += __ldcg(a.partial + int64_t(b) * NPART + 6);
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
             k += __shfl_xor_sync(0xffffffffu, k, o);
             e += __shfl_xor_sync(0xffffffffu, e, o);
+            v0 += __shfl_xor_sync(0xffffffffu, v0, o);
+            v1 += __shfl_xor_sync(0xffffffffu, v1, o);
+            v2 += __shfl_xor_sync(0xffffffffu, v2, o);
         }
         if (lane == 0) {
             SysState &ss = a.ss[s];
-            if (mode == MODE_LANGEVIN || mode == MODE_FORCES) {
+            if ((mode == MODE_LANGEVIN || mode == MODE_NH_INITIAL || mode == MODE_VCOM) && sd.nlipid > 0) {
+                ss.vcom[0] = v0 / double(sd.nlipid);
+                ss.vcom[1] = v1 / double(sd.nlipid);
+                ss.vcom[2] = v2 / double(sd.nlipid);
+            }
+            if (mode == MODE_VCOM) {
+                ss.ke2 = k;
+            } else if (mode == MODE_LANGEVIN || mode == MODE_FORCES) {
                 if (mode == MODE_LANGEVIN) ss.ke2 = k;
                 ss.epot = e;
             } else {
@@ -489,10 +603,11 @@ __device__ __forceinline__ void finish(const KArgs<R> &a, double ke, double ep, 
     }
 }
 
-template<class R, bool E, int V> __global__ void __launch_bounds__(STEP_BS, (V & 2) ? 6 : 8) k_step_langevin(KArgs<R> a) {
+template<class R, bool E, int V> __global__ void __launch_bounds__(STEP_BS, STEP_MINB(R, V)) k_step_langevin(KArgs<R> a) {
     using T4 = typename Vec<R>::T4;
     __shared__ T4 sh[27];
     __shared__ FFDev<R> F;
+    __shared__ StageBuf<R> sb;
     stage_ff<R>(&F, a.ff);
     init_shift<R>(sh);
     const int cur = __ldcg(&a.S->cur), lp = __ldcg(&a.S->lp);
@@ -502,18 +617,24 @@ template<class R, bool E, int V> __global__ void __launch_bounds__(STEP_BS, (V &
     const SysDev &sd = a.sys[s];
     const T4 pi = a.pos[cur][i];
     prefetch_warp_list(a.nbr, i, a.cap, a.nnb[i]);
+    const bool stg = stage_warp<R>(a, i, cur, sb);
     const int w = wbits(pi.w);
     const int ty = w_type(w);
-    double ke = 0, ep = 0;
+    double ke = 0, ep = 0, vsx = 0, vsy = 0, vsz = 0;
     float md2 = 0.f;
     int flags = 0;
     if (ty != GHOST) {
         const T4 ni = a.nrm[cur][i];
         R3<R> f = {0, 0, 0}, t = {0, 0, 0};
         R e = 0;
-        particle_forces<R, E, V>(a, F, i, cur, lp, w, pi, ni, sd, a.ss[s], sh, f, t, e, flags);
+        forces_of<R, E, V>(stg, sb, a, F, i, cur, lp, w, pi, ni, sd, a.ss[s], sh, f, t, e, flags);
         const R dt = R(a.dt);
         T4 v = a.vel[lp][i], o = a.omg[lp][i];
+        if (a.zero_bulk && ty == 0) {  // zero_bulk_velocity on the lipids (src/zero_bulk_velocity.h:38-45)
+            v.x -= R(__ldcg(&a.ss[s].vcom[0]));
+            v.y -= R(__ldcg(&a.ss[s].vcom[1]));
+            v.z -= R(__ldcg(&a.ss[s].vcom[2]));
+        }
         // ROTATION: t <- n x t; o += dt t; n <- normalize(n + (o x n) dt)
         const R tx = ni.y * t.z - ni.z * t.y, ty_ = ni.z * t.x - ni.x * t.z, tz = ni.x * t.y - ni.y * t.x;
         o.x += dt * tx;
@@ -553,14 +674,20 @@ template<class R, bool E, int V> __global__ void __launch_bounds__(STEP_BS, (V &
         if (!isfinite(p.x + p.y + p.z + v.x + v.y + v.z)) flags |= ERRB_NAN;
         ke = double(F.mass[ty]) * (double(v.x) * double(v.x) + double(v.y) * double(v.y) + double(v.z) * double(v.z));
         ep = double(e);
+        if (ty == 0) {
+            vsx = double(v.x);
+            vsy = double(v.y);
+            vsz = double(v.z);
+        }
     }
-    finish<R>(a, ke, ep, md2, flags, MODE_LANGEVIN, 1);
+    finish<R>(a, ke, ep, md2, flags, MODE_LANGEVIN, 1, vsx, vsy, vsz);
 }
 
-template<class R, bool E, int V> __global__ void __launch_bounds__(STEP_BS, (V & 2) ? 6 : 8) k_nh_final(KArgs<R> a, int count_step) {
+template<class R, bool E, int V> __global__ void __launch_bounds__(STEP_BS, STEP_MINB(R, V)) k_nh_final(KArgs<R> a, int count_step) {
     using T4 = typename Vec<R>::T4;
     __shared__ T4 sh[27];
     __shared__ FFDev<R> F;
+    __shared__ StageBuf<R> sb;
     stage_ff<R>(&F, a.ff);
     init_shift<R>(sh);
     const int cur = __ldcg(&a.S->cur), lp = __ldcg(&a.S->lp);
@@ -569,6 +696,7 @@ template<class R, bool E, int V> __global__ void __launch_bounds__(STEP_BS, (V &
     const SysDev &sd = a.sys[s];
     const T4 pi = a.pos[cur][i];
     prefetch_warp_list(a.nbr, i, a.cap, a.nnb[i]);
+    const bool stg = stage_warp<R>(a, i, cur, sb);
     const int w = wbits(pi.w);
     const int ty = w_type(w);
     double ke = 0, ep = 0;
@@ -577,11 +705,16 @@ template<class R, bool E, int V> __global__ void __launch_bounds__(STEP_BS, (V &
         const T4 ni = a.nrm[cur][i];
         R3<R> f = {0, 0, 0}, t = {0, 0, 0};
         R e = 0;
-        particle_forces<R, E, V>(a, F, i, cur, lp, w, pi, ni, sd, a.ss[s], sh, f, t, e, flags);
+        forces_of<R, E, V>(stg, sb, a, F, i, cur, lp, w, pi, ni, sd, a.ss[s], sh, f, t, e, flags);
         const R dt = R(a.dt);
         const R zeta = R(__ldcg(&a.ss[s].zeta));
         const R im = F.inv_mass[ty];
         T4 v = a.vel[lp][i], o = a.omg[lp][i];
+        if (a.zero_bulk && count_step && ty == 0) {  // between the forces and the final half (src/openrbc.cpp:228)
+            v.x -= R(__ldcg(&a.ss[s].vcom[0]));
+            v.y -= R(__ldcg(&a.ss[s].vcom[1]));
+            v.z -= R(__ldcg(&a.ss[s].vcom[2]));
+        }
         T4 tq = v;
         tq.x = ni.y * t.z - ni.z * t.y;  // post_torque: t <- n x t
         tq.y = ni.z * t.x - ni.x * t.z;
@@ -616,7 +749,7 @@ template<class R> __global__ void __launch_bounds__(STEP_BS) k_nh_initial(KArgs<
     T4 p = a.pos[cur][i];
     const int w = wbits(p.w);
     const int ty = w_type(w);
-    double ke = 0;
+    double ke = 0, vsx = 0, vsy = 0, vsz = 0;
     float md2 = 0.f;
     int flags = 0;
     if (ty != GHOST) {
@@ -651,6 +784,11 @@ template<class R> __global__ void __launch_bounds__(STEP_BS) k_nh_initial(KArgs<
             }
         }
         ke = double(a.ff->mass[ty]) * (double(v.x) * double(v.x) + double(v.y) * double(v.y) + double(v.z) * double(v.z));
+        if (ty == 0) {
+            vsx = double(v.x);
+            vsy = double(v.y);
+            vsz = double(v.z);
+        }
         o.x += R(0.5) * dt * t.x;
         o.y += R(0.5) * dt * t.y;
         o.z += R(0.5) * dt * t.z;
@@ -671,13 +809,63 @@ template<class R> __global__ void __launch_bounds__(STEP_BS) k_nh_initial(KArgs<
         md2 = float(ddx * ddx + ddy * ddy + ddz * ddz);
         if (!isfinite(p.x + p.y + p.z)) flags |= ERRB_NAN;
     }
-    finish<R>(a, ke, 0.0, md2, flags, MODE_NH_INITIAL, 0);
+    finish<R>(a, ke, 0.0, md2, flags, MODE_NH_INITIAL, 0, vsx, vsy, vsz);
 }
 
-template<class R, bool E, int V> __global__ void __launch_bounds__(STEP_BS, (V & 2) ? 6 : 8) k_forces(KArgs<R> a) {
+/* Velocity sums of each system after the velocities were replaced (upload,
+ * set_state, assign_temperature): sum m v^2 and the mean lipid velocity; the
+ * step kernels keep both current afterwards. */
+template<class R> __global__ void __launch_bounds__(STEP_BS) k_vcom(KArgs<R> a) {
+    using T4 = typename Vec<R>::T4;
+    const int cur = __ldcg(&a.S->cur), lp = __ldcg(&a.S->lp);
+    const int i = blockIdx.x * STEP_BS + threadIdx.x;
+    double ke = 0, vsx = 0, vsy = 0, vsz = 0;
+    const int ty = w_type(wbits(a.pos[cur][i].w));
+    if (ty != GHOST) {
+        const T4 v = a.vel[lp][i];
+        ke = double(a.ff->mass[ty]) * (double(v.x) * double(v.x) + double(v.y) * double(v.y) + double(v.z) * double(v.z));
+        if (ty == 0) {
+            vsx = double(v.x);
+            vsy = double(v.y);
+            vsz = double(v.z);
+        }
+    }
+    finish<R>(a, ke, 0.0, 0.f, 0, MODE_VCOM, 0, vsx, vsy, vsz);
+}
+
+/* assign_temperature (src/assign_temperature.h:26-44, called at
+ * src/openrbc.cpp:160): v = sqrt(2 kT / m) g, g three unit Gaussians from
+ * Box-Muller on one Philox4x32-10 block keyed by the seed with counter
+ * (tag, 0x6B8B4567, 0x327B23C6, system), u = (word + 1/2) / 2^32.  The factor
+ * 2 of the reference is kept.  Computed in FP64, stored in R. */
+template<class R> __global__ void __launch_bounds__(256) k_assign_temperature(KArgs<R> a, double kT, uint64_t seed) {
+    using T4 = typename Vec<R>::T4;
+    const int cur = __ldcg(&a.S->cur), lp = __ldcg(&a.S->lp);
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.npad) return;
+    const int ty = w_type(wbits(a.pos[cur][i].w));
+    if (ty == GHOST) return;
+    const int s = a.blk_sys[i / SYS_PAD];
+    uint32_t o[4];
+    philox4(uint32_t(a.tag[lp][i]), 0x6B8B4567u, 0x327B23C6u, uint32_t(s), uint32_t(seed), uint32_t(seed >> 32), o);
+    double u[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) u[k] = (double(o[k]) + 0.5) * (1.0 / 4294967296.0);
+    const double r0 = sqrt(-2.0 * log(u[0])), r1 = sqrt(-2.0 * log(u[2]));
+    const double twopi = 6.283185307179586;
+    const double sc = sqrt(2.0 / double(a.ff->mass[ty]) * kT);
+    T4 v = a.vel[lp][i];
+    v.x = R(sc * r0 * cos(twopi * u[1]));
+    v.y = R(sc * r0 * sin(twopi * u[1]));
+    v.z = R(sc * r1 * cos(twopi * u[3]));
+    a.vel[lp][i] = v;
+}
+
+template<class R, bool E, int V> __global__ void __launch_bounds__(STEP_BS, STEP_MINB(R, V)) k_forces(KArgs<R> a) {
     using T4 = typename Vec<R>::T4;
     __shared__ T4 sh[27];
     __shared__ FFDev<R> F;
+    __shared__ StageBuf<R> sb;
     stage_ff<R>(&F, a.ff);
     init_shift<R>(sh);
     const int cur = __ldcg(&a.S->cur), lp = __ldcg(&a.S->lp);
@@ -686,6 +874,7 @@ template<class R, bool E, int V> __global__ void __launch_bounds__(STEP_BS, (V &
     const SysDev &sd = a.sys[s];
     const T4 pi = a.pos[cur][i];
     prefetch_warp_list(a.nbr, i, a.cap, a.nnb[i]);
+    const bool stg = stage_warp<R>(a, i, cur, sb);
     const int w = wbits(pi.w);
     double ep = 0;
     int flags = 0;
@@ -693,7 +882,7 @@ template<class R, bool E, int V> __global__ void __launch_bounds__(STEP_BS, (V &
         const T4 ni = a.nrm[cur][i];
         R3<R> f = {0, 0, 0}, t = {0, 0, 0};
         R e = 0;
-        particle_forces<R, E, V>(a, F, i, cur, lp, w, pi, ni, sd, a.ss[s], sh, f, t, e, flags);
+        forces_of<R, E, V>(stg, sb, a, F, i, cur, lp, w, pi, ni, sd, a.ss[s], sh, f, t, e, flags);
         T4 q = pi;
         q.x = f.x;
         q.y = f.y;
@@ -840,6 +1029,12 @@ template<class R> void launch_forces(const KArgs<R> &a, cudaStream_t st) {
 template<class R> void launch_mesh(const KArgs<R> &a, cudaStream_t st) {
     if (a.nmblk > 0) k_mesh<R><<<a.nmblk, 256, 0, st>>>(a);
 }
+template<class R> void launch_vcom(const KArgs<R> &a, cudaStream_t st) {
+    k_vcom<R><<<a.nblk, STEP_BS, 0, st>>>(a);
+}
+template<class R> void launch_assign_temperature(const KArgs<R> &a, double kT, uint64_t seed, cudaStream_t st) {
+    k_assign_temperature<R><<<(a.npad + 255) / 256, 256, 0, st>>>(a, kT, seed);
+}
 
 #define ORBC_INST(R)                                                                   \
     template void launch_step_langevin<R>(const KArgs<R> &, cudaStream_t, bool);      \
@@ -847,6 +1042,8 @@ template<class R> void launch_mesh(const KArgs<R> &a, cudaStream_t st) {
     template void launch_nh_prologue<R>(const KArgs<R> &, cudaStream_t);              \
     template void launch_nh_initial<R>(const KArgs<R> &, cudaStream_t);               \
     template void launch_forces<R>(const KArgs<R> &, cudaStream_t);                   \
+    template void launch_vcom<R>(const KArgs<R> &, cudaStream_t);                     \
+    template void launch_assign_temperature<R>(const KArgs<R> &, double, uint64_t, cudaStream_t); \
     template void launch_mesh<R>(const KArgs<R> &, cudaStream_t);
 ORBC_INST(float)
 ORBC_INST(double)

@@ -35,7 +35,7 @@ class Simulation:
                  energy: bool = False, box: Optional[Sequence[Sequence[float]]] = None,
                  periodic: Sequence[int] = (0, 0, 0), bond_table: Optional[dict] = None,
                  max_neighbors: int = 0, rebuild_every: Optional[int] = None, bounce: bool = True,
-                 mesh_constraint: Optional[dict] = None, kernel_variant: int = 0):
+                 mesh_constraint: Optional[dict] = None, kernel_variant: int = 0, zero_bulk: bool = False):
         self.param = param or RTParameter(init="lipid")
         p = N.Params()
         L = N.lib()
@@ -52,6 +52,7 @@ class Simulation:
         p.use_graph = 1 if use_graph else 0
         p.energy = 1 if energy else 0
         p.kernel_variant = int(kernel_variant)
+        p.zero_bulk = 1 if zero_bulk else 0
         bx = box if box is not None else prm.box
         for d in range(3):
             p.lo[d], p.hi[d] = float(bx[d][0]), float(bx[d][1])
@@ -175,6 +176,24 @@ class Simulation:
     def rebuild(self):
         self._check(N.lib().orbc_gpu_rebuild(self.h))
 
+    def assign_temperature(self, kBT: Optional[float] = None, seed: Optional[int] = None, amplify: float = 1.0):
+        """integrate(assign_temperature(param, amplify), lipid, protein)
+        (src/assign_temperature.h:26-44, src/openrbc.cpp:160) on the device:
+        v = sqrt(2 kBT amplify / m) g.  Defaults: the parameter's kBT and rseed."""
+        kT = (self.param.kBT if kBT is None else float(kBT)) * float(amplify)
+        sd = (int(self.param.rseed) if seed is None else int(seed)) & 0xFFFFFFFFFFFFFFFF
+        self._check(N.lib().orbc_gpu_assign_temperature(self.h, kT, sd))
+
+    def rdf(self, sys: int = 0, type_a: int = -1, type_b: int = -1, dr: float = 0.1, nbins: int = 10000,
+            rcut: float = 0.0):
+        """Pair-distance histogram of one system (orbc_gpu_rdf; src/rdf.h:26-81).
+        Returns (counts[nbins] as uint64, dropped pair count)."""
+        counts = np.zeros(int(nbins), np.uint64)
+        dropped = C.c_int64()
+        self._check(N.lib().orbc_gpu_rdf(self.h, int(sys), int(type_a), int(type_b), float(dr), int(nbins),
+                                         float(rcut), counts.ctypes.data, C.byref(dropped)))
+        return counts, dropped.value
+
     def profile(self, nsteps: int = 20) -> dict:
         """Per-kernel CUDA-event times over nsteps un-captured steps (orbc_gpu_profile)."""
         pr = N.Profile()
@@ -195,6 +214,25 @@ class Simulation:
         launches = C.c_int64()
         self._check(N.lib().orbc_gpu_last_timing(self.h, C.byref(ms), C.byref(launches)))
         return ms.value, launches.value
+
+
+def rdf_table(counts, dr: float = 0.1):
+    """The reference's rdf.txt rows (src/rdf.h:39-43): r = dr i and
+    counts[i] / (4 * 3.14 * r^2 * dr), including its literal 3.14 and the
+    infinite first row."""
+    c = np.asarray(counts, np.float64)
+    r = dr * np.arange(len(c))
+    with np.errstate(divide="ignore", invalid="ignore"):
+        g = c / (4.0 * 3.14 * r * r * dr)
+    return r, g
+
+
+def write_rdf(path, counts, dr: float = 0.1):
+    """Write rdf.txt as the reference does: one `r value` line per bin."""
+    r, g = rdf_table(counts, dr)
+    with open(path, "w") as f:
+        for a, b in zip(r, g):
+            f.write(f"{a:g} {b:g}\n")
 
 
 def morton_encode(points, bsize=(2000.0, 2000.0, 2000.0)) -> np.ndarray:

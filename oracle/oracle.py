@@ -53,6 +53,7 @@ class OrcSystemC(C.Structure):
         ("dt", C.c_double), ("kBT", C.c_double), ("eta", C.c_double),
         ("zeta", C.c_double), ("Q", C.c_double),
         ("seed", C.c_uint64), ("step", C.c_int64), ("sys", C.c_int), ("bounce", C.c_int),
+        ("zero_bulk", C.c_int),
         ("kv", C.c_double), ("V0", C.c_double), ("ka", C.c_double), ("A0", C.c_double),
         ("bstyle", C.c_int * MAX_BOND_TYPES), ("bK", C.c_double * MAX_BOND_TYPES),
         ("br0", C.c_double * MAX_BOND_TYPES), ("bR", C.c_double * MAX_BOND_TYPES),
@@ -99,6 +100,7 @@ class State:
     step: int = 0
     sys: int = 0
     bounce: int = 0
+    zero_bulk: int = 0
     kv: float = 0.0
     V0: float = 0.0
     ka: float = 0.0
@@ -154,6 +156,7 @@ class State:
         for name in ("dt", "kBT", "eta", "zeta", "Q", "kv", "V0", "ka", "A0"):
             setattr(s, name, float(getattr(self, name)))
         s.seed, s.step, s.sys, s.bounce = int(self.seed), int(self.step), int(self.sys), int(self.bounce)
+        s.zero_bulk = int(self.zero_bulk)
         for k in range(MAX_BOND_TYPES):
             s.bstyle[k] = int(self.bstyle[k])
             s.bK[k] = float(self.bK[k])
@@ -185,6 +188,7 @@ def lib(fast: bool = False):
             L.orc_morton_order.argtypes = [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]
             L.orc_noise.argtypes = [C.c_uint64, C.c_int64, C.c_int, C.c_int, C.c_void_p]
             L.orc_ff_tables.argtypes = [C.c_void_p] * 4
+            L.orc_assign_temperature.argtypes = [P(OrcSystemC), C.c_double, C.c_uint64]
             L.orc_set_threads.argtypes = [C.c_int]
             L.orc_get_threads.restype = C.c_int
             if fast:
@@ -248,6 +252,29 @@ def nh_steps(st: State, nsteps: int) -> dict:
     lib().orc_step_nh_f64(C.byref(c), int(nsteps), C.byref(th))
     _sync_back(st, c)
     return _thermo(th)
+
+
+def assign_temperature(st: State, kT: float, seed: int) -> None:
+    lib().orc_assign_temperature(C.byref(st._c()), float(kT), int(seed))
+
+
+def rdf(x, type, type_a=-1, type_b=-1, dr=0.1, nbins=10000, rcut=0.0, centre=(0.0, 0.0, 0.0),
+        L=(0.0, 0.0, 0.0), single=False):
+    """Pair-distance histogram (orc_rdf; src/rdf.h:26-81).  Returns
+    (counts, counted, dropped)."""
+    x = np.ascontiguousarray(x, np.float64).reshape(-1, 3)
+    t = np.ascontiguousarray(type, np.int32).reshape(-1)
+    c = np.ascontiguousarray(centre, np.float64)
+    Lb = np.ascontiguousarray(L, np.float64)
+    counts = np.zeros(int(nbins), np.uint64)
+    dropped = C.c_int64()
+    L_ = lib()
+    L_.orc_rdf.restype = C.c_int64
+    n = L_.orc_rdf(x.ctypes.data_as(C.c_void_p), t.ctypes.data_as(C.c_void_p), C.c_int64(len(x)), int(type_a),
+                   int(type_b), C.c_double(dr), int(nbins), C.c_double(rcut), c.ctypes.data_as(C.c_void_p),
+                   Lb.ctypes.data_as(C.c_void_p), 1 if single else 0, counts.ctypes.data_as(C.c_void_p),
+                   C.byref(dropped))
+    return counts, int(n), dropped.value
 
 
 def thermo(st: State) -> dict:

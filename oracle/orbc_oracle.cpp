@@ -683,6 +683,23 @@ template<class FN> double chunked_sum(int64_t n, FN &&term) {
     return s;
 }
 
+/* zero_bulk_velocity (src/zero_bulk_velocity.h:29-56) applied to the lipids
+ * as the reference's call site does (src/openrbc.cpp:228): v -= mean lipid v. */
+void zero_bulk(orc_system *s) {
+    double sum[3] = {0, 0, 0};
+    int64_t nl = 0;
+    for (int64_t i = 0; i < s->n; ++i)
+        if (s->type[i] == 0) {
+            for (int d = 0; d < 3; ++d) sum[d] += s->v[3 * i + d];
+            ++nl;
+        }
+    if (!nl) return;
+    for (int d = 0; d < 3; ++d) sum[d] /= double(nl);
+    for (int64_t i = 0; i < s->n; ++i)
+        if (s->type[i] == 0)
+            for (int d = 0; d < 3; ++d) s->v[3 * i + d] -= sum[d];
+}
+
 /* src/integrate_langevin.h:105-146, per particle, in R. */
 template<class R> int langevin_impl(orc_system *s, int nsteps, orc_thermo *th) {
     const int64_t n = s->n;
@@ -697,6 +714,7 @@ template<class R> int langevin_impl(orc_system *s, int nsteps, orc_thermo *th) {
     const R dt_over_m = dt / R(1);
     for (int st = 0; st < nsteps; ++st) {
         forces_impl<R>(s, f3.data(), t3.data(), nullptr, th);
+        if (s->zero_bulk) zero_bulk(s);
         const int64_t step = s->step;
 #pragma omp parallel for schedule(static)
         for (int64_t i = 0; i < n; ++i) {
@@ -850,6 +868,7 @@ int orc_step_nh_f64(orc_system *s, int nsteps, orc_thermo *th) {
     for (int k = 0; k < nsteps; ++k) {
         nh_initial(s);
         forces_impl<double>(s, s->f, s->t, nullptr, th);
+        if (s->zero_bulk) zero_bulk(s);  // src/openrbc.cpp:228, between the forces and the final half
         nh_final(s);
         s->step++;
     }
@@ -923,6 +942,63 @@ int64_t orc_pairs(const orc_system *s, const double *rcut2, int32_t *pairs, int6
     return cnt;
 }
 
+/* src/rdf.h:26-47 (all pairs, dr-wide bins, `static_cast<int>(dx / dr)`) and
+ * :49-81 (type filter, cutoff). */
+}  // extern "C"
+
+template<class T>
+static int64_t rdf_impl(const double *x3, const int *type, int64_t n, int ta, int tb, double dr_, int nbins,
+                        double rcut_, const double *c3, const double *L3, uint64_t *counts, int64_t *dropped) {
+    std::vector<T> x(static_cast<size_t>(3 * n));
+    for (int64_t i = 0; i < n; ++i)
+        for (int d = 0; d < 3; ++d) x[size_t(3 * i + d)] = T(x3[3 * i + d] - c3[d]);
+    const T dr = T(dr_), rcut = T(rcut_);
+    const T L[3] = {T(L3 ? L3[0] : 0), T(L3 ? L3[1] : 0), T(L3 ? L3[2] : 0)};
+    auto match = [&](int t, int want) { return want < 0 || t == want; };
+    int64_t counted = 0, drop = 0;
+    std::vector<uint64_t> h(static_cast<size_t>(nbins), 0);
+    for (int64_t i = 0; i < n; ++i)
+        for (int64_t j = i + 1; j < n; ++j) {
+            const int ti = type[i], tj = type[j];
+            if (!((match(ti, ta) && match(tj, tb)) || (match(ti, tb) && match(tj, ta)))) continue;
+            T dd[3];
+            for (int d = 0; d < 3; ++d) {
+                T q = x[size_t(3 * i + d)] - x[size_t(3 * j + d)];
+                if (L[d] > T(0)) {
+                    const T m = std::rint(q / L[d]);
+                    const T sh = L[d] * m;
+                    q = q - sh;
+                }
+                dd[d] = q;
+            }
+            const T a0 = dd[0] * dd[0], a1 = dd[1] * dd[1], a2 = dd[2] * dd[2];
+            const T r = std::sqrt((a0 + a1) + a2);
+            if (rcut > T(0) && !(r < rcut)) {
+                ++drop;
+                continue;
+            }
+            const T q = r / dr;
+            const int64_t b = q < T(2147483647.0) ? int64_t(int(q)) : int64_t(2147483647);
+            if (b >= nbins) {
+                ++drop;
+                continue;
+            }
+            ++h[size_t(b)];
+            ++counted;
+        }
+    for (int k = 0; k < nbins; ++k) counts[k] = h[size_t(k)];
+    if (dropped) *dropped = drop;
+    return counted;
+}
+
+extern "C" {
+
+int64_t orc_rdf(const double *x3, const int *type, int64_t n, int type_a, int type_b, double dr, int nbins,
+                double rcut, const double *centre3, const double *L3, int single, uint64_t *counts, int64_t *dropped) {
+    return single ? rdf_impl<float>(x3, type, n, type_a, type_b, dr, nbins, rcut, centre3, L3, counts, dropped)
+                  : rdf_impl<double>(x3, type, n, type_a, type_b, dr, nbins, rcut, centre3, L3, counts, dropped);
+}
+
 /* src/reorder_morton.h:25-42 */
 static inline uint32_t bit_space3(uint32_t x) {
     x = (x | (x << 12)) & 0x00FC003Fu;
@@ -953,6 +1029,24 @@ void orc_morton_order(const double *p3, int64_t n, const double *bsize, int32_t 
 }
 
 void orc_noise(uint64_t seed, int64_t step, int tag, int sys, double r[3]) { noise3(seed, step, tag, sys, r); }
+
+void orc_assign_temperature(orc_system *s, double kT, uint64_t seed) {
+    const FF<double> &F = ff<double>();
+    for (int64_t i = 0; i < s->n; ++i) {
+        const uint32_t ctr[4] = {uint32_t(s->tag[i]), 0x6B8B4567u, 0x327B23C6u, uint32_t(s->sys)};
+        const uint32_t key[2] = {uint32_t(seed), uint32_t(seed >> 32)};
+        uint32_t o[4];
+        philox(ctr, key, o);
+        // two Box-Muller pairs from four 32-bit words -> three Gaussians
+        double u[4];
+        for (int k = 0; k < 4; ++k) u[k] = (double(o[k]) + 0.5) * (1.0 / 4294967296.0);
+        const double r0 = std::sqrt(-2.0 * std::log(u[0])), r1 = std::sqrt(-2.0 * std::log(u[2]));
+        const double g[3] = {r0 * std::cos(2.0 * M_PI * u[1]), r0 * std::sin(2.0 * M_PI * u[1]),
+                             r1 * std::cos(2.0 * M_PI * u[3])};
+        const double sc = std::sqrt(2.0 / F.mass[s->type[i]] * kT);
+        for (int d = 0; d < 3; ++d) s->v[3 * i + d] = sc * g[d];
+    }
+}
 
 void orc_ff_tables(double *mass6, double *radius6, double *cutsq36, double *lj_cutsq36) {
     const FF<double> &F = ff<double>();

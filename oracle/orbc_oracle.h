@@ -49,6 +49,8 @@ typedef struct {
     int64_t step;           /* step counter (RNG counter word)                  */
     int sys;                /* system id (RNG counter word) for batched runs    */
     int bounce;             /* reflective walls at lo/hi (src/integrate_nh.h:124-144) */
+    int zero_bulk;          /* subtract the mean lipid velocity before integrating
+                               (src/zero_bulk_velocity.h:29-56, src/openrbc.cpp:228) */
     /* global mesh constraints: F = -k (Q - Q0)/Q0 dQ/dx, Q = V or A */
     double kv, V0, ka, A0;
     /* bond-type table */
@@ -91,6 +93,24 @@ int orc_step_langevin_f32(orc_system *s, int nsteps, orc_thermo *th);
  * (src/openrbc.cpp:189-242).  zeta in s is updated. */
 int orc_nh_prologue_f64(orc_system *s, orc_thermo *th);
 int orc_step_nh_f64(orc_system *s, int nsteps, orc_thermo *th);
+
+/* assign_temperature (src/assign_temperature.h:26-44): v_d = sqrt(2 kT / m) g
+ * with g a unit Gaussian (Box-Muller on Philox4x32-10 keyed by seed and tag;
+ * the reference's factor 2 is kept). */
+void orc_assign_temperature(orc_system *s, double kT, uint64_t seed);
+
+/* rdf / rdf_1peak_r (src/rdf.h:26-81): histogram of pair distances
+ * r = |x_i - x_j| over all unordered pairs i < j of the n points x3 whose
+ * types match (type_a, type_b) in either order (-1 matches any type),
+ * bin = (int)(r / dr), pairs with r >= rcut (rcut > 0) or bin >= nbins
+ * dropped and counted in *dropped.  Coordinates are taken relative to
+ * centre3; periodic axes (L[d] > 0) use the minimum image
+ * d - L rint(d / L).  single != 0 evaluates everything in FP32 (the
+ * reference's default `real`), else FP64; each operation is rounded once
+ * (no contraction), so a GPU that performs the same operations produces the
+ * same counts.  Returns the number of counted pairs. */
+int64_t orc_rdf(const double *x3, const int *type, int64_t n, int type_a, int type_b, double dr, int nbins,
+                double rcut, const double *centre3, const double *L3, int single, uint64_t *counts, int64_t *dropped);
 
 /* Temperature, area and volume of the current state. */
 int orc_thermo_f64(const orc_system *s, orc_thermo *th);

@@ -239,9 +239,18 @@ def test_binning_and_sort_bit_exact():
     ref = np.where(np.array(per)[None, :] == 1, cu, cc)
     off = x - (lo + (ref + 0.5) * Lc)
     assert np.array_equal(c["offset"], off)
-    # slots are the stable order by (linear cell id, upload index) within the system
-    lin = cc[:, 0] + nc[0] * (cc[:, 1] + nc[1] * cc[:, 2])
-    order = np.lexsort((np.arange(len(lin)), lin))
+    # slots are the stable order by (cell id, upload index) within the system; the
+    # cell id walks 4 x 4 x 4 tiles of cells row-major, Morton order inside a tile
+    nt = (nc + 3) // 4
+    t = cc // 4
+    r = cc % 4
+
+    def spread2(v):
+        return (v & 1) | ((v & 2) << 2)
+
+    cid = (t[:, 0] + nt[0] * (t[:, 1] + nt[1] * t[:, 2])) * 64 + (spread2(r[:, 0]) | (spread2(r[:, 1]) << 1) |
+                                                                  (spread2(r[:, 2]) << 2))
+    order = np.lexsort((np.arange(len(cid)), cid))
     assert np.array_equal(np.argsort(c["slot"]), order)
 
 
