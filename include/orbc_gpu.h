@@ -47,7 +47,8 @@ enum {
     ORBC_ERR_BOND = 6,         /* FENE / WLC bond stretched beyond its maximum            */
     ORBC_ERR_STATE = 7,        /* call out of order (e.g. step before upload)             */
     ORBC_ERR_NOMEM = 8,        /* device allocation failed                                */
-    ORBC_ERR_NODEV = 9         /* no CUDA device                                          */
+    ORBC_ERR_NODEV = 9,        /* no CUDA device                                          */
+    ORBC_ERR_IO = 10           /* a trajectory or checkpoint file could not be read / written */
 };
 
 enum { ORBC_PREC_FP64 = 0, ORBC_PREC_MIXED = 1 };
@@ -83,9 +84,11 @@ typedef struct {
     double bond_K[ORBC_MAX_BOND_TYPES];
     double bond_r0[ORBC_MAX_BOND_TYPES];
     double bond_R[ORBC_MAX_BOND_TYPES];
-    /* force-kernel form 0..3: bit 0 = software-pipelined neighbour pass
+    /* kernel forms 0..7: bit 0 = software-pipelined neighbour pass
        (else 2-way unrolled), bit 1 = non-lipid pair path inlined (else
-       called); orbc_gpu_autotune picks it per workload */
+       called), bit 2 = neighbour list built by per-particle 27-cell sweeps
+       (else one sweep per warp of its cells' neighbourhood);
+       orbc_gpu_autotune picks it per workload */
     int kernel_variant;
     /* 1: remove each system's mean lipid velocity between the force
        evaluation and the integrator every step, as the disabled call
@@ -176,6 +179,51 @@ int orbc_gpu_cells(orbc_handle *h, int sys, double *lo3, double *lc3, int *nc3, 
 
 /* Force a neighbour-list rebuild now (sort + bins + list). */
 int orbc_gpu_rebuild(orbc_handle *h);
+
+/* Trajectory frame in the reference's .orbc layout (save_frame,
+ * src/trajectory.h:26-105), so its reader and orbc-util read it:
+ * FRAMEBEG int32 nstep, NATOM uint64 N, IDENTITY N x (int32 tag, int32 type),
+ * then per `fields` bit (the reference's DumpField, src/runtime_parameter.h:
+ * 30-36) POSITION (1), VELOCITY (8), ROTATION (2) as N x 3 `real`, VORONOI
+ * (4) as N x int32 (the particle's grid-cell id here: there is no Voronoi
+ * tessellation), FORCE (16) as N x 3 `real` (evaluated at the current state),
+ * then FRAMEEND.  Particles are written lipids first, then proteins, each in
+ * upload order, as the reference's save_frame(lipid, protein) does.
+ * real_bytes = 4 matches the reference's default build, 8 its FP64 build.
+ * append = 0 truncates the file.  async = 1 returns as soon as the frame is
+ * queued: the device gathers it into a staging buffer, a second stream copies
+ * it to one of two pinned host buffers and a writer thread writes it while
+ * the caller goes on stepping (a third frame waits for a free buffer);
+ * orbc_gpu_flush waits for the queue and reports write errors.  async = 0
+ * writes before returning. */
+#define ORBC_DUMP_POSITION 1
+#define ORBC_DUMP_ROTATION 2
+#define ORBC_DUMP_VORONOI 4
+#define ORBC_DUMP_VELOCITY 8
+#define ORBC_DUMP_FORCE 16
+int orbc_gpu_save_frame(orbc_handle *h, const char *path, int append, int nstep, int fields, int real_bytes,
+                        int async);
+int orbc_gpu_flush(orbc_handle *h);
+
+/* Checkpoint / restart (no counterpart in the reference, whose trajectory
+ * lacks angular velocities, the thermostat and the RNG state): positions,
+ * orientations, velocities and angular velocities (FP64, upload order), the
+ * step counter that keys the noise, the RNG seed, each system's Nose-Hoover
+ * zeta and the carried Nose-Hoover forces and torques.  load_checkpoint needs
+ * a handle holding the same topology (orbc_gpu_upload of the same particles,
+ * in the same order); the run then continues where the saved one was. */
+int orbc_gpu_save_checkpoint(orbc_handle *h, const char *path);
+int orbc_gpu_load_checkpoint(orbc_handle *h, const char *path);
+
+/* Energy minimisation (the loop of src/openrbc.cpp:88-146): nsteps times
+ * forces, post_torque t <- n x t (src/integrate_nh.h:146-154), the
+ * step-limited steepest-descent move per particle (dx = f / m, dn = t x n,
+ * h = (|dx| > dr_max || |dn| > dn_max) ? min(dr_max / |dx|, dn_max / |dn|)
+ * : params.dt; x += f h / m; n <- normalize(n + dn h), :113-130) and
+ * bounce_back at the box walls on open axes when params.bounce (:132).  The
+ * reference's defaults are nsteps = 1000 and dr_max = dn_max = 0.05
+ * (src/runtime_parameter.h:56-58).  The step counter does not advance. */
+int orbc_gpu_minimize(orbc_handle *h, int nsteps, double dr_max, double dn_max, orbc_thermo *out);
 
 /* assign_temperature (src/assign_temperature.h:26-44, applied to lipids and
  * proteins at src/openrbc.cpp:160): every particle's velocity becomes

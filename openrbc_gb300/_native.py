@@ -14,7 +14,8 @@ LIB_PATH = os.path.join(PKG, "liborbc_gpu.so")
 
 ORBC_OK = 0
 ERRORS = {1: "ORBC_ERR_ARG", 2: "ORBC_ERR_CUDA", 3: "ORBC_ERR_NBR_OVERFLOW", 4: "ORBC_ERR_NAN",
-          5: "ORBC_ERR_GRID", 6: "ORBC_ERR_BOND", 7: "ORBC_ERR_STATE", 8: "ORBC_ERR_NOMEM", 9: "ORBC_ERR_NODEV"}
+          5: "ORBC_ERR_GRID", 6: "ORBC_ERR_BOND", 7: "ORBC_ERR_STATE", 8: "ORBC_ERR_NOMEM", 9: "ORBC_ERR_NODEV",
+          10: "ORBC_ERR_IO"}
 PREC_FP64, PREC_MIXED = 0, 1
 INT_LANGEVIN, INT_NOSE_HOOVER = 0, 1
 BOND_HARMONIC, BOND_FENE, BOND_WLC_POW = 0, 1, 2
@@ -28,7 +29,8 @@ EXPORTS = [
     "orbc_gpu_neighbors", "orbc_gpu_cells", "orbc_gpu_rebuild", "orbc_gpu_last_timing",
     "orbc_gpu_morton_encode", "orbc_gpu_morton_order", "orbc_gpu_destroy", "orbc_gpu_error",
     "orbc_gpu_version", "orbc_gpu_profile", "orbc_gpu_morton_order_noalloc", "orbc_gpu_autotune",
-    "orbc_gpu_assign_temperature", "orbc_gpu_rdf",
+    "orbc_gpu_assign_temperature", "orbc_gpu_rdf", "orbc_gpu_minimize", "orbc_gpu_save_frame", "orbc_gpu_flush",
+    "orbc_gpu_save_checkpoint", "orbc_gpu_load_checkpoint",
     "orbc_gen_lattice", "orbc_gen_rbc_counts", "orbc_gen_rbc", "orbc_gen_vesicle_sizes", "orbc_gen_vesicle",
 ]
 
@@ -119,6 +121,11 @@ def lib():
         L.orbc_gpu_rebuild.argtypes = [H]
         L.orbc_gpu_assign_temperature.argtypes = [H, d, C.c_uint64]
         L.orbc_gpu_rdf.argtypes = [H, i32, i32, i32, d, i32, d, vp, P(i64)]
+        L.orbc_gpu_minimize.argtypes = [H, i32, d, d, P(Thermo)]
+        L.orbc_gpu_save_frame.argtypes = [H, C.c_char_p, i32, i32, i32, i32, i32]
+        L.orbc_gpu_flush.argtypes = [H]
+        L.orbc_gpu_save_checkpoint.argtypes = [H, C.c_char_p]
+        L.orbc_gpu_load_checkpoint.argtypes = [H, C.c_char_p]
         L.orbc_gpu_last_timing.argtypes = [H, P(d), P(i64)]
         L.orbc_gpu_morton_encode.argtypes = [vp, i64, vp, vp]
         L.orbc_gpu_morton_order.argtypes = [vp, i64, vp, vp]

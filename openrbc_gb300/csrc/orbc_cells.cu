@@ -281,15 +281,13 @@ template<class R> __global__ void __launch_bounds__(256) k_ranges_gather(KArgs<R
 template<class R> __global__ void __launch_bounds__(128) k_nlist(KArgs<R> a, int gated) {
     using T4 = typename Vec<R>::T4;
     if (gated && !__ldcg(&a.S->rebuild)) return;
-    constexpr int CAND = sizeof(T4) == 16 ? 256 : 160;  // staged candidates per warp
+    constexpr int CAND = sizeof(T4) == 16 ? 384 : 192;  // staged candidates per warp and pass
     constexpr int NLW = 4;                                // warps per block
-    constexpr int NLBOX = 128;                            // largest box (cells) swept warp-wide
     __shared__ float rl2s[256], ri2s[256];
     __shared__ T4 s_pos[NLW][CAND];
-    __shared__ int2 s_jk[NLW][CAND];
-    __shared__ int s_off[NLW][NLBOX + 1], s_beg[NLW][NLBOX];
-    __shared__ unsigned char s_need[NLW][NLBOX];
-    constexpr bool STG = sizeof(T4) == 16;  // warp staging in the mixed-precision step kernels
+    __shared__ int s_j[NLW][CAND];
+    __shared__ unsigned char s_code[NLW][CAND];           // shift code of the candidate's cell (0..26)
+    __shared__ int s_off[NLW][28], s_beg[NLW][27];
     const int warp = threadIdx.x >> 5;
     for (int k = threadIdx.x; k < 256; k += blockDim.x) {
         rl2s[k] = __ldg(&a.ff->rlist2[k]);
@@ -301,6 +299,7 @@ template<class R> __global__ void __launch_bounds__(128) k_nlist(KArgs<R> a, int
     int maxc = 0;
     // n is a multiple of the block size, so whole warps stay in the loop together
     const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const T4 p = a.pos[cur][i];
         const int ty = w_type(wbits(p.w));
@@ -312,15 +311,18 @@ template<class R> __global__ void __launch_bounds__(128) k_nlist(KArgs<R> a, int
         // Entries inside the pair's interaction range fill rows 0, 1, ... of
         // this slot's column; skin-shell entries fill rows cap-1, cap-2, ...
         int nin = 0, nout = 0, total = 0;
+        // x_i - x_j = (o_i - o_j) - d * Lc, each operation rounded once
+        auto dist2 = [&](const T4 &pi, const T4 &q, int dx, int dy, int dz) {
+            const R ex = add_rn(sub_rn(pi.x, q.x), mul_rn(R(-dx), L[0]));
+            const R ey = add_rn(sub_rn(pi.y, q.y), mul_rn(R(-dy), L[1]));
+            const R ez = add_rn(sub_rn(pi.z, q.z), mul_rn(R(-dz), L[2]));
+            return add_rn(add_rn(mul_rn(ex, ex), mul_rn(ey, ey)), mul_rn(ez, ez));
+        };
         auto test = [&](int j, const T4 &q, int dx, int dy, int dz) {
             const int tj = w_type(wbits(q.w));
             const float rl2 = rl2s[ty * 16 + tj];
             if (!(rl2 > 0.f)) return;
-            // x_i - x_j = (o_i - o_j) - d * Lc
-            const R ex = add_rn(sub_rn(p.x, q.x), mul_rn(R(-dx), L[0]));
-            const R ey = add_rn(sub_rn(p.y, q.y), mul_rn(R(-dy), L[1]));
-            const R ez = add_rn(sub_rn(p.z, q.z), mul_rn(R(-dz), L[2]));
-            const R r2 = add_rn(add_rn(mul_rn(ex, ex), mul_rn(ey, ey)), mul_rn(ez, ez));
+            const R r2 = dist2(p, q, dx, dy, dz);
             if (r2 < R(rl2)) {
                 const uint32_t ent = uint32_t(j) | (uint32_t((dx + 1) + 3 * (dy + 1) + 9 * (dz + 1)) << NB_SHIFT);
                 if (nin + nout < a.cap) {
@@ -332,52 +334,30 @@ template<class R> __global__ void __launch_bounds__(128) k_nlist(KArgs<R> a, int
                 ++total;
             }
         };
-        // Bounding box of the warp's cells.  Consecutive slots sit in a few
-        // neighbouring cells (cell ids follow tiles), so one sweep of the cells
-        // of the box (grown by one cell) that some lane's 27-cell neighbourhood
-        // covers, with every lane testing every candidate, replaces 32
-        // diverging 27-cell sweeps.  The ranges of those cells are fetched one
-        // per lane and scanned into candidate offsets; the candidates are then
-        // staged in shared memory (CAND at a time, all loads in flight
-        // together) and every lane reads them as broadcasts.  A wide box falls
-        // back to per-lane sweeps.  When the candidates form at most STG_RMAX
-        // contiguous slot ranges and number at most STG_CAND, the warp's
-        // entries hold the candidate's local index and the ranges go to
-        // wmeta, so the step kernels can copy the candidates to shared memory
-        // and read them there.
-        bool staged = false;
-        int nranges = 0, total_c = 0;
-        const bool any_real = __any_sync(0xffffffffu, real);
-        int lo[3], hi[3], vol = any_real ? 1 : 0;
-#pragma unroll
-        for (int d = 0; d < 3; ++d) {
-            // cells are < 2048 per axis; ghost lanes get neutral bounds
-            lo[d] = __reduce_min_sync(0xffffffffu, real ? cc[d] : 4096) - 1;
-            hi[d] = __reduce_max_sync(0xffffffffu, real ? cc[d] : -4096) + 1;
-            vol *= max(hi[d] - lo[d] + 1, 0);
-        }
-        if (vol > 0 && vol <= NLBOX) {
-            const int bx_n = hi[0] - lo[0] + 1, by_n = hi[1] - lo[1] + 1;
+        // Form 0 (warp sweep): consecutive slots sit in a few neighbouring
+        // cells (cell ids follow tiles).  For each distinct cell of the warp,
+        // 27 lanes fetch the ranges of its 27 neighbour cells, a warp scan
+        // turns them into offsets and the candidates are staged in shared
+        // memory (CAND per pass, all loads issued together); then for each
+        // particle in that cell the 32 lanes test 32 candidates at a time and
+        // accepted entries are placed by ballot and prefix count.  Form 1
+        // (per-lane sweep): every lane walks its own 27 cells.
+        bool swept = false;
+        if (!a.nlist_lane) {
+            swept = true;
+            const int kme = cc[0] | (cc[1] << 11) | (cc[2] << 22);
             int *off = s_off[warp];
             int *beg = s_beg[warp];
-            unsigned char *need = s_need[warp];
-            // this lane's cell relative to the box corner (inside [1, n-2] per axis)
-            const int rx0 = cc[0] - lo[0], ry0 = cc[1] - lo[1], rz0 = cc[2] - lo[2];
-            for (int k = lane; k < vol; k += 32) need[k] = 0;
-            __syncwarp();
-            if (real)
-                for (int dz = -1; dz <= 1; ++dz)
-                    for (int dy = -1; dy <= 1; ++dy)
-                        for (int dx = -1; dx <= 1; ++dx)
-                            need[(rx0 + dx) + bx_n * ((ry0 + dy) + by_n * (rz0 + dz))] = 1;
-            __syncwarp();
-            int2 *meta = a.wmeta + int64_t(i >> 5) * 32;
-            int running = 0, carry_end = -1;
-            for (int base = 0; base < vol; base += 32) {
+            unsigned todo = __ballot_sync(0xffffffffu, real);
+            while (todo) {
+                // the lanes in one cell share its candidates
+                const int kd = __shfl_sync(0xffffffffu, kme, __ffs(todo) - 1);
+                const unsigned grp = __ballot_sync(0xffffffffu, real && kme == kd);
+                todo &= ~grp;
+                const int xd = kd & 2047, yd = (kd >> 11) & 2047, zd = (kd >> 22) & 1023;
                 int2 rg = make_int2(0, 0);
-                const int cidx = base + lane;
-                if (cidx < vol && need[cidx]) {
-                    int x = lo[0] + cidx % bx_n, y = lo[1] + (cidx / bx_n) % by_n, z = lo[2] + cidx / (bx_n * by_n);
+                if (lane < 27) {
+                    int x = xd + lane % 3 - 1, y = yd + (lane / 3) % 3 - 1, z = zd + lane / 9 - 1;
                     bool ok = true;
                     if (sd.per[0]) x = x < 0 ? x + sd.nc[0] : (x >= sd.nc[0] ? x - sd.nc[0] : x);
                     else ok = ok && x >= 0 && x < sd.nc[0];
@@ -394,58 +374,89 @@ template<class R> __global__ void __launch_bounds__(128) k_nlist(KArgs<R> a, int
                     const int t = __shfl_up_sync(0xffffffffu, inc, o);
                     if (lane >= o) inc += t;
                 }
-                const int my_off = running + inc - cnt;
-                if (cidx < vol) {
-                    off[cidx] = my_off;
-                    beg[cidx] = rg.x;
+                if (lane < 27) {
+                    off[lane] = inc - cnt;
+                    beg[lane] = rg.x;
                 }
-                if (STG) {
-                    // a non-empty cell opens a new slot range unless the previous
-                    // non-empty cell (box order) ends where it begins
-                    const unsigned nem = __ballot_sync(0xffffffffu, cnt > 0);
-                    const unsigned below = nem & ((1u << lane) - 1u);
-                    const int pe = __shfl_sync(0xffffffffu, rg.y, below ? 31 - __clz(below) : 0);
-                    const bool newr = cnt > 0 && rg.x != (below ? pe : carry_end);
-                    const unsigned nm = __ballot_sync(0xffffffffu, newr);
-                    const int rid = nranges + __popc(nm & ((1u << lane) - 1u));
-                    if (newr && rid < STG_RMAX) meta[1 + rid] = make_int2(rg.x, my_off);
-                    nranges += __popc(nm);
-                    if (nem) carry_end = __shfl_sync(0xffffffffu, rg.y, 31 - __clz(nem));
-                }
-                running += __shfl_sync(0xffffffffu, inc, 31);
-            }
-            if (lane == 0) off[vol] = running;
-            __syncwarp();
-            total_c = running;
-            staged = STG && nranges <= STG_RMAX && total_c <= STG_CAND;
-            for (int c0 = 0; c0 < total_c; c0 += CAND) {
-                const int nch = min(CAND, total_c - c0);
-                for (int t = lane; t < nch; t += 32) {
-                    const int idx = c0 + t;
-                    int l = 0, h = vol;  // off[l] <= idx < off[h]
-                    while (h - l > 1) {
-                        const int mid = (l + h) >> 1;
-                        if (off[mid] <= idx) l = mid;
-                        else h = mid;
-                    }
-                    const int j = beg[l] + (idx - off[l]);
-                    s_pos[warp][t] = a.pos[cur][j];
-                    const int kx = l % bx_n, ky = (l / bx_n) % by_n, kz = l / (bx_n * by_n);
-                    s_jk[warp][t] = make_int2(j, kx | (ky << 8) | (kz << 16));
-                }
+                const int total_c = __shfl_sync(0xffffffffu, inc, 31);
+                if (lane == 0) off[27] = total_c;
                 __syncwarp();
-                if (real) {
-                    for (int t = 0; t < nch; ++t) {
-                        const int2 jk = s_jk[warp][t];
-                        const int dx = (jk.y & 255) - rx0, dy = ((jk.y >> 8) & 255) - ry0, dz = (jk.y >> 16) - rz0;
-                        if (unsigned(dx + 1) > 2u || unsigned(dy + 1) > 2u || unsigned(dz + 1) > 2u || jk.x == i)
-                            continue;
-                        test(staged ? c0 + t : jk.x, s_pos[warp][t], dx, dy, dz);
+                // per-particle counters of this cell's particles, carried across passes
+                int cin = 0, cout = 0, ctot = 0;
+                for (int c0 = 0; c0 < total_c; c0 += CAND) {
+                    const int nch = min(CAND, total_c - c0);
+                    for (int t = lane; t < nch; t += 32) {
+                        const int idx = c0 + t;
+                        int l = 0;  // last neighbour cell with off[l] <= idx
+#pragma unroll
+                        for (int step = 16; step > 0; step >>= 1)
+                            if (l + step < 27 && off[l + step] <= idx) l += step;
+                        const int j = beg[l] + (idx - off[l]);
+                        s_pos[warp][t] = a.pos[cur][j];
+                        s_j[warp][t] = j;
+                        s_code[warp][t] = (unsigned char)l;
                     }
+                    __syncwarp();
+                    for (unsigned g = grp; g; g &= g - 1u) {
+                        const int il = __ffs(g) - 1;
+                        T4 pi = p;
+                        pi.x = __shfl_sync(0xffffffffu, p.x, il);
+                        pi.y = __shfl_sync(0xffffffffu, p.y, il);
+                        pi.z = __shfl_sync(0xffffffffu, p.z, il);
+                        const int ti = __shfl_sync(0xffffffffu, ty, il);
+                        const int gi = i - lane + il;
+                        int qin = __shfl_sync(0xffffffffu, cin, il), qout = __shfl_sync(0xffffffffu, cout, il);
+                        int qtot = __shfl_sync(0xffffffffu, ctot, il);
+                        for (int b0 = 0; b0 < nch; b0 += 32) {
+                            const int t = b0 + lane;
+                            bool acc = false, inner = false;
+                            uint32_t ent = 0;
+                            if (t < nch) {
+                                const int j = s_j[warp][t];
+                                const T4 q = s_pos[warp][t];
+                                const int tj = w_type(wbits(q.w));
+                                const float rl2 = rl2s[ti * 16 + tj];
+                                if (j != gi && rl2 > 0.f) {
+                                    const int code = s_code[warp][t];
+                                    const int dx = code % 3 - 1, dy = (code / 3) % 3 - 1, dz = code / 9 - 1;
+                                    const R r2 = dist2(pi, q, dx, dy, dz);
+                                    if (r2 < R(rl2)) {
+                                        acc = true;
+                                        inner = r2 < R(ri2s[ti * 16 + tj]);
+                                        ent = uint32_t(j) | (uint32_t(code) << NB_SHIFT);
+                                    }
+                                }
+                            }
+                            const unsigned ma = __ballot_sync(0xffffffffu, acc);
+                            const unsigned mi = __ballot_sync(0xffffffffu, acc && inner);
+                            // entries past the capacity are counted, not written
+                            const bool wr = acc && qin + qout + __popc(ma & lt) < a.cap;
+                            const unsigned mw = __ballot_sync(0xffffffffu, wr);
+                            if (wr) {
+                                const int row = inner ? qin + __popc(mi & mw & lt)
+                                                      : a.cap - 1 - (qout + __popc(~mi & mw & lt));
+                                a.nbr[nbr_index(gi, row, a.cap)] = ent;
+                            }
+                            qin += __popc(mi & mw);
+                            qout += __popc(~mi & mw);
+                            qtot += __popc(ma);
+                        }
+                        if (lane == il) {
+                            cin = qin;
+                            cout = qout;
+                            ctot = qtot;
+                        }
+                    }
+                    __syncwarp();
                 }
-                __syncwarp();
+                if (grp & (1u << lane)) {
+                    nin = cin;
+                    nout = cout;
+                    total = ctot;
+                }
             }
-        } else if (real) {
+        }
+        if (!swept && real) {
             for (int dz = -1; dz <= 1; ++dz) {
                 int z = cc[2] + dz;
                 if (sd.per[2]) {
@@ -475,7 +486,6 @@ template<class R> __global__ void __launch_bounds__(128) k_nlist(KArgs<R> a, int
             }
         }
         a.nnb[i] = real ? (nin | (nout << 16)) : 0;
-        if (lane == 0) a.wmeta[int64_t(i >> 5) * 32] = staged ? make_int2(nranges, total_c) : make_int2(0, 0);
         maxc = max(maxc, total);
     }
     // block max -> global max; last block finalises the rebuild

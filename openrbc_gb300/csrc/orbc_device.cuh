@@ -22,6 +22,7 @@ constexpr int NT = 6;            // particle types (src/forcefield_canonical.h:3
 constexpr int GHOST = 15;        // type of padding slots
 constexpr int SYS_PAD = 256;     // slot padding per system
 constexpr int STEP_BS = 128;     // threads per block of the force / integrator kernels (divides SYS_PAD)
+constexpr int LITE_BS = 64;      // threads per block of the Langevin step without per-system sums
 constexpr int MAX_BT = 8;        // bond types
 constexpr int MAX_DEG = 15;      // bonds / faces per particle (4-bit fields)
 constexpr uint32_t NB_MASK = (1u << 27) - 1u;
@@ -29,12 +30,6 @@ constexpr int NB_SHIFT = 27;
 constexpr int MAX_SLOTS = 1 << 27;
 constexpr int NPART = 8;         // per-block partial sums: ke2, epot, maxd2, flags, lipid sum v (3), pad
 constexpr int MESH_CHUNK = 1024; // faces per block of the area / volume kernel
-// Warp staging (mixed precision): the union of the 27-cell neighbourhoods of
-// a warp's 32 slots is at most STG_RMAX contiguous slot ranges holding at most
-// STG_CAND particles; the step kernels copy their positions and orientations
-// to shared memory once and the warp's list entries index that copy.
-constexpr int STG_CAND = 304;
-constexpr int STG_RMAX = 31;
 
 enum : int {
     ERRB_NBR_OVERFLOW = 1,  // a neighbour list overflowed its capacity
@@ -168,8 +163,6 @@ template<class R> struct KArgs {
     double *mesh_partial;    // [nmblk][2] area, volume
     uint32_t *nbr;           // warp-blocked ELL neighbour list (nbr_index)
     int *nnb;                // inner count | shell count << 16 (see k_nlist)
-    int2 *wmeta;             // per warp of slots, 32 entries: {staged ranges (0 = not staged), candidates},
-                             // then {first slot, first local index} of each range
     int cap;
     int2 *ranges;            // cell -> [begin, end) of its slots
     int *slot_of_home;
@@ -192,6 +185,7 @@ template<class R> struct KArgs {
     int variant;             // force-kernel form (see launch_step_langevin)
     int carry_forces;        // forces / torques persist between kernels (Nose-Hoover)
     int zero_bulk;           // remove the mean lipid velocity before integrating
+    int nlist_lane;          // neighbour-list form: 0 warp box sweep, 1 per-lane 27-cell sweep
     const FFDev<R> *ff;      // force-field tables (global; staged into shared memory per block)
 };
 
@@ -206,6 +200,12 @@ template<class R> void launch_nh_initial(const KArgs<R> &a, cudaStream_t st);
 template<class R> void launch_nh_prologue(const KArgs<R> &a, cudaStream_t st);
 template<class R> void launch_forces(const KArgs<R> &a, cudaStream_t st);
 template<class R> void launch_vcom(const KArgs<R> &a, cudaStream_t st);
+template<class R> void launch_minimize(const KArgs<R> &a, double dr_opt, double dn_opt, cudaStream_t st);
+template<class R>
+void launch_frame_pack(const KArgs<R> &a, const int *file_of_home, int real_bytes, void *pos, void *vel, void *rot,
+                       int *cell, void *frc, cudaStream_t st);
+template<class R> void launch_set_carried(const KArgs<R> &a, const double *f3, const double *t3, int64_t nhome,
+                                          cudaStream_t st);
 template<class R>
 cudaError_t launch_rdf(const double *x3, const int *type, int n, const double centre[3], const double L[3], int ta,
                        int tb, double dr, int nbins, double rcut, unsigned long long *counts,

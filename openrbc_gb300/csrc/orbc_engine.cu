@@ -7,15 +7,165 @@
 
 #include <algorithm>
 #include <cmath>
+#include <condition_variable>
 #include <cstdio>
 #include <cstring>
+#include <deque>
 #include <memory>
+#include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 namespace orbc {
 
 static thread_local std::string g_last_error;
+
+/* ------------------------------------------------------------------------- */
+/* Trajectory frames (src/trajectory.h:26-105): the device gathers a frame's  */
+/* payload (POSITION, VELOCITY, ROTATION, VORONOI, FORCE) into a staging      */
+/* buffer, a copy stream moves it to one of two pinned host buffers, and a    */
+/* writer thread appends titles, header, identity and payload to the file --  */
+/* the caller's stream goes on stepping meanwhile.                            */
+/* ------------------------------------------------------------------------- */
+class FrameWriter {
+   public:
+    struct Job {
+        std::string path;
+        bool append = false;
+        int nstep = 0, fields = 0, real_bytes = 4;
+        uint64_t natom = 0;
+        std::shared_ptr<const std::vector<int32_t>> ident;  // (tag, type) pairs in file order
+        size_t bytes = 0;                                   // payload bytes in the host buffer
+    };
+    ~FrameWriter() { stop(); }
+
+    /* A free buffer of at least `bytes` (waits for a pending write to end). */
+    int acquire(size_t bytes, int device, std::string &err) {
+        std::unique_lock<std::mutex> lk(m_);
+        if (!started_) {
+            dev_ = device;
+            th_ = std::thread([this] { run(); });
+            started_ = true;
+        }
+        cv_.wait(lk, [this] { return !slot_[0].busy || !slot_[1].busy; });
+        const int s = slot_[0].busy ? 1 : 0;
+        Slot &sl = slot_[s];
+        if (!sl.ev && cudaEventCreateWithFlags(&sl.ev, cudaEventDisableTiming) != cudaSuccess) {
+            err = "frame writer: cudaEventCreate failed";
+            return -1;
+        }
+        if (sl.cap < bytes) {
+            if (sl.h) cudaFreeHost(sl.h);
+            sl.h = nullptr;
+            sl.cap = 0;
+            if (cudaMallocHost(&sl.h, bytes ? bytes : 1) != cudaSuccess) {
+                err = "frame writer: pinned allocation of " + std::to_string(bytes) + " bytes failed";
+                return -1;
+            }
+            sl.cap = bytes;
+        }
+        sl.busy = true;
+        return s;
+    }
+    char *host(int s) { return slot_[s].h; }
+    cudaEvent_t event(int s) { return slot_[s].ev; }
+    void submit(int s, Job job) {
+        std::lock_guard<std::mutex> lk(m_);
+        slot_[s].job = std::move(job);
+        q_.push_back(s);
+        cv_.notify_all();
+    }
+    /* Wait until every submitted frame is on disk; returns the first write
+     * error since the last flush (empty if none). */
+    std::string flush() {
+        std::unique_lock<std::mutex> lk(m_);
+        cv_.wait(lk, [this] { return q_.empty() && !slot_[0].busy && !slot_[1].busy; });
+        std::string e;
+        e.swap(werr_);
+        return e;
+    }
+    void stop() {
+        {
+            std::unique_lock<std::mutex> lk(m_);
+            if (!started_) return;
+            cv_.wait(lk, [this] { return q_.empty() && !slot_[0].busy && !slot_[1].busy; });
+            quit_ = true;
+            cv_.notify_all();
+        }
+        th_.join();
+        started_ = false;
+        for (Slot &sl : slot_) {
+            if (sl.h) cudaFreeHost(sl.h);
+            if (sl.ev) cudaEventDestroy(sl.ev);
+            sl.h = nullptr;
+            sl.ev = nullptr;
+            sl.cap = 0;
+        }
+    }
+
+   private:
+    struct Slot {
+        char *h = nullptr;
+        size_t cap = 0;
+        cudaEvent_t ev = nullptr;
+        bool busy = false;
+        Job job;
+    };
+    Slot slot_[2];
+    std::deque<int> q_;
+    std::mutex m_;
+    std::condition_variable cv_;
+    std::thread th_;
+    bool started_ = false, quit_ = false;
+    int dev_ = 0;
+    std::string werr_;
+
+    static bool put_title(FILE *f, const char *t) {
+        char b[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        std::memcpy(b, t, std::strlen(t));
+        return std::fwrite(b, 1, 8, f) == 8;
+    }
+    void run() {
+        cudaSetDevice(dev_);
+        for (;;) {
+            int s;
+            {
+                std::unique_lock<std::mutex> lk(m_);
+                cv_.wait(lk, [this] { return quit_ || !q_.empty(); });
+                if (q_.empty()) return;
+                s = q_.front();
+            }
+            Slot &sl = slot_[s];
+            const Job &j = sl.job;
+            std::string e;
+            if (cudaEventSynchronize(sl.ev) != cudaSuccess) e = "frame writer: device copy failed";
+            FILE *f = e.empty() ? std::fopen(j.path.c_str(), j.append ? "ab" : "wb") : nullptr;
+            if (e.empty() && !f) e = "frame writer: cannot open " + j.path;
+            if (f) {
+                bool ok = put_title(f, "FRAMEBEG") && std::fwrite(&j.nstep, 4, 1, f) == 1 && put_title(f, "NATOM") &&
+                          std::fwrite(&j.natom, 8, 1, f) == 1 && put_title(f, "IDENTITY") &&
+                          std::fwrite(j.ident->data(), 4, j.ident->size(), f) == j.ident->size();
+                static const char *titles[5] = {"POSITION", "VELOCITY", "ROTATION", "VORONOI", "FORCE"};
+                static const int bits[5] = {1, 8, 2, 4, 16};
+                size_t off = 0;
+                for (int k = 0; k < 5 && ok; ++k) {
+                    if (!(j.fields & bits[k])) continue;
+                    const size_t b = size_t(j.natom) * (k == 3 ? 4 : 3 * size_t(j.real_bytes));
+                    ok = put_title(f, titles[k]) && std::fwrite(sl.h + off, 1, b, f) == b;
+                    off += b;
+                }
+                ok = ok && put_title(f, "FRAMEEND");
+                if (std::fclose(f) != 0 || !ok) e = "frame writer: write to " + j.path + " failed";
+            }
+            std::lock_guard<std::mutex> lk(m_);
+            if (!e.empty() && werr_.empty()) werr_ = e;
+            q_.pop_front();
+            sl.busy = false;
+            cv_.notify_all();
+        }
+    }
+};
 
 /* ------------------------------------------------------------------------- */
 /* Force field in FP64 (src/forcefield_canonical.h:23-156).                  */
@@ -133,6 +283,11 @@ class EngineBase {
                        const int *bonds3, const double *bond_r0, size_t nb, const int *faces3, size_t nf) = 0;
     virtual int set_state(const double *x3, const double *n3, const double *v3, const double *o3) = 0;
     virtual int assign_temperature(double kT, uint64_t seed) = 0;
+    virtual int minimize(int nsteps, double dr_opt, double dn_opt, orbc_thermo *out) = 0;
+    virtual int save_frame(const char *path, int append, int nstep, int fields, int real_bytes, int async) = 0;
+    virtual int flush_frames() = 0;
+    virtual int save_checkpoint(const char *path) = 0;
+    virtual int load_checkpoint(const char *path) = 0;
     virtual int step(int nsteps, orbc_thermo *out) = 0;
     virtual int download(double *x3, double *n3, double *v3, double *o3) = 0;
     virtual int forces(double *f3, double *t3, double *e) = 0;
@@ -176,9 +331,13 @@ template<class R> class Engine : public EngineBase {
    public:
     explicit Engine(const orbc_params &p) { P = p; }
     ~Engine() override {
+        fw.stop();  // pending frames reach the disk before the buffers go
         drop_graph();
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
+        for (cudaEvent_t &e : fpack)
+            if (e) cudaEventDestroy(e);
+        if (cs) cudaStreamDestroy(cs);
         if (st) cudaStreamDestroy(st);
     }
 
@@ -186,8 +345,11 @@ template<class R> class Engine : public EngineBase {
         int ndev = 0;
         if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(ORBC_ERR_NODEV, "no CUDA device");
         CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        CK(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
         CK(cudaEventCreate(&ev0));
         CK(cudaEventCreate(&ev1));
+        for (cudaEvent_t &e : fpack) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        CK(cudaGetDevice(&device));
         return ORBC_OK;
     }
 
@@ -218,6 +380,22 @@ template<class R> class Engine : public EngineBase {
         }
         this->nsys = nsys;
         nhome = n;
+        {  // frame order (src/trajectory.h:75-77): lipids, then proteins, each in upload order
+            std::vector<int> hf(static_cast<size_t>(n));
+            auto id = std::make_shared<std::vector<int32_t>>(static_cast<size_t>(2 * n));
+            int64_t k = 0;
+            for (int pass = 0; pass < 2; ++pass)
+                for (int64_t q = 0; q < n; ++q)
+                    if ((type[q] == 0) == (pass == 0)) {
+                        hf[size_t(q)] = int(k);
+                        (*id)[size_t(2 * k)] = tag[q];
+                        (*id)[size_t(2 * k + 1)] = type[q];
+                        ++k;
+                    }
+            ident = id;
+            CK(fmap.alloc(size_t(n)));
+            CK(cudaMemcpy(fmap.p, hf.data(), hf.size() * sizeof(int), cudaMemcpyHostToDevice));
+        }
         const FFHost &F = ffh();
         // tag -> caller index
         int maxtag = 0;
@@ -279,7 +457,7 @@ template<class R> class Engine : public EngineBase {
                     sd.Lc[dd] = Lc;
                     sd.lo[dd] = 0.5 * (mn + mx) - 0.5 * nc * Lc;
                 }
-                if (P.bounce && P.integrator == ORBC_INT_NOSE_HOOVER) {
+                if (P.bounce && !sd.per[dd]) {  // walls (Nose-Hoover step, minimisation) on open axes
                     sd.wlo[dd] = d.lo[dd];
                     sd.whi[dd] = d.hi[dd];
                 }
@@ -428,7 +606,7 @@ template<class R> class Engine : public EngineBase {
         if (epart.alloc(size_t(npad)) || faces.alloc(hfaces.size()) || ranges.alloc(size_t(total_cells)) ||
             soh.alloc(size_t(n)) || blk_sys.alloc(size_t(nb256)) || partial.alloc(size_t(nblk) * NPART) ||
             Sd.alloc(1) || sysd.alloc(size_t(nsys)) || ssd.alloc(size_t(nsys)) || counts.alloc(size_t(256) * ntiles) ||
-            dtot.alloc(256) || invd.alloc(size_t(npad)) || ffd.alloc(1) || nnb.alloc(size_t(npad)) || wmeta.alloc(size_t(npad)) ||
+            dtot.alloc(256) || invd.alloc(size_t(npad)) || ffd.alloc(1) || nnb.alloc(size_t(npad)) ||
             stage.alloc(size_t(n) * 12) || mesh_bs.alloc(hmbs.size()) || mesh_part.alloc(hmbs.size() * 2 + 2))
             return fail(ORBC_ERR_NOMEM, "upload: device allocation failed");
         cap = P.max_neighbors > 0 ? P.max_neighbors : 64;
@@ -458,7 +636,6 @@ template<class R> class Engine : public EngineBase {
         CK(cudaMemsetAsync(partial.p, 0, size_t(nblk) * NPART * sizeof(double), st));
         CK(cudaMemsetAsync(epart.p, 0, size_t(npad) * sizeof(double), st));
         CK(cudaMemsetAsync(nnb.p, 0, size_t(npad) * sizeof(int), st));
-        CK(cudaMemsetAsync(wmeta.p, 0, size_t(npad) * sizeof(int2), st));
         // other parity copies start equal (gather overwrites them before use)
         Scalars hs;
         std::memset(&hs, 0, sizeof(hs));
@@ -506,6 +683,170 @@ template<class R> class Engine : public EngineBase {
         return ORBC_OK;
     }
 
+    int minimize(int nsteps, double dr_opt, double dn_opt, orbc_thermo *out) override {
+        if (!uploaded) return fail(ORBC_ERR_STATE, "minimize before upload");
+        if (nsteps < 0 || !(dr_opt > 0) || !(dn_opt > 0))
+            return fail(ORBC_ERR_ARG, "minimize: need nsteps >= 0 and positive move limits");
+        for (int k = 0; k < nsteps; ++k) {
+            launch_rebuild<R>(a, st, true);
+            if (has_mesh) launch_mesh<R>(a, st);
+            launch_minimize<R>(a, dr_opt, dn_opt, st);
+        }
+        CK(cudaGetLastError());
+        CK(cudaStreamSynchronize(st));
+        nh_primed = false;   // forces of the new configuration are not carried
+        vcom_valid = false;  // walls may have reversed velocities
+        Scalars hs;
+        CK(cudaMemcpy(&hs, Sd.p, sizeof(Scalars), cudaMemcpyDeviceToHost));
+        if (out) {
+            int rc = thermo(-1, out);
+            if (rc) return rc;
+        }
+        if (hs.max_nnb > cap * 0.85 || (hs.error & ERRB_NBR_OVERFLOW)) {
+            int rc = grow_capacity(hs.max_nnb);
+            if (rc) return rc;
+        }
+        const int code = err_code_of(hs.error & ~ERRB_GRID);
+        if (code) return fail(code, "minimize: device reported error bits " + std::to_string(hs.error));
+        return ORBC_OK;
+    }
+
+    int save_frame(const char *path, int append, int nstep, int fields, int real_bytes, int async) override {
+        if (!uploaded) return fail(ORBC_ERR_STATE, "save_frame before upload");
+        if (!path || (fields & ~31) || (real_bytes != 4 && real_bytes != 8))
+            return fail(ORBC_ERR_ARG, "save_frame: need a path, fields within 0..31 and real_bytes 4 or 8");
+        const size_t n = size_t(nhome), vec = 3 * n * size_t(real_bytes);
+        // payload in file order: POSITION, VELOCITY, ROTATION, VORONOI, FORCE
+        size_t off[5], bytes = 0;
+        const int bits[5] = {1, 8, 2, 4, 16};
+        for (int k = 0; k < 5; ++k) {
+            off[k] = bytes;
+            if (fields & bits[k]) bytes += k == 3 ? 4 * n : vec;
+        }
+        if (fields & 16) {
+            // Nose-Hoover carries the forces of the current positions; otherwise evaluate them
+            if (!(P.integrator == ORBC_INT_NOSE_HOOVER && nh_primed)) {
+                launch_rebuild<R>(a, st, true);
+                if (has_mesh) launch_mesh<R>(a, st);
+                launch_forces<R>(a, st);
+                nh_primed = false;
+            }
+        }
+        std::string err;
+        const int sl = fw.acquire(bytes, device, err);
+        if (sl < 0) return fail(ORBC_ERR_NOMEM, err);
+        if (fstage[sl].n < bytes) CK(fstage[sl].alloc(bytes));
+        char *d = fstage[sl].p;
+        auto at = [&](int k) -> void * { return (fields & bits[k]) ? d + off[k] : nullptr; };
+        launch_frame_pack<R>(a, fmap.p, real_bytes, at(0), at(1), at(2), static_cast<int *>(at(3)), at(4), st);
+        CK(cudaGetLastError());
+        CK(cudaEventRecord(fpack[sl], st));
+        CK(cudaStreamWaitEvent(cs, fpack[sl], 0));
+        if (bytes) CK(cudaMemcpyAsync(fw.host(sl), d, bytes, cudaMemcpyDeviceToHost, cs));
+        CK(cudaEventRecord(fw.event(sl), cs));
+        FrameWriter::Job job;
+        job.path = path;
+        job.append = append != 0;
+        job.nstep = nstep;
+        job.fields = fields;
+        job.real_bytes = real_bytes;
+        job.natom = uint64_t(n);
+        job.ident = ident;
+        job.bytes = bytes;
+        fw.submit(sl, std::move(job));
+        if (!async) return flush_frames();
+        return ORBC_OK;
+    }
+
+    int flush_frames() override {
+        const std::string e = fw.flush();
+        if (!e.empty()) return fail(ORBC_ERR_IO, e);
+        return ORBC_OK;
+    }
+
+    /* Checkpoint: the caller-order state in FP64 plus everything a bitwise
+     * continuation of the step needs beyond it -- step counter (the noise
+     * counter), RNG key, per-system Nose-Hoover zeta and the carried forces
+     * and torques of the Nose-Hoover step. */
+    int save_checkpoint(const char *path) override {
+        if (!uploaded) return fail(ORBC_ERR_STATE, "save_checkpoint before upload");
+        if (!path) return fail(ORBC_ERR_ARG, "save_checkpoint: no path");
+        const size_t m = size_t(nhome) * 3;
+        std::vector<double> buf(6 * m);
+        int rc = download(buf.data(), buf.data() + m, buf.data() + 2 * m, buf.data() + 3 * m);
+        if (rc) return rc;
+        const int carried = (P.integrator == ORBC_INT_NOSE_HOOVER && nh_primed) ? 1 : 0;
+        if (carried) {
+            double *dd = stage.p;
+            launch_download<R>(a, nullptr, nullptr, nullptr, nullptr, dd, dd + m, nullptr, st);
+            CK(cudaGetLastError());
+            CK(cudaMemcpyAsync(buf.data() + 4 * m, dd, 2 * m * sizeof(double), cudaMemcpyDeviceToHost, st));
+        }
+        std::vector<SysState> hss(static_cast<size_t>(nsys));
+        Scalars hs;
+        CK(cudaMemcpyAsync(hss.data(), ssd.p, hss.size() * sizeof(SysState), cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(&hs, Sd.p, sizeof(Scalars), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        FILE *f = std::fopen(path, "wb");
+        if (!f) return fail(ORBC_ERR_IO, std::string("save_checkpoint: cannot open ") + path);
+        const char magic[8] = {'O', 'R', 'B', 'C', 'C', 'K', 'P', 'T'};
+        const int32_t hdr[4] = {1, P.precision, nsys, carried};
+        const int64_t counts[2] = {nhome, int64_t(hs.step)};
+        const uint64_t seed = P.seed;
+        bool ok = std::fwrite(magic, 1, 8, f) == 8 && std::fwrite(hdr, 4, 4, f) == 4 &&
+                  std::fwrite(counts, 8, 2, f) == 2 && std::fwrite(&seed, 8, 1, f) == 1;
+        for (int k = 0; ok && k < nsys; ++k) ok = std::fwrite(&hss[size_t(k)].zeta, 8, 1, f) == 1;
+        const size_t nd = (carried ? 6 : 4) * m;
+        ok = ok && std::fwrite(buf.data(), sizeof(double), nd, f) == nd;
+        if (std::fclose(f) != 0 || !ok) return fail(ORBC_ERR_IO, std::string("save_checkpoint: write failed: ") + path);
+        return ORBC_OK;
+    }
+
+    int load_checkpoint(const char *path) override {
+        if (!uploaded) return fail(ORBC_ERR_STATE, "load_checkpoint before upload (the topology comes from upload)");
+        if (!path) return fail(ORBC_ERR_ARG, "load_checkpoint: no path");
+        FILE *f = std::fopen(path, "rb");
+        if (!f) return fail(ORBC_ERR_IO, std::string("load_checkpoint: cannot open ") + path);
+        char magic[8];
+        int32_t hdr[4];
+        int64_t counts[2];
+        uint64_t seed;
+        bool ok = std::fread(magic, 1, 8, f) == 8 && std::memcmp(magic, "ORBCCKPT", 8) == 0 &&
+                  std::fread(hdr, 4, 4, f) == 4 && std::fread(counts, 8, 2, f) == 2 && std::fread(&seed, 8, 1, f) == 1;
+        if (!ok || hdr[0] != 1 || hdr[2] != nsys || counts[0] != nhome) {
+            std::fclose(f);
+            return fail(ORBC_ERR_ARG, "load_checkpoint: not a checkpoint of this topology (particles / systems differ)");
+        }
+        const int carried = hdr[3];
+        std::vector<double> zeta(static_cast<size_t>(nsys));
+        const size_t m = size_t(nhome) * 3, nd = (carried ? 6 : 4) * m;
+        std::vector<double> buf(nd);
+        ok = std::fread(zeta.data(), 8, zeta.size(), f) == zeta.size() && std::fread(buf.data(), 8, nd, f) == nd;
+        std::fclose(f);
+        if (!ok) return fail(ORBC_ERR_IO, std::string("load_checkpoint: truncated file ") + path);
+        int rc = set_state(buf.data(), buf.data() + m, buf.data() + 2 * m, buf.data() + 3 * m);
+        if (rc) return rc;
+        std::vector<SysState> hss(static_cast<size_t>(nsys));
+        CK(cudaMemcpyAsync(hss.data(), ssd.p, hss.size() * sizeof(SysState), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        for (int k = 0; k < nsys; ++k) hss[size_t(k)].zeta = zeta[size_t(k)];
+        CK(cudaMemcpyAsync(ssd.p, hss.data(), hss.size() * sizeof(SysState), cudaMemcpyHostToDevice, st));
+        const long long stepv = counts[1];
+        CK(cudaMemcpyAsync(&Sd.p->step, &stepv, sizeof(stepv), cudaMemcpyHostToDevice, st));
+        P.seed = seed;
+        a.seed = seed;
+        drop_graph();  // the captured graph holds the kernel arguments (seed)
+        if (carried && P.integrator == ORBC_INT_NOSE_HOOVER) {
+            double *dd = stage.p;
+            CK(cudaMemcpyAsync(dd, buf.data() + 4 * m, 2 * m * sizeof(double), cudaMemcpyHostToDevice, st));
+            launch_set_carried<R>(a, dd, dd + m, nhome, st);
+            CK(cudaGetLastError());
+            nh_primed = true;
+        }
+        CK(cudaStreamSynchronize(st));
+        return ORBC_OK;
+    }
+
     int assign_temperature(double kT, uint64_t seed) override {
         if (!uploaded) return fail(ORBC_ERR_STATE, "assign_temperature before upload");
         if (!(kT >= 0)) return fail(ORBC_ERR_ARG, "assign_temperature: kT must be >= 0");
@@ -531,8 +872,10 @@ template<class R> class Engine : public EngineBase {
             launch_step_langevin<R>(a, st, P.energy != 0);
         }
     }
+    /* Langevin without energy or bulk-velocity removal: no per-step sums */
+    bool lite() const { return P.integrator == ORBC_INT_LANGEVIN && !P.energy && !P.zero_bulk; }
     int fixed_launches_per_step() const {
-        int k = 1 + (has_mesh ? 1 : 0) + (P.integrator == ORBC_INT_NOSE_HOOVER ? 1 : 0);
+        int k = 1 + (has_mesh ? 1 : 0) + (P.integrator == ORBC_INT_NOSE_HOOVER ? 1 : 0) + (lite() ? 1 : 0);
         return k + (graph_cond ? 1 : 0);
     }
     int rebuild_launches() const { return 1 + 3 * passes + 1 + 1; }
@@ -730,6 +1073,11 @@ template<class R> class Engine : public EngineBase {
             launch_mesh<R>(a, st);
             CK(cudaGetLastError());
         }
+        // the lite Langevin step keeps no per-step sums: reduce sum m v^2 now
+        if (lite()) {
+            launch_vcom<R>(a, st);
+            CK(cudaGetLastError());
+        }
         std::vector<SysState> hss(static_cast<size_t>(nsys));
         Scalars hs;
         CK(cudaMemcpyAsync(hss.data(), ssd.p, hss.size() * sizeof(SysState), cudaMemcpyDeviceToHost, st));
@@ -773,24 +1121,15 @@ template<class R> class Engine : public EngineBase {
         CK(cudaMemcpy(hn.data(), nnb.p, hn.size() * sizeof(int), cudaMemcpyDeviceToHost));
         CK(cudaMemcpy(hh.data(), home[hs.lp].p, hh.size() * sizeof(int), cudaMemcpyDeviceToHost));
         CK(cudaMemcpy(hl.data(), nbr.p, hl.size() * sizeof(uint32_t), cudaMemcpyDeviceToHost));
-        std::vector<int2> hm(static_cast<size_t>(npad));
-        CK(cudaMemcpy(hm.data(), wmeta.p, hm.size() * sizeof(int2), cudaMemcpyDeviceToHost));
         std::vector<std::vector<int>> per(static_cast<size_t>(nhome));
         for (int p = 0; p < npad; ++p) {
             const int h = hh[size_t(p)];
             if (h < 0) continue;
-            const int2 *m = hm.data() + size_t(p >> 5) * 32;  // staged warp: entries are local indices
             const int nin = hn[size_t(p)] & 0xffff, nout = hn[size_t(p)] >> 16;
             for (int k = 0; k < nin + nout; ++k) {
                 const int row = k < nin ? k : cap - 1 - (k - nin);
                 const uint32_t ent = hl[size_t(nbr_index(p, row, cap))];
-                int j = int(ent & NB_MASK);
-                if (m[0].x > 0) {
-                    int r = 0;
-                    while (r + 1 < m[0].x && m[2 + r].y <= j) ++r;
-                    j = m[1 + r].x + (j - m[1 + r].y);
-                }
-                per[size_t(h)].push_back(hh[size_t(j)]);
+                per[size_t(h)].push_back(hh[size_t(ent & NB_MASK)]);
             }
             std::sort(per[size_t(h)].begin(), per[size_t(h)].end());
         }
@@ -978,38 +1317,42 @@ template<class R> class Engine : public EngineBase {
         CK(cudaMemcpy(hss.data(), ssd.p, hss.size() * sizeof(SysState), cudaMemcpyDeviceToHost));
         for (size_t k = 0; k < hss.size(); ++k) topo.descs[k].zeta = hss[k].zeta;
         const double skins[] = {0.3, 0.45, 0.6, 0.8, 1.0};
-        const int variants[] = {0, 1, 2, 3};
         double best_ms = 1e300, best_skin = P.skin;
         int best_var = P.kernel_variant, nt = 0;
-        for (double sk : skins) {
-            for (int var : variants) {
-                P.skin = sk;
-                P.kernel_variant = var;
-                rc = relayout(x, nv, v, o, hs.step);
-                if (rc) return rc;
-                rc = step(3, nullptr);  // warm: builds the graph
-                if (rc) return rc;
-                Scalars b4;
-                CK(cudaMemcpy(&b4, Sd.p, sizeof(Scalars), cudaMemcpyDeviceToHost));
-                rc = step(trial_steps, nullptr);
-                if (rc) return rc;
-                Scalars af;
-                CK(cudaMemcpy(&af, Sd.p, sizeof(Scalars), cudaMemcpyDeviceToHost));
-                const double ms = last_ms / trial_steps;
-                if (trials && nt < max_trials) {
-                    trials[nt].skin = sk;
-                    trials[nt].variant = var;
-                    trials[nt].ms_per_step = ms;
-                    trials[nt].rebuilds_per_step = double(af.rebuilds - b4.rebuilds) / trial_steps;
-                }
-                ++nt;
-                if (ms < best_ms) {
-                    best_ms = ms;
-                    best_skin = sk;
-                    best_var = var;
-                }
+        auto trial = [&](double sk, int var) -> int {
+            P.skin = sk;
+            P.kernel_variant = var;
+            int r = relayout(x, nv, v, o, hs.step);
+            if (r) return r;
+            r = step(3, nullptr);  // warm: builds the graph
+            if (r) return r;
+            Scalars b4;
+            CK(cudaMemcpy(&b4, Sd.p, sizeof(Scalars), cudaMemcpyDeviceToHost));
+            r = step(trial_steps, nullptr);
+            if (r) return r;
+            Scalars af;
+            CK(cudaMemcpy(&af, Sd.p, sizeof(Scalars), cudaMemcpyDeviceToHost));
+            const double ms = last_ms / trial_steps;
+            if (trials && nt < max_trials) {
+                trials[nt].skin = sk;
+                trials[nt].variant = var;
+                trials[nt].ms_per_step = ms;
+                trials[nt].rebuilds_per_step = double(af.rebuilds - b4.rebuilds) / trial_steps;
             }
-        }
+            ++nt;
+            if (ms < best_ms) {
+                best_ms = ms;
+                best_skin = sk;
+                best_var = var;
+            }
+            return ORBC_OK;
+        };
+        // skin x force-kernel form (bits 0-1), then the list-build form (bit 2) at the best pair
+        const int list_form = P.kernel_variant & 4;
+        for (double sk : skins)
+            for (int var = 0; var < 4; ++var)
+                if ((rc = trial(sk, var | list_form))) return rc;
+        if ((rc = trial(best_skin, best_var ^ 4))) return rc;
         if (ntrials) *ntrials = nt;
         P.skin = best_skin;
         P.kernel_variant = best_var;
@@ -1144,7 +1487,6 @@ template<class R> class Engine : public EngineBase {
         a.mesh_partial = mesh_part.p;
         a.nbr = nbr.p;
         a.nnb = nnb.p;
-        a.wmeta = wmeta.p;
         a.cap = cap;
         a.ranges = ranges.p;
         a.slot_of_home = soh.p;
@@ -1166,7 +1508,8 @@ template<class R> class Engine : public EngineBase {
         a.skin_half2 = R(0.25 * P.skin * P.skin);
         a.seed = P.seed;
         a.rebuild_every = P.rebuild_every;
-        a.variant = P.kernel_variant;
+        a.variant = P.kernel_variant & 3;
+        a.nlist_lane = (P.kernel_variant >> 2) & 1;
         a.carry_forces = P.integrator == ORBC_INT_NOSE_HOOVER ? 1 : 0;
         a.zero_bulk = P.zero_bulk ? 1 : 0;
         a.ff = ffd.p;
@@ -1223,8 +1566,13 @@ template<class R> class Engine : public EngineBase {
         graph_cond = false;
     }
 
-    cudaStream_t st = nullptr;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaStream_t st = nullptr, cs = nullptr;  // step stream, frame-copy stream
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, fpack[2] = {nullptr, nullptr};
+    int device = 0;
+    FrameWriter fw;
+    DevBuf<char> fstage[2];
+    DevBuf<int> fmap;                                    // file position of each upload index
+    std::shared_ptr<const std::vector<int32_t>> ident;  // (tag, type) pairs in file order
     cudaGraphExec_t gexec = nullptr;
     bool graph_cond = false;
     int graph_steps = 0;
@@ -1245,7 +1593,6 @@ template<class R> class Engine : public EngineBase {
     DevBuf<int> soh, blk_sys, counts, dtot, invd, nnb, mesh_bs;
     DevBuf<double> mesh_part;
     DevBuf<uint32_t> nbr;
-    DevBuf<int2> wmeta;
     DevBuf<Scalars> Sd;
     DevBuf<SysDev> sysd;
     DevBuf<SysState> ssd;
@@ -1301,7 +1648,7 @@ int orbc_gpu_create(const orbc_params *p, orbc_handle **out) {
     *out = nullptr;
     if (!(p->dt > 0) || p->skin < 0 || (p->precision != ORBC_PREC_FP64 && p->precision != ORBC_PREC_MIXED) ||
         (p->integrator != ORBC_INT_LANGEVIN && p->integrator != ORBC_INT_NOSE_HOOVER) ||
-        (p->kernel_variant < 0 || p->kernel_variant > 3) || (p->zero_bulk != 0 && p->zero_bulk != 1)) {
+        (p->kernel_variant < 0 || p->kernel_variant > 7) || (p->zero_bulk != 0 && p->zero_bulk != 1)) {
         g_last_error = "create: invalid parameters";
         return ORBC_ERR_ARG;
     }
@@ -1382,6 +1729,20 @@ int orbc_gpu_rebuild(orbc_handle *h) { return h ? h->e->rebuild() : ORBC_ERR_ARG
 int orbc_gpu_rdf(orbc_handle *h, int sys, int type_a, int type_b, double dr, int nbins, double rcut,
                  uint64_t *counts, int64_t *dropped) {
     return h ? h->e->rdf(sys, type_a, type_b, dr, nbins, rcut, counts, dropped) : ORBC_ERR_ARG;
+}
+int orbc_gpu_save_frame(orbc_handle *h, const char *path, int append, int nstep, int fields, int real_bytes,
+                        int async) {
+    return h ? h->e->save_frame(path, append, nstep, fields, real_bytes, async) : ORBC_ERR_ARG;
+}
+int orbc_gpu_flush(orbc_handle *h) { return h ? h->e->flush_frames() : ORBC_ERR_ARG; }
+int orbc_gpu_save_checkpoint(orbc_handle *h, const char *path) {
+    return h ? h->e->save_checkpoint(path) : ORBC_ERR_ARG;
+}
+int orbc_gpu_load_checkpoint(orbc_handle *h, const char *path) {
+    return h ? h->e->load_checkpoint(path) : ORBC_ERR_ARG;
+}
+int orbc_gpu_minimize(orbc_handle *h, int nsteps, double dr_max, double dn_max, orbc_thermo *out) {
+    return h ? h->e->minimize(nsteps, dr_max, dn_max, out) : ORBC_ERR_ARG;
 }
 int orbc_gpu_assign_temperature(orbc_handle *h, double kBT, uint64_t seed) {
     return h ? h->e->assign_temperature(kBT, seed) : ORBC_ERR_ARG;

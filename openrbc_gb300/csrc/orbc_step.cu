@@ -38,60 +38,6 @@ template<> __device__ __forceinline__ double4a ldg4<double>(const double4a *p) {
     return r;
 }
 
-/* Partner loads: read-only global path, or the warp's shared-memory copy. */
-template<class R, bool SM> __device__ __forceinline__ typename Vec<R>::T4 ldp(const typename Vec<R>::T4 *p) {
-    if (SM)
-        return *p;
-    else
-        return ldg4<R>(p);
-}
-
-/* Shared-memory copy of the warp's neighbourhood (mixed precision only). */
-template<class R> struct StageBuf {
-    static constexpr int N = sizeof(typename Vec<R>::T4) == 16 ? STG_CAND : 1;
-    typename Vec<R>::T4 pos[STEP_BS / 32][N], nrm[STEP_BS / 32][N];
-};
-
-/* Copy the positions and orientations of this warp's candidate ranges (wmeta)
- * to shared memory with cp.async; returns whether the warp's list entries are
- * local indices into that copy.  All 32 lanes must call it. */
-template<class R>
-__device__ __forceinline__ bool stage_warp(const KArgs<R> &a, int i, int cur, StageBuf<R> &sb) {
-    if constexpr (StageBuf<R>::N == 1) {
-        return false;
-    } else {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int2 m = a.wmeta[int64_t(i >> 5) * 32 + lane];
-    const int nr = __shfl_sync(0xffffffffu, m.x, 0);
-    if (nr == 0) return false;
-    const int ntot = __shfl_sync(0xffffffffu, m.y, 0);
-    const typename Vec<R>::T4 *pos = a.pos[cur], *nrm = a.nrm[cur];
-    for (int t0 = 0; t0 < ntot; t0 += 32) {
-        const int t = t0 + lane;
-        // range r holding candidate t: the last r < nr with first local index <= t
-        int r = 0;
-#pragma unroll
-        for (int step = 16; step > 0; step >>= 1) {
-            const int c = r + step;
-            const int oc = __shfl_sync(0xffffffffu, m.y, min(c + 1, 31));
-            if (c < nr && oc <= t) r = c;
-        }
-        const int first = __shfl_sync(0xffffffffu, m.x, r + 1);
-        const int loc = __shfl_sync(0xffffffffu, m.y, r + 1);
-        if (t < ntot) {
-            const int j = first + (t - loc);
-            const unsigned dp = unsigned(__cvta_generic_to_shared(&sb.pos[warp][t]));
-            const unsigned dn = unsigned(__cvta_generic_to_shared(&sb.nrm[warp][t]));
-            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dp), "l"(pos + j) : "memory");
-            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dn), "l"(nrm + j) : "memory");
-        }
-    }
-    asm volatile("cp.async.wait_all;" ::: "memory");
-    __syncwarp();
-    return true;
-    }
-}
-
 __device__ __forceinline__ void inv_sqrt(float r2, float &r, float &rinv) {
     rinv = rsqrtf(r2);
     r = r2 * rinv;
@@ -281,17 +227,17 @@ template<class R> __device__ __forceinline__ void init_shift(typename Vec<R>::T4
 
 /* All forces and torques on particle slot i: pair terms over its neighbour
  * list (variant V, see launch_step_langevin), bonds, mesh constraint. */
-template<class R, bool E, int V, bool SM>
+template<class R, bool E, int V>
 __device__ __forceinline__ void particle_forces(const KArgs<R> &a, const FFDev<R> &F, int i, int cur, int lp, int w,
                                                 const typename Vec<R>::T4 &pi, const typename Vec<R>::T4 &ni,
                                                 const SysDev &sd, const SysState &ss,
-                                                const typename Vec<R>::T4 *sh, const typename Vec<R>::T4 *srcp,
-                                                const typename Vec<R>::T4 *srcn, R3<R> &f, R3<R> &t, R &e,
+                                                const typename Vec<R>::T4 *sh, R3<R> &f, R3<R> &t, R &e,
                                                 int &flags) {
     using T4 = typename Vec<R>::T4;
     const int ty = w_type(w);
     const R Lx = R(sd.Lc[0]), Ly = R(sd.Lc[1]), Lz = R(sd.Lc[2]);
-    const T4 *__restrict__ pos = a.pos[cur];  // bond and face partners (global slots)
+    const T4 *__restrict__ pos = a.pos[cur];
+    const T4 *__restrict__ nrm = a.nrm[cur];
     const uint32_t *__restrict__ nb = a.nbr + nbr_index(i, 0, a.cap);
     const int packed = a.nnb[i];
     const int nin = packed & 0xffff, nout = packed >> 16;
@@ -333,8 +279,8 @@ __device__ __forceinline__ void particle_forces(const KArgs<R> &a, const FFDev<R
         uint32_t e2 = nin > 1 ? __ldg(nb + stride) : 0u;
         T4 pn, nn;
         if (nin > 0) {
-            pn = ldp<R, SM>(srcp + int(e1 & NB_MASK));
-            nn = ldp<R, SM>(srcn + int(e1 & NB_MASK));
+            pn = ldg4<R>(pos + int(e1 & NB_MASK));
+            nn = ldg4<R>(nrm + int(e1 & NB_MASK));
         }
         for (int k = 0; k < nin; ++k) {
             const uint32_t ent = e1;
@@ -342,8 +288,8 @@ __device__ __forceinline__ void particle_forces(const KArgs<R> &a, const FFDev<R
             e1 = e2;
             if (k + 2 < nin) e2 = __ldg(nb + int64_t(k + 2) * stride);
             if (k + 1 < nin) {
-                pn = ldp<R, SM>(srcp + int(e1 & NB_MASK));
-                nn = ldp<R, SM>(srcn + int(e1 & NB_MASK));
+                pn = ldg4<R>(pos + int(e1 & NB_MASK));
+                nn = ldg4<R>(nrm + int(e1 & NB_MASK));
             }
             pair(ent, pj, nj);
         }
@@ -352,7 +298,7 @@ __device__ __forceinline__ void particle_forces(const KArgs<R> &a, const FFDev<R
         for (int k = 0; k < nin; ++k) {
             const uint32_t ent = __ldg(nb + int64_t(k) * stride);
             const int j = int(ent & NB_MASK);
-            pair(ent, ldp<R, SM>(srcp + j), ldp<R, SM>(srcn + j));
+            pair(ent, ldg4<R>(pos + j), ldg4<R>(nrm + j));
         }
     }
     // Shell rows: partners in the skin at the last build, mostly still outside
@@ -361,7 +307,7 @@ __device__ __forceinline__ void particle_forces(const KArgs<R> &a, const FFDev<R
     for (int k = 0; k < nout; ++k) {
         const uint32_t ent = __ldg(shell - int64_t(k) * stride);
         const int j = int(ent & NB_MASK);
-        const T4 pj = ldp<R, SM>(srcp + j);
+        const T4 pj = ldg4<R>(pos + j);
         const T4 s = sh[ent >> NB_SHIFT];
         const R dx = (pi.x - pj.x) + s.x * Lx;
         const R dy = (pi.y - pj.y) + s.y * Ly;
@@ -369,7 +315,7 @@ __device__ __forceinline__ void particle_forces(const KArgs<R> &a, const FFDev<R
         const R r2 = dx * dx + dy * dy + dz * dz;
         const int tj = w_type(wbits(pj.w));
         const R lim = ((ty | tj) == 0) ? ll_cutsq : F.pair[ty * NT + tj].anysq;
-        if (r2 < lim) pair(ent, pj, ldp<R, SM>(srcn + j));
+        if (r2 < lim) pair(ent, pj, ldg4<R>(nrm + j));
     }
     // bonds
     const int bd = w_bdeg(w);
@@ -440,27 +386,27 @@ template<class R> __device__ __forceinline__ R u11(uint32_t u) { return R(u >> 8
 
 constexpr int STEP_WARPS = STEP_BS / 32;
 
-/* particle_forces with the partners read from the warp's shared-memory copy
- * (stg) or from global memory. */
-template<class R, bool E, int V>
-__device__ __forceinline__ void forces_of(bool stg, const StageBuf<R> &sb, const KArgs<R> &a, const FFDev<R> &F,
-                                          int i, int cur, int lp, int w, const typename Vec<R>::T4 &pi,
-                                          const typename Vec<R>::T4 &ni, const SysDev &sd, const SysState &ss,
-                                          const typename Vec<R>::T4 *sh, R3<R> &f, R3<R> &t, R &e, int &flags) {
-    if constexpr (StageBuf<R>::N > 1) {
-        if (stg) {
-            const int warp = threadIdx.x >> 5;
-            particle_forces<R, E, V, true>(a, F, i, cur, lp, w, pi, ni, sd, ss, sh, sb.pos[warp], sb.nrm[warp], f, t,
-                                           e, flags);
-            return;
+/* Reflective walls (src/integrate_nh.h:124-144) on the axes where the system
+ * has them (wlo < whi), applied in the frame of the particle's cell. */
+template<class R>
+__device__ __forceinline__ void bounce_walls(const SysDev &sd, int c, typename Vec<R>::T4 &p, typename Vec<R>::T4 &v) {
+    const int cc[3] = {cx_of(c), cy_of(c), cz_of(c)};
+    R *pp[3] = {&p.x, &p.y, &p.z};
+    R *vv[3] = {&v.x, &v.y, &v.z};
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        if (!(sd.wlo[d] < sd.whi[d])) continue;
+        const double center = sd.lo[d] + (double(cc[d]) + 0.5) * sd.Lc[d];
+        const R lo = R(sd.wlo[d] - center), hi = R(sd.whi[d] - center);
+        if (*pp[d] < lo) {
+            *pp[d] = lo + (lo - *pp[d]);
+            *vv[d] = -*vv[d];
+        } else if (*pp[d] > hi) {
+            *pp[d] = hi - (*pp[d] - hi);
+            *vv[d] = -*vv[d];
         }
     }
-    particle_forces<R, E, V, false>(a, F, i, cur, lp, w, pi, ni, sd, ss, sh, a.pos[cur], a.nrm[cur], f, t, e, flags);
 }
-
-// resident blocks per SM the force kernels are compiled for: the mixed form
-// is limited by its shared-memory stage to 5 blocks
-#define STEP_MINB(R, V) (sizeof(R) == 4 ? 5 : (((V) & 2) ? 6 : 8))
 
 enum { MODE_LANGEVIN = 0, MODE_NH_FINAL = 1, MODE_NH_INITIAL = 2, MODE_FORCES = 3, MODE_VCOM = 4 };
 
@@ -603,91 +549,214 @@ __device__ __forceinline__ void finish(const KArgs<R> &a, double ke, double ep, 
     }
 }
 
-template<class R, bool E, int V> __global__ void __launch_bounds__(STEP_BS, STEP_MINB(R, V)) k_step_langevin(KArgs<R> a) {
+/* One particle of the fused Langevin step: forces at the current state, then
+ * src/integrate_langevin.h:105-146 (rotation, then translation with the
+ * counter-based noise).  Writes the new state; returns the squared
+ * displacement since the list was built, sum m v^2, the energy and the lipid
+ * velocity (for the bulk-velocity removal). */
+template<class R, bool E, int V>
+__device__ __forceinline__ void langevin_particle(const KArgs<R> &a, const FFDev<R> &F, const typename Vec<R>::T4 *sh,
+                                                  int i, int s, int cur, int lp, long long step,
+                                                  const typename Vec<R>::T4 &pi, int w, bool zero_bulk, double &ke,
+                                                  double &ep, float &md2, int &flags, double &vsx, double &vsy,
+                                                  double &vsz) {
+    using T4 = typename Vec<R>::T4;
+    const int ty = w_type(w);
+    const SysDev &sd = a.sys[s];
+    const T4 ni = a.nrm[cur][i];
+    R3<R> f = {0, 0, 0}, t = {0, 0, 0};
+    R e = 0;
+    particle_forces<R, E, V>(a, F, i, cur, lp, w, pi, ni, sd, a.ss[s], sh, f, t, e, flags);
+    const R dt = R(a.dt);
+    T4 v = a.vel[lp][i], o = a.omg[lp][i];
+    if (zero_bulk && ty == 0) {  // zero_bulk_velocity on the lipids (src/zero_bulk_velocity.h:38-45)
+        v.x -= R(__ldcg(&a.ss[s].vcom[0]));
+        v.y -= R(__ldcg(&a.ss[s].vcom[1]));
+        v.z -= R(__ldcg(&a.ss[s].vcom[2]));
+    }
+    // ROTATION: t <- n x t; o += dt t; n <- normalize(n + (o x n) dt)
+    const R tx = ni.y * t.z - ni.z * t.y, ty_ = ni.z * t.x - ni.x * t.z, tz = ni.x * t.y - ni.y * t.x;
+    o.x += dt * tx;
+    o.y += dt * ty_;
+    o.z += dt * tz;
+    const R gx = ni.x + (o.y * ni.z - o.z * ni.y) * dt;
+    const R gy = ni.y + (o.z * ni.x - o.x * ni.z) * dt;
+    const R gz = ni.z + (o.x * ni.y - o.y * ni.x) * dt;
+    const R gi = rnorm3(gx, gy, gz);
+    T4 nn = ni;
+    nn.x = gx * gi;
+    nn.y = gy * gi;
+    nn.z = gz * gi;
+    // TRANSLATION: f -= gamma v + sigma r; v += f dt/m; x += v dt
+    uint32_t r0, r1, r2;
+    philox3(uint32_t(a.tag[lp][i]), uint32_t(step), uint32_t((unsigned long long)step >> 32), uint32_t(s),
+            uint32_t(a.seed), uint32_t(a.seed >> 32), r0, r1, r2);
+    const R gam = F.gamma[ty], sig = F.sigma[ty];
+    const R dtm = dt * F.inv_mass[ty];
+    f.x -= gam * v.x + sig * u11<R>(r0);
+    f.y -= gam * v.y + sig * u11<R>(r1);
+    f.z -= gam * v.z + sig * u11<R>(r2);
+    v.x += f.x * dtm;
+    v.y += f.y * dtm;
+    v.z += f.z * dtm;
+    T4 p = pi;
+    p.x += v.x * dt;
+    p.y += v.y * dt;
+    p.z += v.z * dt;
+    a.pos[cur ^ 1][i] = p;
+    a.nrm[cur ^ 1][i] = nn;
+    a.vel[lp][i] = v;
+    a.omg[lp][i] = o;
+    const T4 xr = a.xref[lp][i];
+    const R ddx = p.x - xr.x, ddy = p.y - xr.y, ddz = p.z - xr.z;
+    md2 = float(ddx * ddx + ddy * ddy + ddz * ddz);
+    if (!isfinite(p.x + p.y + p.z + v.x + v.y + v.z)) flags |= ERRB_NAN;
+    ke = double(F.mass[ty]) * (double(v.x) * double(v.x) + double(v.y) * double(v.y) + double(v.z) * double(v.z));
+    ep = double(e);
+    if (ty == 0) {
+        vsx = double(v.x);
+        vsy = double(v.y);
+        vsz = double(v.z);
+    }
+}
+
+/* Langevin step with the per-system sums (energy, bulk-velocity removal):
+ * force-field table staged in shared memory, block partials reduced by the
+ * last block. */
+template<class R, bool E, int V> __global__ void __launch_bounds__(STEP_BS, (V & 2) ? 6 : 8) k_step_langevin(KArgs<R> a) {
     using T4 = typename Vec<R>::T4;
     __shared__ T4 sh[27];
     __shared__ FFDev<R> F;
-    __shared__ StageBuf<R> sb;
     stage_ff<R>(&F, a.ff);
     init_shift<R>(sh);
     const int cur = __ldcg(&a.S->cur), lp = __ldcg(&a.S->lp);
     const long long step = __ldcg(&a.S->step);
     const int i = blockIdx.x * STEP_BS + threadIdx.x;
     const int s = a.blk_sys[(blockIdx.x * STEP_BS) / SYS_PAD];
+    const T4 pi = a.pos[cur][i];
+    prefetch_warp_list(a.nbr, i, a.cap, a.nnb[i]);
+    const int w = wbits(pi.w);
+    double ke = 0, ep = 0, vsx = 0, vsy = 0, vsz = 0;
+    float md2 = 0.f;
+    int flags = 0;
+    if (w_type(w) != GHOST)
+        langevin_particle<R, E, V>(a, F, sh, i, s, cur, lp, step, pi, w, a.zero_bulk != 0, ke, ep, md2, flags, vsx,
+                                   vsy, vsz);
+    finish<R>(a, ke, ep, md2, flags, MODE_LANGEVIN, 1, vsx, vsy, vsz);
+}
+
+/* Langevin step without per-system sums (no energy, no bulk-velocity
+ * removal): small blocks that retire independently, the force-field table read
+ * through the read-only path, and no end-of-block reduction -- a warp whose
+ * particles moved more than skin/2 raises the rebuild flag itself, and
+ * k_advance flips the buffers after the kernel.  The temperature is reduced on
+ * demand (k_vcom). */
+template<class R, int V>
+__global__ void __launch_bounds__(LITE_BS, (V & 2) ? 12 : 16) k_step_langevin_lite(KArgs<R> a) {
+    using T4 = typename Vec<R>::T4;
+    __shared__ T4 sh[27];
+    init_shift<R>(sh);
+    const FFDev<R> *__restrict__ Fp = a.ff;
+    const int cur = __ldcg(&a.S->cur), lp = __ldcg(&a.S->lp);
+    const long long step = __ldcg(&a.S->step);
+    const int i = blockIdx.x * LITE_BS + threadIdx.x;
+    const int s = a.blk_sys[i / SYS_PAD];
+    const T4 pi = a.pos[cur][i];
+    prefetch_warp_list(a.nbr, i, a.cap, a.nnb[i]);
+    const int w = wbits(pi.w);
+    double ke = 0, ep = 0, vsx = 0, vsy = 0, vsz = 0;
+    float md2 = 0.f;
+    int flags = 0;
+    if (w_type(w) != GHOST)
+        langevin_particle<R, false, V>(a, *Fp, sh, i, s, cur, lp, step, pi, w, false, ke, ep, md2, flags, vsx, vsy,
+                                       vsz);
+    const unsigned m = __reduce_max_sync(0xffffffffu, __float_as_uint(md2));  // md2 >= 0: bit order = value order
+    const int fl = int(__reduce_or_sync(0xffffffffu, unsigned(flags)));
+    if ((threadIdx.x & 31) == 0) {
+        if (double(__uint_as_float(m)) > double(a.skin_half2) || !(__uint_as_float(m) == __uint_as_float(m)))
+            a.S->rebuild = 1;
+        if (fl) atomicOr(&a.S->error, fl);
+    }
+}
+
+/* After a lite Langevin step (count_step = 1) or a minimisation step (0):
+ * flip the position buffers, advance the step counter and apply the
+ * every-k-steps rebuild rule. */
+__global__ void k_advance(Scalars *S, int rebuild_every, int count_step) {
+    S->cur ^= 1;
+    S->step += count_step;
+    S->since_rebuild += 1;
+    if (rebuild_every > 0 && S->since_rebuild >= rebuild_every) S->rebuild = 1;
+}
+
+/* One step of the energy minimisation (src/openrbc.cpp:88-146): forces,
+ * post_torque t <- n x t (src/integrate_nh.h:146-154), the step-limited
+ * steepest-descent move of :113-130 and bounce_back (:132).  Positions and
+ * orientations ping-pong like the Langevin step; the step counter (the noise
+ * key) does not advance. */
+template<class R, int V>
+__global__ void __launch_bounds__(LITE_BS, (V & 2) ? 12 : 16) k_minimize(KArgs<R> a, double dr_opt, double dn_opt) {
+    using T4 = typename Vec<R>::T4;
+    __shared__ T4 sh[27];
+    init_shift<R>(sh);
+    const FFDev<R> *__restrict__ Fp = a.ff;
+    const int cur = __ldcg(&a.S->cur), lp = __ldcg(&a.S->lp);
+    const int i = blockIdx.x * LITE_BS + threadIdx.x;
+    const int s = a.blk_sys[i / SYS_PAD];
     const SysDev &sd = a.sys[s];
     const T4 pi = a.pos[cur][i];
     prefetch_warp_list(a.nbr, i, a.cap, a.nnb[i]);
-    const bool stg = stage_warp<R>(a, i, cur, sb);
     const int w = wbits(pi.w);
     const int ty = w_type(w);
-    double ke = 0, ep = 0, vsx = 0, vsy = 0, vsz = 0;
     float md2 = 0.f;
     int flags = 0;
     if (ty != GHOST) {
         const T4 ni = a.nrm[cur][i];
         R3<R> f = {0, 0, 0}, t = {0, 0, 0};
         R e = 0;
-        forces_of<R, E, V>(stg, sb, a, F, i, cur, lp, w, pi, ni, sd, a.ss[s], sh, f, t, e, flags);
-        const R dt = R(a.dt);
-        T4 v = a.vel[lp][i], o = a.omg[lp][i];
-        if (a.zero_bulk && ty == 0) {  // zero_bulk_velocity on the lipids (src/zero_bulk_velocity.h:38-45)
-            v.x -= R(__ldcg(&a.ss[s].vcom[0]));
-            v.y -= R(__ldcg(&a.ss[s].vcom[1]));
-            v.z -= R(__ldcg(&a.ss[s].vcom[2]));
-        }
-        // ROTATION: t <- n x t; o += dt t; n <- normalize(n + (o x n) dt)
+        particle_forces<R, false, V>(a, *Fp, i, cur, lp, w, pi, ni, sd, a.ss[s], sh, f, t, e, flags);
         const R tx = ni.y * t.z - ni.z * t.y, ty_ = ni.z * t.x - ni.x * t.z, tz = ni.x * t.y - ni.y * t.x;
-        o.x += dt * tx;
-        o.y += dt * ty_;
-        o.z += dt * tz;
-        const R gx = ni.x + (o.y * ni.z - o.z * ni.y) * dt;
-        const R gy = ni.y + (o.z * ni.x - o.x * ni.z) * dt;
-        const R gz = ni.z + (o.x * ni.y - o.y * ni.x) * dt;
-        const R gi = rnorm3(gx, gy, gz);
+        const R m = Fp->mass[ty];
+        const R dxx = f.x / m, dxy = f.y / m, dxz = f.z / m;
+        const R dnx = ty_ * ni.z - tz * ni.y, dny = tz * ni.x - tx * ni.z, dnz = tx * ni.y - ty_ * ni.x;
+        const R ndx = sqrt(dxx * dxx + dxy * dxy + dxz * dxz), ndn = sqrt(dnx * dnx + dny * dny + dnz * dnz);
+        const R dr = R(dr_opt), dn = R(dn_opt);
+        const R h = (ndx > dr || ndn > dn) ? min(dr / ndx, dn / ndn) : R(a.dt);
+        const R hm = h / m;
+        T4 p = pi;
+        p.x += f.x * hm;
+        p.y += f.y * hm;
+        p.z += f.z * hm;
+        const R gx = ni.x + dnx * h, gy = ni.y + dny * h, gz = ni.z + dnz * h;
+        const R gi = R(1) / sqrt(gx * gx + gy * gy + gz * gz);
         T4 nn = ni;
         nn.x = gx * gi;
         nn.y = gy * gi;
         nn.z = gz * gi;
-        // TRANSLATION: f -= gamma v + sigma r; v += f dt/m; x += v dt
-        uint32_t r0, r1, r2;
-        philox3(uint32_t(a.tag[lp][i]), uint32_t(step), uint32_t((unsigned long long)step >> 32), uint32_t(s),
-                uint32_t(a.seed), uint32_t(a.seed >> 32), r0, r1, r2);
-        const R gam = F.gamma[ty], sig = F.sigma[ty];
-        const R dtm = dt * F.inv_mass[ty];
-        f.x -= gam * v.x + sig * u11<R>(r0);
-        f.y -= gam * v.y + sig * u11<R>(r1);
-        f.z -= gam * v.z + sig * u11<R>(r2);
-        v.x += f.x * dtm;
-        v.y += f.y * dtm;
-        v.z += f.z * dtm;
-        T4 p = pi;
-        p.x += v.x * dt;
-        p.y += v.y * dt;
-        p.z += v.z * dt;
+        T4 v = a.vel[lp][i];
+        const T4 v0 = v;
+        bounce_walls<R>(sd, a.cell[lp][i], p, v);
+        if (v.x != v0.x || v.y != v0.y || v.z != v0.z) a.vel[lp][i] = v;
         a.pos[cur ^ 1][i] = p;
         a.nrm[cur ^ 1][i] = nn;
-        a.vel[lp][i] = v;
-        a.omg[lp][i] = o;
         const T4 xr = a.xref[lp][i];
         const R ddx = p.x - xr.x, ddy = p.y - xr.y, ddz = p.z - xr.z;
         md2 = float(ddx * ddx + ddy * ddy + ddz * ddz);
-        if (!isfinite(p.x + p.y + p.z + v.x + v.y + v.z)) flags |= ERRB_NAN;
-        ke = double(F.mass[ty]) * (double(v.x) * double(v.x) + double(v.y) * double(v.y) + double(v.z) * double(v.z));
-        ep = double(e);
-        if (ty == 0) {
-            vsx = double(v.x);
-            vsy = double(v.y);
-            vsz = double(v.z);
-        }
+        if (!isfinite(p.x + p.y + p.z + nn.x + nn.y + nn.z)) flags |= ERRB_NAN;
     }
-    finish<R>(a, ke, ep, md2, flags, MODE_LANGEVIN, 1, vsx, vsy, vsz);
+    const unsigned mm = __reduce_max_sync(0xffffffffu, __float_as_uint(md2));
+    const int fl = int(__reduce_or_sync(0xffffffffu, unsigned(flags)));
+    if ((threadIdx.x & 31) == 0) {
+        if (double(__uint_as_float(mm)) > double(a.skin_half2) || !(__uint_as_float(mm) == __uint_as_float(mm)))
+            a.S->rebuild = 1;
+        if (fl) atomicOr(&a.S->error, fl);
+    }
 }
 
-template<class R, bool E, int V> __global__ void __launch_bounds__(STEP_BS, STEP_MINB(R, V)) k_nh_final(KArgs<R> a, int count_step) {
+template<class R, bool E, int V> __global__ void __launch_bounds__(STEP_BS, (V & 2) ? 6 : 8) k_nh_final(KArgs<R> a, int count_step) {
     using T4 = typename Vec<R>::T4;
     __shared__ T4 sh[27];
     __shared__ FFDev<R> F;
-    __shared__ StageBuf<R> sb;
     stage_ff<R>(&F, a.ff);
     init_shift<R>(sh);
     const int cur = __ldcg(&a.S->cur), lp = __ldcg(&a.S->lp);
@@ -696,7 +765,6 @@ template<class R, bool E, int V> __global__ void __launch_bounds__(STEP_BS, STEP
     const SysDev &sd = a.sys[s];
     const T4 pi = a.pos[cur][i];
     prefetch_warp_list(a.nbr, i, a.cap, a.nnb[i]);
-    const bool stg = stage_warp<R>(a, i, cur, sb);
     const int w = wbits(pi.w);
     const int ty = w_type(w);
     double ke = 0, ep = 0;
@@ -705,7 +773,7 @@ template<class R, bool E, int V> __global__ void __launch_bounds__(STEP_BS, STEP
         const T4 ni = a.nrm[cur][i];
         R3<R> f = {0, 0, 0}, t = {0, 0, 0};
         R e = 0;
-        forces_of<R, E, V>(stg, sb, a, F, i, cur, lp, w, pi, ni, sd, a.ss[s], sh, f, t, e, flags);
+        particle_forces<R, E, V>(a, F, i, cur, lp, w, pi, ni, sd, a.ss[s], sh, f, t, e, flags);
         const R dt = R(a.dt);
         const R zeta = R(__ldcg(&a.ss[s].zeta));
         const R im = F.inv_mass[ty];
@@ -765,24 +833,7 @@ template<class R> __global__ void __launch_bounds__(STEP_BS) k_nh_initial(KArgs<
         p.y += v.y * dt;
         p.z += v.z * dt;
         // bounce back at the walls (src/integrate_nh.h:199-208), in the cell frame
-        if (sd.wlo[0] < sd.whi[0]) {
-            const int c = a.cell[lp][i];
-            const int cc[3] = {cx_of(c), cy_of(c), cz_of(c)};
-            R *pp[3] = {&p.x, &p.y, &p.z};
-            R *vv[3] = {&v.x, &v.y, &v.z};
-#pragma unroll
-            for (int d = 0; d < 3; ++d) {
-                const double center = sd.lo[d] + (double(cc[d]) + 0.5) * sd.Lc[d];
-                const R lo = R(sd.wlo[d] - center), hi = R(sd.whi[d] - center);
-                if (*pp[d] < lo) {
-                    *pp[d] = lo + (lo - *pp[d]);
-                    *vv[d] = -*vv[d];
-                } else if (*pp[d] > hi) {
-                    *pp[d] = hi - (*pp[d] - hi);
-                    *vv[d] = -*vv[d];
-                }
-            }
-        }
+        bounce_walls<R>(sd, a.cell[lp][i], p, v);
         ke = double(a.ff->mass[ty]) * (double(v.x) * double(v.x) + double(v.y) * double(v.y) + double(v.z) * double(v.z));
         if (ty == 0) {
             vsx = double(v.x);
@@ -861,11 +912,10 @@ template<class R> __global__ void __launch_bounds__(256) k_assign_temperature(KA
     a.vel[lp][i] = v;
 }
 
-template<class R, bool E, int V> __global__ void __launch_bounds__(STEP_BS, STEP_MINB(R, V)) k_forces(KArgs<R> a) {
+template<class R, bool E, int V> __global__ void __launch_bounds__(STEP_BS, (V & 2) ? 6 : 8) k_forces(KArgs<R> a) {
     using T4 = typename Vec<R>::T4;
     __shared__ T4 sh[27];
     __shared__ FFDev<R> F;
-    __shared__ StageBuf<R> sb;
     stage_ff<R>(&F, a.ff);
     init_shift<R>(sh);
     const int cur = __ldcg(&a.S->cur), lp = __ldcg(&a.S->lp);
@@ -874,7 +924,6 @@ template<class R, bool E, int V> __global__ void __launch_bounds__(STEP_BS, STEP
     const SysDev &sd = a.sys[s];
     const T4 pi = a.pos[cur][i];
     prefetch_warp_list(a.nbr, i, a.cap, a.nnb[i]);
-    const bool stg = stage_warp<R>(a, i, cur, sb);
     const int w = wbits(pi.w);
     double ep = 0;
     int flags = 0;
@@ -882,7 +931,7 @@ template<class R, bool E, int V> __global__ void __launch_bounds__(STEP_BS, STEP
         const T4 ni = a.nrm[cur][i];
         R3<R> f = {0, 0, 0}, t = {0, 0, 0};
         R e = 0;
-        forces_of<R, E, V>(stg, sb, a, F, i, cur, lp, w, pi, ni, sd, a.ss[s], sh, f, t, e, flags);
+        particle_forces<R, E, V>(a, F, i, cur, lp, w, pi, ni, sd, a.ss[s], sh, f, t, e, flags);
         T4 q = pi;
         q.x = f.x;
         q.y = f.y;
@@ -990,10 +1039,14 @@ template<class R> __global__ void __launch_bounds__(256) k_mesh(KArgs<R> a) {
  * 2-way unrolled loop; bit 1: the rare non-lipid pair path inlined, with up
  * to 85 registers, instead of called).  The autotuner picks one per workload. */
 template<class R, int V> void step_langevin_v(const KArgs<R> &a, cudaStream_t st, bool energy) {
-    if (energy)
+    if (energy) {
         k_step_langevin<R, true, V><<<a.nblk, STEP_BS, 0, st>>>(a);
-    else
+    } else if (a.zero_bulk) {
         k_step_langevin<R, false, V><<<a.nblk, STEP_BS, 0, st>>>(a);
+    } else {
+        k_step_langevin_lite<R, V><<<a.npad / LITE_BS, LITE_BS, 0, st>>>(a);
+        k_advance<<<1, 1, 0, st>>>(a.S, a.rebuild_every, 1);
+    }
 }
 template<class R, int V> void nh_final_v(const KArgs<R> &a, cudaStream_t st, bool energy) {
     if (energy)
@@ -1029,6 +1082,18 @@ template<class R> void launch_forces(const KArgs<R> &a, cudaStream_t st) {
 template<class R> void launch_mesh(const KArgs<R> &a, cudaStream_t st) {
     if (a.nmblk > 0) k_mesh<R><<<a.nmblk, 256, 0, st>>>(a);
 }
+template<class R, int V> void minimize_v(const KArgs<R> &a, double dr_opt, double dn_opt, cudaStream_t st) {
+    k_minimize<R, V><<<a.npad / LITE_BS, LITE_BS, 0, st>>>(a, dr_opt, dn_opt);
+    k_advance<<<1, 1, 0, st>>>(a.S, a.rebuild_every, 0);
+}
+template<class R> void launch_minimize(const KArgs<R> &a, double dr_opt, double dn_opt, cudaStream_t st) {
+    switch (a.variant) {
+        case 1: minimize_v<R, 1>(a, dr_opt, dn_opt, st); break;
+        case 2: minimize_v<R, 2>(a, dr_opt, dn_opt, st); break;
+        case 3: minimize_v<R, 3>(a, dr_opt, dn_opt, st); break;
+        default: minimize_v<R, 0>(a, dr_opt, dn_opt, st); break;
+    }
+}
 template<class R> void launch_vcom(const KArgs<R> &a, cudaStream_t st) {
     k_vcom<R><<<a.nblk, STEP_BS, 0, st>>>(a);
 }
@@ -1043,6 +1108,7 @@ template<class R> void launch_assign_temperature(const KArgs<R> &a, double kT, u
     template void launch_nh_initial<R>(const KArgs<R> &, cudaStream_t);               \
     template void launch_forces<R>(const KArgs<R> &, cudaStream_t);                   \
     template void launch_vcom<R>(const KArgs<R> &, cudaStream_t);                     \
+    template void launch_minimize<R>(const KArgs<R> &, double, double, cudaStream_t); \
     template void launch_assign_temperature<R>(const KArgs<R> &, double, uint64_t, cudaStream_t); \
     template void launch_mesh<R>(const KArgs<R> &, cudaStream_t);
 ORBC_INST(float)

@@ -176,6 +176,38 @@ class Simulation:
     def rebuild(self):
         self._check(N.lib().orbc_gpu_rebuild(self.h))
 
+    def save_frame(self, path: str, nstep: Optional[int] = None, fields: Optional[int] = None, append: bool = True,
+                   real_bytes: int = 4, asynchronous: bool = False):
+        """save_frame (src/trajectory.h:61-105) through orbc_gpu_save_frame:
+        fields default to the parameter's dump_field, nstep to the step
+        counter; real_bytes 4 is the reference's default `real`."""
+        if nstep is None:
+            nstep = int(self.thermo()["step"])
+        f = int(self.param.dump_field if fields is None else fields)
+        self._check(N.lib().orbc_gpu_save_frame(self.h, str(path).encode(), 1 if append else 0, int(nstep), f,
+                                                int(real_bytes), 1 if asynchronous else 0))
+
+    def flush(self):
+        """Wait until every queued frame is written (orbc_gpu_flush)."""
+        self._check(N.lib().orbc_gpu_flush(self.h))
+
+    def save_checkpoint(self, path: str):
+        self._check(N.lib().orbc_gpu_save_checkpoint(self.h, str(path).encode()))
+
+    def load_checkpoint(self, path: str):
+        self._check(N.lib().orbc_gpu_load_checkpoint(self.h, str(path).encode()))
+
+    def minimize(self, nsteps: Optional[int] = None, dr_max: Optional[float] = None,
+                 dn_max: Optional[float] = None) -> dict:
+        """Energy minimisation (orbc_gpu_minimize; src/openrbc.cpp:88-146) with
+        the parameter's opt_nstep, dr_opt and dn_opt by default."""
+        th = N.Thermo()
+        self._check(N.lib().orbc_gpu_minimize(
+            self.h, int(self.param.opt_nstep if nsteps is None else nsteps),
+            float(self.param.dr_opt if dr_max is None else dr_max),
+            float(self.param.dn_opt if dn_max is None else dn_max), C.byref(th)))
+        return th.as_dict()
+
     def assign_temperature(self, kBT: Optional[float] = None, seed: Optional[int] = None, amplify: float = 1.0):
         """integrate(assign_temperature(param, amplify), lipid, protein)
         (src/assign_temperature.h:26-44, src/openrbc.cpp:160) on the device:

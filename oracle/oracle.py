@@ -254,6 +254,14 @@ def nh_steps(st: State, nsteps: int) -> dict:
     return _thermo(th)
 
 
+def minimize(st: State, nsteps: int, dr_opt: float = 0.05, dn_opt: float = 0.05) -> dict:
+    c = st._c()
+    th = OrcThermoC()
+    lib().orc_minimize_f64(C.byref(c), int(nsteps), C.c_double(dr_opt), C.c_double(dn_opt), C.byref(th))
+    _sync_back(st, c)
+    return _thermo(th)
+
+
 def assign_temperature(st: State, kT: float, seed: int) -> None:
     lib().orc_assign_temperature(C.byref(st._c()), float(kT), int(seed))
 

@@ -876,6 +876,46 @@ int orc_step_nh_f64(orc_system *s, int nsteps, orc_thermo *th) {
     return 0;
 }
 
+int orc_minimize_f64(orc_system *s, int nsteps, double dr_opt, double dn_opt, orc_thermo *th) {
+    const int64_t n = s->n;
+    const FF<double> &F = ff<double>();
+    std::vector<double> f3(static_cast<size_t>(3 * n)), t3(static_cast<size_t>(3 * n));
+    for (int it = 0; it < nsteps; ++it) {
+        forces_impl<double>(s, f3.data(), t3.data(), nullptr, th);
+#pragma omp parallel for schedule(static)
+        for (int64_t i = 0; i < n; ++i) {
+            double *x = &s->x[3 * i], *nn = &s->nrm[3 * i], *v = &s->v[3 * i];
+            const double *f = &f3[size_t(3 * i)];
+            double t[3], dn[3], tmp[3];
+            cross3(nn, &t3[size_t(3 * i)], t);  // post_torque
+            const double m = F.mass[s->type[i]];
+            double dx[3];
+            for (int d = 0; d < 3; ++d) dx[d] = f[d] / m;
+            cross3(t, nn, dn);
+            const double ndx = std::sqrt(dot3(dx, dx)), ndn = std::sqrt(dot3(dn, dn));
+            const double h = (ndx > dr_opt || ndn > dn_opt) ? std::min(dr_opt / ndx, dn_opt / ndn) : s->dt;
+            for (int d = 0; d < 3; ++d) x[d] += f[d] * (h / m);
+            cross3(t, nn, tmp);
+            for (int d = 0; d < 3; ++d) nn[d] += tmp[d] * h;
+            const double inv = 1.0 / std::sqrt(dot3(nn, nn));
+            for (int d = 0; d < 3; ++d) nn[d] *= inv;
+            if (s->bounce)
+                for (int d = 0; d < 3; ++d) {
+                    if (s->periodic[d]) continue;
+                    if (x[d] < s->lo[d]) {
+                        x[d] = s->lo[d] + (s->lo[d] - x[d]);
+                        v[d] = -v[d];
+                    } else if (x[d] > s->hi[d]) {
+                        x[d] = s->hi[d] - (x[d] - s->hi[d]);
+                        v[d] = -v[d];
+                    }
+                }
+        }
+    }
+    if (th) orc_thermo_f64(s, th);
+    return 0;
+}
+
 int orc_thermo_f64(const orc_system *s, orc_thermo *th) {
     const FF<double> &F = ff<double>();
     th->ke2 = chunked_sum(s->n, [&](int64_t i) {

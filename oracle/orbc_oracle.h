@@ -94,6 +94,14 @@ int orc_step_langevin_f32(orc_system *s, int nsteps, orc_thermo *th);
 int orc_nh_prologue_f64(orc_system *s, orc_thermo *th);
 int orc_step_nh_f64(orc_system *s, int nsteps, orc_thermo *th);
 
+/* Energy minimisation loop (src/openrbc.cpp:88-146), nsteps iterations of:
+ * forces; post_torque t <- n x t (src/integrate_nh.h:146-154); per particle
+ * dx = f / m, dn = t x n, h = (|dx| > dr_opt || |dn| > dn_opt) ?
+ * min(dr_opt / |dx|, dn_opt / |dn|) : dt; x += f (h / m); n += (t x n) h;
+ * n <- n / |n| (:113-130); bounce_back at lo / hi when s->bounce
+ * (src/integrate_nh.h:124-144).  FP64.  s->step is not advanced. */
+int orc_minimize_f64(orc_system *s, int nsteps, double dr_opt, double dn_opt, orc_thermo *th);
+
 /* assign_temperature (src/assign_temperature.h:26-44): v_d = sqrt(2 kT / m) g
  * with g a unit Gaussian (Box-Muller on Philox4x32-10 keyed by seed and tag;
  * the reference's factor 2 is kept). */

@@ -27,6 +27,8 @@
 #include "integrate_nh.h"
 #include "reorder_morton.h"
 #include "runtime_parameter.h"
+#include "trajectory.h"
+#include "voronoi.h"
 
 using namespace openrbc;
 using namespace openrbc::config;
@@ -186,6 +188,38 @@ double ref_temperature(int64_t n, const double *x, const double *nrm, const doub
     State s;
     s.load(n, x, nrm, v, nullptr, type, tag, 0, nullptr);
     return compute_temperature(s.lipid, s.protein, p);
+}
+
+/* save_frame (src/trajectory.h:61-105) of the given state: lipids (type 0,
+ * implicit tags 1, 2, ... in input order) then proteins, with nstep and the
+ * dump_field bits `fields`; affil gives each input particle's cell
+ * affiliation, f its force.  Writes at most cap bytes to buf and returns the
+ * frame size. */
+int64_t ref_save_frame(int64_t n, const double *x, const double *nrm, const double *v, const double *f,
+                       const int *type, const int *tag, const int *affil, int nstep, int fields, char *buf,
+                       int64_t cap) {
+    omp_set_num_threads(1);
+    RTParameter &p = params();
+    p.nstep = nstep;
+    p.dump_field = fields;
+    State s;
+    s.load(n, x, nrm, v, nullptr, type, tag, 0, nullptr);
+    VCellList cl[2];
+    cl[0].affiliation.resize(s.lipid.size());
+    cl[1].affiliation.resize(s.protein.size());
+    for (size_t k = 0; k < s.lipid_src.size(); ++k) {
+        cl[0].affiliation[k] = affil[s.lipid_src[k]];
+        for (int d = 0; d < 3; ++d) s.lipid.f[k][d] = real(f[3 * s.lipid_src[k] + d]);
+    }
+    for (size_t k = 0; k < s.prot_src.size(); ++k) {
+        cl[1].affiliation[k] = affil[s.prot_src[k]];
+        for (int d = 0; d < 3; ++d) s.protein.f[k][d] = real(f[3 * s.prot_src[k] + d]);
+    }
+    std::ostringstream out;
+    save_frame(out, s.lipid, s.protein, cl[0], cl[1], p);
+    const std::string b = out.str();
+    if (int64_t(b.size()) <= cap) std::memcpy(buf, b.data(), b.size());
+    return int64_t(b.size());
 }
 
 /* morton_encode (src/reorder_morton.h:35-40) with the reference box. */

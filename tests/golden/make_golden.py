@@ -175,6 +175,36 @@ def main():
     np.savez_compressed(os.path.join(OUT, "morton.npz"), p=p, keys64=k64, p32=p32, keys32=k32)
     print("morton:", len(p), "points")
 
+    # ---- trajectory frames (src/trajectory.h:61-105) ---------------------------
+    # 48 lipids and 16 proteins interleaved; lipid tags are the reference's
+    # implicit 1, 2, ... in input order, protein tags 1000 + k.
+    g = np.load(os.path.join(OUT, "cell_ico12.npz"))
+    lip = np.flatnonzero(g["type"] == 0)[:48]
+    pro = np.flatnonzero(g["type"] != 0)[:16]
+    sel = np.sort(np.concatenate([lip, pro]))
+    fx, fn, fv = (np.ascontiguousarray(g[k][sel]) for k in ("x", "nrm", "v"))
+    fty = np.ascontiguousarray(g["type"][sel]).astype(np.int32)
+    ftg = np.zeros(len(sel), np.int32)
+    ftg[fty == 0] = np.arange(1, int((fty == 0).sum()) + 1)
+    ftg[fty != 0] = 1000 + np.arange(int((fty != 0).sum()))
+    ff = np.random.default_rng(7).normal(0, 3.0, fx.shape)
+    faff = np.random.default_rng(8).integers(0, 500, len(sel)).astype(np.int32)
+    frames = {}
+    for prec, fields, nstep in (("f32", 31, 120), ("f64", 31, 120), ("f32", 7, 0)):
+        R = orc.ref(prec)
+        vp = C.c_void_p
+        R.ref_save_frame.restype = C.c_int64
+        R.ref_save_frame.argtypes = [C.c_int64, vp, vp, vp, vp, vp, vp, vp, C.c_int, C.c_int, vp, C.c_int64]
+        args = [C.c_int64(len(sel)), fx.ctypes.data, fn.ctypes.data, fv.ctypes.data, ff.ctypes.data,
+                fty.ctypes.data, ftg.ctypes.data, faff.ctypes.data, C.c_int(nstep), C.c_int(fields)]
+        size = R.ref_save_frame(*args, None, C.c_int64(0))
+        buf = C.create_string_buffer(size)
+        R.ref_save_frame(*args, buf, C.c_int64(size))
+        frames[f"frame_{prec}_{fields}_{nstep}"] = np.frombuffer(buf.raw[:size], np.uint8)
+    np.savez_compressed(os.path.join(OUT, "frames.npz"), x=fx, nrm=fn, v=fv, f=ff, type=fty, tag=ftg, affil=faff,
+                        **frames)
+    print("frames:", {k: len(v) for k, v in frames.items()})
+
 
 if __name__ == "__main__":
     main()
