@@ -177,6 +177,12 @@ int orbc_gpu_neighbors(orbc_handle *h, int *counts, int *list, int64_t cap, int6
 int orbc_gpu_cells(orbc_handle *h, int sys, double *lo3, double *lc3, int *nc3, int *cell, double *offset3,
                    int *slot);
 
+/* Measured FMA throughput of the current GPU in TFLOP/s (FP32 and FP64;
+ * 8 independent FMA chains per thread, every SM busy, ~10 ms): the ALU
+ * roofline denominators of the force kernels.  No counterpart in the
+ * reference. */
+int orbc_gpu_fma_peak(double *tflops_fp32, double *tflops_fp64);
+
 /* Force a neighbour-list rebuild now (sort + bins + list). */
 int orbc_gpu_rebuild(orbc_handle *h);
 
@@ -214,6 +220,19 @@ int orbc_gpu_flush(orbc_handle *h);
  * in the same order); the run then continues where the saved one was. */
 int orbc_gpu_save_checkpoint(orbc_handle *h, const char *path);
 int orbc_gpu_load_checkpoint(orbc_handle *h, const char *path);
+
+/* Stray-lipid cleanup (delete_lipid, src/cleanup.h:29-91, called every
+ * freq_cleanup steps at src/openrbc.cpp:201): lipids are affiliated with the
+ * nearest generator -- the lipid centroid of a 4 x 4 x 4 tile of grid cells
+ * holding at least 8 lipids, standing in for the reference's Voronoi
+ * centroids -- among the surrounding tiles; per generator, a lipid is removed
+ * unless its squared distance to the generator is below stray_tolerance^2
+ * times the median one (a lipid with no generator within two tiles is
+ * removed).  Proteins are never removed.  Survivors keep their order and are
+ * renumbered 0 .. n' - 1 (upload indices, per system), as the reference's
+ * compaction does; *removed receives the count.  The reference's default
+ * stray_tolerance is 2.5 (src/runtime_parameter.h:51). */
+int orbc_gpu_cleanup(orbc_handle *h, double stray_tolerance, int64_t *removed);
 
 /* Energy minimisation (the loop of src/openrbc.cpp:88-146): nsteps times
  * forces, post_torque t <- n x t (src/integrate_nh.h:146-154), the

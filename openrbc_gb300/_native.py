@@ -30,7 +30,7 @@ EXPORTS = [
     "orbc_gpu_morton_encode", "orbc_gpu_morton_order", "orbc_gpu_destroy", "orbc_gpu_error",
     "orbc_gpu_version", "orbc_gpu_profile", "orbc_gpu_morton_order_noalloc", "orbc_gpu_autotune",
     "orbc_gpu_assign_temperature", "orbc_gpu_rdf", "orbc_gpu_minimize", "orbc_gpu_save_frame", "orbc_gpu_flush",
-    "orbc_gpu_save_checkpoint", "orbc_gpu_load_checkpoint",
+    "orbc_gpu_save_checkpoint", "orbc_gpu_load_checkpoint", "orbc_gpu_cleanup", "orbc_gpu_fma_peak",
     "orbc_gen_lattice", "orbc_gen_rbc_counts", "orbc_gen_rbc", "orbc_gen_vesicle_sizes", "orbc_gen_vesicle",
 ]
 
@@ -124,6 +124,8 @@ def lib():
         L.orbc_gpu_minimize.argtypes = [H, i32, d, d, P(Thermo)]
         L.orbc_gpu_save_frame.argtypes = [H, C.c_char_p, i32, i32, i32, i32, i32]
         L.orbc_gpu_flush.argtypes = [H]
+        L.orbc_gpu_cleanup.argtypes = [H, d, P(i64)]
+        L.orbc_gpu_fma_peak.argtypes = [P(d), P(d)]
         L.orbc_gpu_save_checkpoint.argtypes = [H, C.c_char_p]
         L.orbc_gpu_load_checkpoint.argtypes = [H, C.c_char_p]
         L.orbc_gpu_last_timing.argtypes = [H, P(d), P(i64)]

@@ -311,18 +311,25 @@ template<class R> __global__ void __launch_bounds__(128) k_nlist(KArgs<R> a, int
         // Entries inside the pair's interaction range fill rows 0, 1, ... of
         // this slot's column; skin-shell entries fill rows cap-1, cap-2, ...
         int nin = 0, nout = 0, total = 0;
-        // x_i - x_j = (o_i - o_j) - d * Lc, each operation rounded once
-        auto dist2 = [&](const T4 &pi, const T4 &q, int dx, int dy, int dz) {
-            const R ex = add_rn(sub_rn(pi.x, q.x), mul_rn(R(-dx), L[0]));
-            const R ey = add_rn(sub_rn(pi.y, q.y), mul_rn(R(-dy), L[1]));
-            const R ez = add_rn(sub_rn(pi.z, q.z), mul_rn(R(-dz), L[2]));
+        // Candidate j seen from i's cell: o_j + d * Lc (d = cell_j - cell_i);
+        // x_i - x_j = o_i - (o_j + d * Lc).  Each operation is rounded once,
+        // in the same order by both list-build forms.
+        auto shifted = [&](const T4 &q, int dx, int dy, int dz) {
+            T4 r = q;
+            r.x = add_rn(q.x, mul_rn(R(dx), L[0]));
+            r.y = add_rn(q.y, mul_rn(R(dy), L[1]));
+            r.z = add_rn(q.z, mul_rn(R(dz), L[2]));
+            return r;
+        };
+        auto dist2 = [&](const T4 &pi, const T4 &qs) {
+            const R ex = sub_rn(pi.x, qs.x), ey = sub_rn(pi.y, qs.y), ez = sub_rn(pi.z, qs.z);
             return add_rn(add_rn(mul_rn(ex, ex), mul_rn(ey, ey)), mul_rn(ez, ez));
         };
         auto test = [&](int j, const T4 &q, int dx, int dy, int dz) {
             const int tj = w_type(wbits(q.w));
             const float rl2 = rl2s[ty * 16 + tj];
             if (!(rl2 > 0.f)) return;
-            const R r2 = dist2(p, q, dx, dy, dz);
+            const R r2 = dist2(p, shifted(q, dx, dy, dz));
             if (r2 < R(rl2)) {
                 const uint32_t ent = uint32_t(j) | (uint32_t((dx + 1) + 3 * (dy + 1) + 9 * (dz + 1)) << NB_SHIFT);
                 if (nin + nout < a.cap) {
@@ -392,7 +399,7 @@ template<class R> __global__ void __launch_bounds__(128) k_nlist(KArgs<R> a, int
                         for (int step = 16; step > 0; step >>= 1)
                             if (l + step < 27 && off[l + step] <= idx) l += step;
                         const int j = beg[l] + (idx - off[l]);
-                        s_pos[warp][t] = a.pos[cur][j];
+                        s_pos[warp][t] = shifted(a.pos[cur][j], l % 3 - 1, (l / 3) % 3 - 1, l / 9 - 1);
                         s_j[warp][t] = j;
                         s_code[warp][t] = (unsigned char)l;
                     }
@@ -417,13 +424,11 @@ template<class R> __global__ void __launch_bounds__(128) k_nlist(KArgs<R> a, int
                                 const int tj = w_type(wbits(q.w));
                                 const float rl2 = rl2s[ti * 16 + tj];
                                 if (j != gi && rl2 > 0.f) {
-                                    const int code = s_code[warp][t];
-                                    const int dx = code % 3 - 1, dy = (code / 3) % 3 - 1, dz = code / 9 - 1;
-                                    const R r2 = dist2(pi, q, dx, dy, dz);
+                                    const R r2 = dist2(pi, q);
                                     if (r2 < R(rl2)) {
                                         acc = true;
                                         inner = r2 < R(ri2s[ti * 16 + tj]);
-                                        ent = uint32_t(j) | (uint32_t(code) << NB_SHIFT);
+                                        ent = uint32_t(j) | (uint32_t(s_code[warp][t]) << NB_SHIFT);
                                     }
                                 }
                             }

@@ -204,6 +204,10 @@ template<class R> void launch_minimize(const KArgs<R> &a, double dr_opt, double 
 template<class R>
 void launch_frame_pack(const KArgs<R> &a, const int *file_of_home, int real_bytes, void *pos, void *vel, void *rot,
                        int *cell, void *frc, cudaStream_t st);
+template<class R>
+int launch_cleanup_mark(const KArgs<R> &a, int mingen, double tol2, double4a *gen, double *dr2, int *gone_home,
+                        unsigned long long *removed, cudaStream_t st);
+template<class R> void launch_cleanup_apply(const KArgs<R> &a, const int *newidx, int *soh_new, cudaStream_t st);
 template<class R> void launch_set_carried(const KArgs<R> &a, const double *f3, const double *t3, int64_t nhome,
                                           cudaStream_t st);
 template<class R>

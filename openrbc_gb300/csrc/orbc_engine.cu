@@ -287,6 +287,7 @@ class EngineBase {
     virtual int save_frame(const char *path, int append, int nstep, int fields, int real_bytes, int async) = 0;
     virtual int flush_frames() = 0;
     virtual int save_checkpoint(const char *path) = 0;
+    virtual int cleanup(double tol, int64_t *removed) = 0;
     virtual int load_checkpoint(const char *path) = 0;
     virtual int step(int nsteps, orbc_thermo *out) = 0;
     virtual int download(double *x3, double *n3, double *v3, double *o3) = 0;
@@ -380,21 +381,9 @@ template<class R> class Engine : public EngineBase {
         }
         this->nsys = nsys;
         nhome = n;
-        {  // frame order (src/trajectory.h:75-77): lipids, then proteins, each in upload order
-            std::vector<int> hf(static_cast<size_t>(n));
-            auto id = std::make_shared<std::vector<int32_t>>(static_cast<size_t>(2 * n));
-            int64_t k = 0;
-            for (int pass = 0; pass < 2; ++pass)
-                for (int64_t q = 0; q < n; ++q)
-                    if ((type[q] == 0) == (pass == 0)) {
-                        hf[size_t(q)] = int(k);
-                        (*id)[size_t(2 * k)] = tag[q];
-                        (*id)[size_t(2 * k + 1)] = type[q];
-                        ++k;
-                    }
-            ident = id;
-            CK(fmap.alloc(size_t(n)));
-            CK(cudaMemcpy(fmap.p, hf.data(), hf.size() * sizeof(int), cudaMemcpyHostToDevice));
+        {
+            int rc = build_file_order(type, tag, n);
+            if (rc) return rc;
         }
         const FFHost &F = ffh();
         // tag -> caller index
@@ -708,6 +697,98 @@ template<class R> class Engine : public EngineBase {
         }
         const int code = err_code_of(hs.error & ~ERRB_GRID);
         if (code) return fail(code, "minimize: device reported error bits " + std::to_string(hs.error));
+        return ORBC_OK;
+    }
+
+    /* Frame order (src/trajectory.h:75-77): lipids, then proteins, each in
+     * upload order; fmap = file position of each upload index. */
+    int build_file_order(const int *type, const int *tag, int64_t n) {
+        std::vector<int> hf(static_cast<size_t>(n));
+        auto id = std::make_shared<std::vector<int32_t>>(static_cast<size_t>(2 * n));
+        int64_t k = 0;
+        for (int pass = 0; pass < 2; ++pass)
+            for (int64_t q = 0; q < n; ++q)
+                if ((type[q] == 0) == (pass == 0)) {
+                    hf[size_t(q)] = int(k);
+                    (*id)[size_t(2 * k)] = tag[q];
+                    (*id)[size_t(2 * k + 1)] = type[q];
+                    ++k;
+                }
+        ident = id;
+        CK(fmap.alloc(size_t(n)));
+        CK(cudaMemcpy(fmap.p, hf.data(), hf.size() * sizeof(int), cudaMemcpyHostToDevice));
+        return ORBC_OK;
+    }
+
+    /* delete_lipid (src/cleanup.h:29-91): see orbc_cleanup.cu. */
+    int cleanup(double tol, int64_t *removed_out) override {
+        if (!uploaded) return fail(ORBC_ERR_STATE, "cleanup before upload");
+        if (!(tol > 0)) return fail(ORBC_ERR_ARG, "cleanup: stray tolerance must be positive");
+        const int mingen = 4;
+        DevBuf<int> gone;
+        DevBuf<double4a> gen;
+        DevBuf<double> dr2;
+        DevBuf<unsigned long long> cnt;
+        CK(gen.alloc(size_t(npad)));
+        CK(dr2.alloc(size_t(npad)));
+        CK(gone.alloc(size_t(nhome)));
+        CK(cnt.alloc(1));
+        // the cells and ranges of the current positions
+        launch_rebuild<R>(a, st, true);
+        CK(cudaMemsetAsync(gone.p, 0, size_t(nhome) * sizeof(int), st));
+        CK(cudaMemsetAsync(cnt.p, 0, sizeof(unsigned long long), st));
+        CK(cudaMemsetAsync(gen.p, 0, size_t(npad) * sizeof(double4a), st));
+        if (launch_cleanup_mark<R>(a, mingen, tol * tol, gen.p, dr2.p, gone.p, cnt.p, st))
+            return fail(ORBC_ERR_CUDA, "cleanup: kernel launch failed");
+        unsigned long long nrem = 0;
+        CK(cudaMemcpyAsync(&nrem, cnt.p, sizeof(nrem), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        if (removed_out) *removed_out = int64_t(nrem);
+        if (nrem == 0) return ORBC_OK;
+        std::vector<int> hg(static_cast<size_t>(nhome)), newidx(static_cast<size_t>(nhome));
+        CK(cudaMemcpy(hg.data(), gone.p, hg.size() * sizeof(int), cudaMemcpyDeviceToHost));
+        // survivors keep their order (the reference compacts with a prefix sum)
+        int64_t k = 0;
+        std::vector<int64_t> offs(static_cast<size_t>(nsys) + 1, 0);
+        std::vector<int> ntype, ntag;
+        ntype.reserve(size_t(nhome));
+        ntag.reserve(size_t(nhome));
+        for (int sy = 0; sy < nsys; ++sy) {
+            int gone_here = 0;
+            for (int64_t h = topo.offsets[size_t(sy)]; h < topo.offsets[size_t(sy) + 1]; ++h) {
+                if (hg[size_t(h)]) {
+                    newidx[size_t(h)] = -1;
+                    ++gone_here;
+                    continue;
+                }
+                newidx[size_t(h)] = int(k++);
+                ntype.push_back(topo.type[size_t(h)]);
+                ntag.push_back(topo.tag[size_t(h)]);
+            }
+            offs[size_t(sy) + 1] = k;
+            hsys[size_t(sy)].nreal -= gone_here;
+            hsys[size_t(sy)].nlipid -= gone_here;
+        }
+        const int64_t nnew = k;
+        CK(gone.alloc(size_t(nhome)));  // reused for the new numbering
+        CK(cudaMemcpyAsync(gone.p, newidx.data(), newidx.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+        DevBuf<int> soh2;
+        CK(soh2.alloc(size_t(std::max<int64_t>(nnew, 1))));
+        launch_cleanup_apply<R>(a, gone.p, soh2.p, st);
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(sysd.p, hsys.data(), hsys.size() * sizeof(SysDev), cudaMemcpyHostToDevice, st));
+        CK(cudaStreamSynchronize(st));
+        std::swap(soh.p, soh2.p);
+        std::swap(soh.n, soh2.n);
+        a.slot_of_home = soh.p;
+        topo.type.swap(ntype);
+        topo.tag.swap(ntag);
+        topo.offsets = offs;
+        nhome = nnew;
+        int rc = build_file_order(topo.type.data(), topo.tag.data(), nhome);
+        if (rc) return rc;
+        drop_graph();
+        vcom_valid = false;
         return ORBC_OK;
     }
 
@@ -1735,6 +1816,9 @@ int orbc_gpu_save_frame(orbc_handle *h, const char *path, int append, int nstep,
     return h ? h->e->save_frame(path, append, nstep, fields, real_bytes, async) : ORBC_ERR_ARG;
 }
 int orbc_gpu_flush(orbc_handle *h) { return h ? h->e->flush_frames() : ORBC_ERR_ARG; }
+int orbc_gpu_cleanup(orbc_handle *h, double stray_tolerance, int64_t *removed) {
+    return h ? h->e->cleanup(stray_tolerance, removed) : ORBC_ERR_ARG;
+}
 int orbc_gpu_save_checkpoint(orbc_handle *h, const char *path) {
     return h ? h->e->save_checkpoint(path) : ORBC_ERR_ARG;
 }

@@ -165,3 +165,62 @@ template cudaError_t launch_rdf<double>(const double *, const int *, int, const 
                                         cudaStream_t);
 
 }  // namespace orbc
+
+/* ------------------------------------------------------------------------- */
+/* FMA throughput (the ALU roofline denominator of the force kernel): every   */
+/* thread runs 8 independent FMA chains; the result is kept live through a    */
+/* data-dependent store so the compiler cannot drop the chains.               */
+/* ------------------------------------------------------------------------- */
+namespace orbc {
+namespace {
+template<class T> __global__ void __launch_bounds__(256) k_fma_peak(T seed, int iters, T *sink) {
+    T x[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) x[k] = seed + T(threadIdx.x + k);
+    const T a = T(0.999999), b = T(1e-7);
+    for (int it = 0; it < iters; ++it) {
+#pragma unroll
+        for (int u = 0; u < 16; ++u) {
+#pragma unroll
+            for (int k = 0; k < 8; ++k) x[k] = fma(x[k], a, b);
+        }
+    }
+    T s = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) s += x[k];
+    if (s == T(-12345.0)) sink[blockIdx.x] = s;  // never true; keeps the work
+}
+}  // namespace
+}  // namespace orbc
+
+extern "C" int orbc_gpu_fma_peak(double *tflops_fp32, double *tflops_fp64) {
+    using namespace orbc;
+    int dev = 0, nsm = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 9;
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    void *sink = nullptr;
+    if (cudaMalloc(&sink, 1 << 16) != cudaSuccess) return 8;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    const int blocks = nsm * 8, threads = 256;
+    auto run = [&](auto tag, int iters) -> double {
+        using T = decltype(tag);
+        k_fma_peak<T><<<blocks, threads>>>(T(1.0), iters / 8, static_cast<T *>(sink));  // warm-up
+        cudaEventRecord(e0);
+        k_fma_peak<T><<<blocks, threads>>>(T(1.0), iters, static_cast<T *>(sink));
+        cudaEventRecord(e1);
+        cudaEventSynchronize(e1);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        const double flops = 2.0 * 8 * 16 * double(iters) * blocks * threads;
+        return ms > 0 ? flops / (ms * 1e-3) / 1e12 : 0.0;
+    };
+    const double t32 = run(float(0), 4096), t64 = run(double(0), 256);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(sink);
+    if (tflops_fp32) *tflops_fp32 = t32;
+    if (tflops_fp64) *tflops_fp64 = t64;
+    return cudaGetLastError() == cudaSuccess ? 0 : 2;
+}

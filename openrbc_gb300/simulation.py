@@ -191,6 +191,15 @@ class Simulation:
         """Wait until every queued frame is written (orbc_gpu_flush)."""
         self._check(N.lib().orbc_gpu_flush(self.h))
 
+    def cleanup(self, stray_tolerance: Optional[float] = None) -> int:
+        """delete_lipid (src/cleanup.h:29-91) through orbc_gpu_cleanup; returns
+        the number of lipids removed (survivors are renumbered in order)."""
+        tol = float(self.param.stray_tolerance if stray_tolerance is None else stray_tolerance)
+        removed = C.c_int64()
+        self._check(N.lib().orbc_gpu_cleanup(self.h, tol, C.byref(removed)))
+        self.n -= removed.value
+        return removed.value
+
     def save_checkpoint(self, path: str):
         self._check(N.lib().orbc_gpu_save_checkpoint(self.h, str(path).encode()))
 

@@ -285,6 +285,25 @@ def rdf(x, type, type_a=-1, type_b=-1, dr=0.1, nbins=10000, rcut=0.0, centre=(0.
     return counts, int(n), dropped.value
 
 
+def cleanup_marks(x, type, cell3, sys, nc3, L3, mingen=4, tol=2.5):
+    """delete_lipid's marking rule with grid-cell centroids as generators
+    (orc_cleanup_marks; src/cleanup.h:40-59).  Returns (keep flags, removed)."""
+    x = np.ascontiguousarray(x, np.float64).reshape(-1, 3)
+    t = np.ascontiguousarray(type, np.int32)
+    tl = np.ascontiguousarray(cell3, np.int32).reshape(-1, 3)
+    sy = np.ascontiguousarray(sys, np.int32)
+    nt = np.ascontiguousarray(nc3, np.int32).reshape(-1, 3)
+    Lb = np.ascontiguousarray(L3, np.float64).reshape(-1, 3)
+    keep = np.zeros(len(x), np.int32)
+    L = lib()
+    L.orc_cleanup_marks.restype = C.c_int64
+    vp = C.c_void_p
+    r = L.orc_cleanup_marks(x.ctypes.data_as(vp), t.ctypes.data_as(vp), tl.ctypes.data_as(vp), sy.ctypes.data_as(vp),
+                            C.c_int64(len(x)), C.c_int(len(nt)), nt.ctypes.data_as(vp), Lb.ctypes.data_as(vp),
+                            C.c_int(mingen), C.c_double(tol), keep.ctypes.data_as(vp))
+    return keep.astype(bool), int(r)
+
+
 def thermo(st: State) -> dict:
     th = OrcThermoC()
     lib().orc_thermo_f64(C.byref(st._c()), C.byref(th))

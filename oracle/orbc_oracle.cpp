@@ -21,9 +21,11 @@
 #include "orbc_oracle.h"
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <vector>
 #ifdef _OPENMP
 #include <omp.h>
@@ -914,6 +916,123 @@ int orc_minimize_f64(orc_system *s, int nsteps, double dr_opt, double dn_opt, or
     }
     if (th) orc_thermo_f64(s, th);
     return 0;
+}
+
+int64_t orc_cleanup_marks(const double *x3, const int *type, const int *cell3, const int *sys, int64_t n, int nsys,
+                          const int *nc3, const double *L3, int mingen, double tol, int *keep) {
+    const int lloyd = 4;
+    std::vector<int64_t> cb(static_cast<size_t>(nsys) + 1, 0);
+    for (int s = 0; s < nsys; ++s)
+        cb[size_t(s) + 1] = cb[size_t(s)] + int64_t(nc3[3 * s]) * nc3[3 * s + 1] * nc3[3 * s + 2];
+    auto gid = [&](int s, const int t[3]) {
+        return cb[size_t(s)] + t[0] + int64_t(nc3[3 * s]) * (t[1] + int64_t(nc3[3 * s + 1]) * t[2]);
+    };
+    struct Gen {
+        double c[3] = {0, 0, 0};
+        double w = 0;  // > 0: a generator
+    };
+    std::map<int64_t, Gen> gen;
+    for (int64_t i = 0; i < n; ++i) {
+        keep[i] = 1;
+        if (type[i] != 0) continue;
+        Gen &g = gen[gid(sys[i], &cell3[3 * i])];
+        for (int d = 0; d < 3; ++d) g.c[d] += x3[3 * i + d];
+        g.w += 1;
+    }
+    for (auto &kv : gen) {
+        for (int d = 0; d < 3; ++d) kv.second.c[d] /= kv.second.w;
+        if (kv.second.w < mingen) kv.second.w = -1;
+    }
+    std::vector<int64_t> aff(static_cast<size_t>(n), -1);
+    std::vector<double> d2(static_cast<size_t>(n), -1.0);
+    for (int it = 0; it <= lloyd; ++it) {
+        if (it > 0) {  // every generator moves by the mean minimum-image offset of its members
+            std::map<int64_t, Gen> acc;
+            for (int64_t i = 0; i < n; ++i)
+                if (aff[size_t(i)] >= 0) {
+                    const Gen &cg = gen[aff[size_t(i)]];
+                    Gen &g = acc[aff[size_t(i)]];
+                    for (int d = 0; d < 3; ++d) {
+                        double q = x3[3 * i + d] - cg.c[d];
+                        const double L = L3[3 * sys[i] + d];
+                        if (L > 0) q -= L * std::rint(q / L);
+                        g.c[d] += q;
+                    }
+                    g.w += 1;
+                }
+            for (auto &kv : gen) {
+                if (!(kv.second.w > 0)) continue;
+                auto f = acc.find(kv.first);
+                if (f == acc.end() || f->second.w < mingen) {  // too few members: dissolved
+                    kv.second.w = -1;
+                    continue;
+                }
+                for (int d = 0; d < 3; ++d) kv.second.c[d] += f->second.c[d] / f->second.w;
+                kv.second.w = f->second.w;
+            }
+        }
+        for (int64_t i = 0; i < n; ++i) {
+            if (type[i] != 0) continue;
+            const int s = sys[i];
+            int64_t best_g = -1;
+            double best = 0;
+            for (int rad = 1; rad <= 2 && best_g < 0; ++rad)
+                for (int dz = -rad; dz <= rad; ++dz)
+                    for (int dy = -rad; dy <= rad; ++dy)
+                        for (int dx = -rad; dx <= rad; ++dx) {
+                            int t[3] = {cell3[3 * i] + dx, cell3[3 * i + 1] + dy, cell3[3 * i + 2] + dz};
+                            bool ok = true;
+                            for (int d = 0; d < 3; ++d) {
+                                const int nt = nc3[3 * s + d];
+                                if (L3[3 * s + d] > 0)
+                                    t[d] = ((t[d] % nt) + nt) % nt;
+                                else
+                                    ok = ok && t[d] >= 0 && t[d] < nt;
+                            }
+                            if (!ok) continue;
+                            const int64_t g = gid(s, t);
+                            auto f = gen.find(g);
+                            if (f == gen.end() || !(f->second.w > 0)) continue;
+                            double r2 = 0;
+                            for (int d = 0; d < 3; ++d) {
+                                double q = x3[3 * i + d] - f->second.c[d];
+                                const double L = L3[3 * s + d];
+                                if (L > 0) q -= L * std::rint(q / L);
+                                r2 += q * q;
+                            }
+                            if (best_g < 0 || r2 < best || (r2 == best && g < best_g)) {
+                                best = r2;
+                                best_g = g;
+                            }
+                        }
+            aff[size_t(i)] = best_g;
+            d2[size_t(i)] = best;
+        }
+    }
+    std::map<int64_t, std::vector<int64_t>> members;
+    int64_t removed = 0;
+    for (int64_t i = 0; i < n; ++i) {
+        if (type[i] != 0) continue;
+        if (aff[size_t(i)] < 0) {  // no generator within two cells: a stray
+            keep[i] = 0;
+            ++removed;
+        } else {
+            members[aff[size_t(i)]].push_back(i);
+        }
+    }
+    for (auto &kv : members) {
+        if (int64_t(kv.second.size()) < mingen) continue;  // no statistics: all kept
+        std::vector<double> v;
+        for (int64_t i : kv.second) v.push_back(d2[size_t(i)]);
+        std::sort(v.begin(), v.end());
+        const double thr = v[v.size() / 2] * tol * tol;
+        for (int64_t i : kv.second)
+            if (!(d2[size_t(i)] < thr)) {
+                keep[i] = 0;
+                ++removed;
+            }
+    }
+    return removed;
 }
 
 int orc_thermo_f64(const orc_system *s, orc_thermo *th) {

@@ -120,6 +120,23 @@ void orc_assign_temperature(orc_system *s, double kT, uint64_t seed);
 int64_t orc_rdf(const double *x3, const int *type, int64_t n, int type_a, int type_b, double dr, int nbins,
                 double rcut, const double *centre3, const double *L3, int single, uint64_t *counts, int64_t *dropped);
 
+/* delete_lipid's marking rule (src/cleanup.h:40-59) with the GPU's
+ * stand-in for the Voronoi cells: generators start as the lipid centroids of
+ * the partition units (cell3[3i] = unit coordinates of particle i -- the GPU
+ * uses 2 x 2 x 2 bricks of grid cells -- in system sys[i], nc3[3s] units per
+ * axis) holding at least mingen lipids; each lipid is affiliated with the
+ * nearest generator homed in the units within one unit (then two; none: a
+ * stray, removed), ties to the lower home unit (numbered x fastest, systems
+ * in order), with the minimum image on axes where
+ * L3[3s + d] > 0; four Lloyd updates (each generator moves by the mean
+ * minimum-image offset of its members, generators left with fewer than
+ * mingen members are dissolved, re-affiliate) follow; per generator with at least mingen members the
+ * threshold is the sorted dr2[count / 2] times tol^2 and a lipid is kept when
+ * dr2 < threshold.  Proteins are always kept.  keep[n] receives 0/1; returns
+ * the number removed.  FP64. */
+int64_t orc_cleanup_marks(const double *x3, const int *type, const int *cell3, const int *sys, int64_t n, int nsys,
+                          const int *nc3, const double *L3, int mingen, double tol, int *keep);
+
 /* Temperature, area and volume of the current state. */
 int orc_thermo_f64(const orc_system *s, orc_thermo *th);
 
