@@ -112,6 +112,35 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.samples)}
 
 
+TRAFFIC_PROFILE = "profiles/k_step_langevin_lite_float_rbc1M.md"
+
+
+def profiled_traffic_per_particle():
+    """DRAM bytes per particle of one launch of the step kernel, from the
+    committed ncu summary (the capture cannot run inside the benchmark)."""
+    path = os.path.join(ROOT, TRAFFIC_PROFILE)
+    try:
+        with open(path) as f:
+            for line in f:
+                if "traffic_bytes_per_particle:" in line:
+                    return float(line.split("traffic_bytes_per_particle:")[1].split("|")[0].strip())
+    except OSError:
+        pass
+    return None
+
+
+def fma_peaks(L):
+    """Measured FP32 / FP64 FMA throughput of this GPU (TFLOP/s)."""
+    import ctypes as C
+    a, b = C.c_double(), C.c_double()
+    try:
+        if L.orbc_gpu_fma_peak(C.byref(a), C.byref(b)) == 0:
+            return a.value, b.value
+    except Exception:
+        pass
+    return None, None
+
+
 def measured_peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(path):
@@ -200,6 +229,8 @@ def main():
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default skin / kernel form")
+    ap.add_argument("--skin", type=float, default=None, help="neighbour skin when not autotuning")
+    ap.add_argument("--form", type=int, default=0, help="kernel form 0..7 when not autotuning")
     args = ap.parse_args()
     rank, ws = dist_setup()
     if args.impl == "reference":
@@ -216,7 +247,7 @@ def main():
         f"({time.perf_counter() - t_gen:.1f} s)")
 
     # ---- mixed precision, device-resident
-    sim = make_sim(w, "mixed")
+    sim = make_sim(w, "mixed", skin=args.skin if args.skin is not None else SKIN, kernel_variant=args.form)
     f_mixed, _, _ = sim.forces()
     tune = None
     if not args.no_autotune:
@@ -273,7 +304,8 @@ def main():
         e2e_s = allreduce_max(time.perf_counter() - t0, ws)
         e2e = {"value": ws * n * e2e_steps / e2e_s, "unit": "particle-steps/s",
                "h2d_bytes_per_step": 4 * 3 * 8 * n, "d2h_bytes_per_step": 4 * 3 * 8 * n, "steps": e2e_steps,
-               "note": "per step: orbc_gpu_set_state (pinned H2D of x, n, v, o; forces a neighbour rebuild) + "
+               "note": "per step: orbc_gpu_set_state (pinned H2D of x, n, v, o; the list is rebuilt only when a "
+                       "particle moved more than skin/2) + "
                        "orbc_gpu_step(1) + orbc_gpu_download (D2H of x, n, v, o)"}
         log(f"e2e: {e2e['value']:.4e} particle-steps/s")
 
@@ -282,11 +314,20 @@ def main():
     achieved = BYTES_PER_PSTEP * n / (kt * 1e-3) / 1e9
     pairs = prof["pairs_in_cutoff"]
     flops = 0.5 * pairs * FLOP_PER_PAIR * n
+    tpp = profiled_traffic_per_particle()
+    fma32, fma64 = fma_peaks(L)
+    alu_tf = flops / (kt * 1e-3) / 1e12
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "traffic": None, "kernel": "k_step_langevin<float>", "kernel_ms": kt,
+            "traffic": tpp * n if tpp else None, "kernel": "k_step_langevin_lite<float>", "kernel_ms": kt,
+            "bytes_per_particle_step": BYTES_PER_PSTEP,
+            "traffic_source": f"{TRAFFIC_PROFILE}: ncu dram__bytes_read.sum + dram__bytes_write.sum of one "
+                              f"launch on the 1.0M-lipid cell, {tpp} B per particle, scaled to {n} particles",
             "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
-            "alu": {"achieved_tflops": flops / (kt * 1e-3) / 1e12,
-                    "unit": "TFLOP/s (FP32, algorithmic: 106 flop per pair, half the list partners inside rc)"}}
+            "alu": {"achieved": alu_tf, "peak": fma32, "frac": (alu_tf / fma32) if fma32 else None,
+                    "unit": "TFLOP/s FP32",
+                    "counts": "106 flop per interacting pair (src/compute_pairwise.h:64-65,129), "
+                              "half the inner list entries",
+                    "peak_source": "orbc_gpu_fma_peak on this GPU (FFMA chains, all SMs)", "fp64_peak": fma64}}
     line = {"metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",

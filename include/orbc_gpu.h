@@ -148,8 +148,10 @@ int orbc_gpu_upload_batch(orbc_handle *h, int nsys, const orbc_system_desc *sys,
 
 /* Overwrite positions / orientations / velocities / angular velocities of
  * the uploaded particles (same order as the upload) without re-sending the
- * topology; forces a neighbour rebuild.  Used when the host containers stay
- * the source of truth between steps. */
+ * topology.  Particles within skin/2 of where the current neighbour list was
+ * built keep their cell; if any moved farther, the list is rebuilt before the
+ * next force evaluation.  Used when the host containers stay the source of
+ * truth between steps. */
 int orbc_gpu_set_state(orbc_handle *h, const double *x3, const double *n3, const double *v3, const double *o3);
 
 /* nsteps of the loop body of src/openrbc.cpp:189-242 (pair forces, bonds,

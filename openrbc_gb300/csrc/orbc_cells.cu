@@ -559,39 +559,64 @@ __global__ void k_set_state(KArgs<R> a, const double *x, const double *nv, const
                             int64_t nhome) {
     using T4 = typename Vec<R>::T4;
     const int cur = __ldcg(&a.S->cur), lp = __ldcg(&a.S->lp);
-    int out = 0;
+    int out = 0, moved = 0;
     for (int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; k < nhome; k += int64_t(gridDim.x) * blockDim.x) {
         const int p = a.slot_of_home[k];
         const SysDev &sd = a.sys[a.blk_sys[p / SYS_PAD]];
         T4 q = a.pos[cur][p];
-        {
-            const int c0 = a.cell[lp][p];  // the next rebin clears only the new cells
-            a.ranges[sd.cell_base + cell_code(sd, cx_of(c0), cy_of(c0), cz_of(c0))] = make_int2(0, 0);
-        }
-        int cc[3];
-        R off[3];
+        // A particle still within skin/2 of where the list was built keeps its
+        // cell (the list's shift codes stay valid) and no rebuild is needed:
+        // the offset is taken from that cell's centre (minimum image on
+        // periodic axes).  Otherwise it is binned afresh and the list rebuilt.
+        const int c0 = a.cell[lp][p];
+        const int cc0[3] = {cx_of(c0), cy_of(c0), cz_of(c0)};
+        const T4 xr = a.xref[lp][p];
+        const R xrv[3] = {xr.x, xr.y, xr.z};
+        R keep[3];
+        R md2 = 0;
         for (int d = 0; d < 3; ++d) {
-            const double xd = x[3 * k + d];
-            const int cu = int(floor(__ddiv_rn(__dsub_rn(xd, sd.lo[d]), sd.Lc[d])));
-            int c = cu;
+            const double center = __dadd_rn(sd.lo[d], __dmul_rn(double(cc0[d]) + 0.5, sd.Lc[d]));
+            double u = __dsub_rn(x[3 * k + d], center);
             if (sd.per[d]) {
-                c %= sd.nc[d];
-                if (c < 0) c += sd.nc[d];
-            } else {
-                c = min(max(cu, 0), sd.nc[d] - 1);
-                if (c != cu) out = 1;
+                const double L = double(sd.nc[d]) * sd.Lc[d];
+                u -= L * rint(u / L);
             }
-            const int cref = sd.per[d] ? cu : c;
-            const double center = __dadd_rn(sd.lo[d], __dmul_rn(double(cref) + 0.5, sd.Lc[d]));
-            off[d] = R(__dsub_rn(xd, center));
-            cc[d] = c;
+            keep[d] = R(u);
+            md2 += (keep[d] - xrv[d]) * (keep[d] - xrv[d]);
         }
-        q.x = off[0];
-        q.y = off[1];
-        q.z = off[2];
-        a.pos[cur][p] = q;
-        a.xref[lp][p] = q;
-        a.cell[lp][p] = cpack(cc[0], cc[1], cc[2]);
+        if (md2 <= a.skin_half2) {
+            q.x = keep[0];
+            q.y = keep[1];
+            q.z = keep[2];
+            a.pos[cur][p] = q;
+        } else {
+            moved = 1;
+            a.ranges[sd.cell_base + cell_code(sd, cc0[0], cc0[1], cc0[2])] = make_int2(0, 0);
+            int cc[3];
+            R off[3];
+            for (int d = 0; d < 3; ++d) {
+                const double xd = x[3 * k + d];
+                const int cu = int(floor(__ddiv_rn(__dsub_rn(xd, sd.lo[d]), sd.Lc[d])));
+                int c = cu;
+                if (sd.per[d]) {
+                    c %= sd.nc[d];
+                    if (c < 0) c += sd.nc[d];
+                } else {
+                    c = min(max(cu, 0), sd.nc[d] - 1);
+                    if (c != cu) out = 1;
+                }
+                const int cref = sd.per[d] ? cu : c;
+                const double center = __dadd_rn(sd.lo[d], __dmul_rn(double(cref) + 0.5, sd.Lc[d]));
+                off[d] = R(__dsub_rn(xd, center));
+                cc[d] = c;
+            }
+            q.x = off[0];
+            q.y = off[1];
+            q.z = off[2];
+            a.pos[cur][p] = q;
+            a.xref[lp][p] = q;
+            a.cell[lp][p] = cpack(cc[0], cc[1], cc[2]);
+        }
         T4 t = a.nrm[cur][p];
         t.x = R(nv[3 * k]);
         t.y = R(nv[3 * k + 1]);
@@ -609,7 +634,7 @@ __global__ void k_set_state(KArgs<R> a, const double *x, const double *nv, const
         a.omg[lp][p] = t;
     }
     if (out) atomicOr(&a.S->error, ERRB_GRID);
-    if (blockIdx.x == 0 && threadIdx.x == 0) a.S->rebuild = 1;
+    if (__syncthreads_or(moved) && threadIdx.x == 0) a.S->rebuild = 1;
 }
 
 template<class R> void launch_set_state(const KArgs<R> &a, const double *x, const double *n, const double *v,

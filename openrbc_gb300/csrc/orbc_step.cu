@@ -652,7 +652,7 @@ template<class R, bool E, int V> __global__ void __launch_bounds__(STEP_BS, (V &
  * k_advance flips the buffers after the kernel.  The temperature is reduced on
  * demand (k_vcom). */
 template<class R, int V>
-__global__ void __launch_bounds__(LITE_BS, (V & 2) ? 12 : 16) k_step_langevin_lite(KArgs<R> a) {
+__global__ void __launch_bounds__(LITE_BS, 16) k_step_langevin_lite(KArgs<R> a) {
     using T4 = typename Vec<R>::T4;
     __shared__ T4 sh[27];
     init_shift<R>(sh);

@@ -296,6 +296,7 @@ def test_list_build_forms_find_the_same_pairs():
             upload_rbc(s, w)
             s.step(7)
             s.set_state(w["x"], w["n"], w["v"], w["o"])
+            s.rebuild()
             counts, lst = s.neighbors()
         sets.append((counts, lst))
     assert np.array_equal(sets[0][0], sets[1][0])
