@@ -312,18 +312,18 @@ template<class R> __global__ void __launch_bounds__(128) k_nlist(KArgs<R> a, int
         // this slot's column; skin-shell entries fill rows cap-1, cap-2, ...
         int nin = 0, nout = 0, total = 0;
         // Candidate j seen from i's cell: o_j + d * Lc (d = cell_j - cell_i);
-        // x_i - x_j = o_i - (o_j + d * Lc).  Each operation is rounded once,
-        // in the same order by both list-build forms.
+        // x_i - x_j = o_i - (o_j + d * Lc).  Both list-build forms use these
+        // two functions, so they accept the same pairs.
         auto shifted = [&](const T4 &q, int dx, int dy, int dz) {
             T4 r = q;
-            r.x = add_rn(q.x, mul_rn(R(dx), L[0]));
-            r.y = add_rn(q.y, mul_rn(R(dy), L[1]));
-            r.z = add_rn(q.z, mul_rn(R(dz), L[2]));
+            r.x = q.x + R(dx) * L[0];
+            r.y = q.y + R(dy) * L[1];
+            r.z = q.z + R(dz) * L[2];
             return r;
         };
         auto dist2 = [&](const T4 &pi, const T4 &qs) {
-            const R ex = sub_rn(pi.x, qs.x), ey = sub_rn(pi.y, qs.y), ez = sub_rn(pi.z, qs.z);
-            return add_rn(add_rn(mul_rn(ex, ex), mul_rn(ey, ey)), mul_rn(ez, ez));
+            const R ex = pi.x - qs.x, ey = pi.y - qs.y, ez = pi.z - qs.z;
+            return ex * ex + ey * ey + ez * ez;
         };
         auto test = [&](int j, const T4 &q, int dx, int dy, int dz) {
             const int tj = w_type(wbits(q.w));
@@ -556,11 +556,11 @@ template<class R> void launch_rebuild(const KArgs<R> &a, cudaStream_t st, bool g
 /* ------------------------------------------------------------------------- */
 template<class R>
 __global__ void k_set_state(KArgs<R> a, const double *x, const double *nv, const double *v, const double *o,
-                            int64_t nhome) {
+                            int64_t k0, int64_t k1) {
     using T4 = typename Vec<R>::T4;
     const int cur = __ldcg(&a.S->cur), lp = __ldcg(&a.S->lp);
     int out = 0, moved = 0;
-    for (int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; k < nhome; k += int64_t(gridDim.x) * blockDim.x) {
+    for (int64_t k = k0 + blockIdx.x * int64_t(blockDim.x) + threadIdx.x; k < k1; k += int64_t(gridDim.x) * blockDim.x) {
         const int p = a.slot_of_home[k];
         const SysDev &sd = a.sys[a.blk_sys[p / SYS_PAD]];
         T4 q = a.pos[cur][p];
@@ -638,18 +638,20 @@ __global__ void k_set_state(KArgs<R> a, const double *x, const double *nv, const
 }
 
 template<class R> void launch_set_state(const KArgs<R> &a, const double *x, const double *n, const double *v,
-                                        const double *o, int64_t nhome, cudaStream_t st) {
-    k_set_state<R><<<grid_for(nhome), 256, 0, st>>>(a, x, n, v, o, nhome);
+                                        const double *o, int64_t k0, int64_t k1, cudaStream_t st) {
+    k_set_state<R><<<grid_for(k1 - k0), 256, 0, st>>>(a, x, n, v, o, k0, k1);
 }
 
+/* Device state -> caller-order AoS doubles.  One thread per upload index (the
+ * slot comes from slot_of_home), so the writes -- the side that streams to
+ * the host -- are coalesced; the slot-side reads are gathers. */
 template<class R>
-__global__ void k_download(KArgs<R> a, double *x, double *nv, double *v, double *o, double *f, double *t,
-                           double *e) {
+__global__ void k_download(KArgs<R> a, int64_t h0, int64_t h1, double *x, double *nv, double *v, double *o,
+                           double *f, double *t, double *e) {
     using T4 = typename Vec<R>::T4;
     const int cur = __ldcg(&a.S->cur), lp = __ldcg(&a.S->lp);
-    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < a.npad; p += gridDim.x * blockDim.x) {
-        const int h = a.home[lp][p];
-        if (h < 0) continue;
+    for (int64_t h = h0 + blockIdx.x * int64_t(blockDim.x) + threadIdx.x; h < h1; h += int64_t(gridDim.x) * blockDim.x) {
+        const int p = a.slot_of_home[h];
         const SysDev &sd = a.sys[a.blk_sys[p / SYS_PAD]];
         if (x) {
             const T4 q = a.pos[cur][p];
@@ -657,13 +659,13 @@ __global__ void k_download(KArgs<R> a, double *x, double *nv, double *v, double 
             const int cc[3] = {cx_of(c), cy_of(c), cz_of(c)};
             const double off[3] = {double(q.x), double(q.y), double(q.z)};
             for (int d = 0; d < 3; ++d)
-                x[3 * int64_t(h) + d] = __dadd_rn(__dadd_rn(sd.lo[d], __dmul_rn(double(cc[d]) + 0.5, sd.Lc[d])), off[d]);
+                x[3 * h + d] = __dadd_rn(__dadd_rn(sd.lo[d], __dmul_rn(double(cc[d]) + 0.5, sd.Lc[d])), off[d]);
         }
         auto put = [&](double *dst, const T4 &q) {
             if (!dst) return;
-            dst[3 * int64_t(h)] = double(q.x);
-            dst[3 * int64_t(h) + 1] = double(q.y);
-            dst[3 * int64_t(h) + 2] = double(q.z);
+            dst[3 * h] = double(q.x);
+            dst[3 * h + 1] = double(q.y);
+            dst[3 * h + 2] = double(q.z);
         };
         if (nv) put(nv, a.nrm[cur][p]);
         if (v) put(v, a.vel[lp][p]);
@@ -674,9 +676,9 @@ __global__ void k_download(KArgs<R> a, double *x, double *nv, double *v, double 
     }
 }
 
-template<class R> void launch_download(const KArgs<R> &a, double *x, double *n, double *v, double *o, double *f,
-                                       double *t, double *e, cudaStream_t st) {
-    k_download<R><<<grid_for(a.npad), 256, 0, st>>>(a, x, n, v, o, f, t, e);
+template<class R> void launch_download(const KArgs<R> &a, int64_t h0, int64_t h1, double *x, double *n, double *v,
+                                       double *o, double *f, double *t, double *e, cudaStream_t st) {
+    k_download<R><<<grid_for(h1 - h0), 256, 0, st>>>(a, h0, h1, x, n, v, o, f, t, e);
 }
 
 __global__ void k_set_cond(cudaGraphConditionalHandle h, const Scalars *S) {
@@ -713,12 +715,12 @@ template void launch_rebuild_stage<float>(const KArgs<float> &, cudaStream_t, bo
 template void launch_rebuild_stage<double>(const KArgs<double> &, cudaStream_t, bool, int);
 template void launch_rebuild<double>(const KArgs<double> &, cudaStream_t, bool);
 template void launch_set_state<float>(const KArgs<float> &, const double *, const double *, const double *,
-                                      const double *, int64_t, cudaStream_t);
+                                      const double *, int64_t, int64_t, cudaStream_t);
 template void launch_set_state<double>(const KArgs<double> &, const double *, const double *, const double *,
-                                       const double *, int64_t, cudaStream_t);
-template void launch_download<float>(const KArgs<float> &, double *, double *, double *, double *, double *, double *,
-                                     double *, cudaStream_t);
-template void launch_download<double>(const KArgs<double> &, double *, double *, double *, double *, double *,
-                                      double *, double *, cudaStream_t);
+                                       const double *, int64_t, int64_t, cudaStream_t);
+template void launch_download<float>(const KArgs<float> &, int64_t, int64_t, double *, double *, double *, double *,
+                                     double *, double *, double *, cudaStream_t);
+template void launch_download<double>(const KArgs<double> &, int64_t, int64_t, double *, double *, double *,
+                                      double *, double *, double *, double *, cudaStream_t);
 
 }  // namespace orbc

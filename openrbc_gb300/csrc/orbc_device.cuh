@@ -216,10 +216,11 @@ cudaError_t launch_rdf(const double *x3, const int *type, int n, const double ce
                        unsigned long long *dropped, void *work, cudaStream_t st);
 template<class R> void launch_assign_temperature(const KArgs<R> &a, double kT, uint64_t seed, cudaStream_t st);
 
+// upload indices [k0, k1) of the caller-order AoS arrays (full-size base pointers)
 template<class R> void launch_set_state(const KArgs<R> &a, const double *x, const double *n, const double *v,
-                                        const double *o, int64_t nhome, cudaStream_t st);
-template<class R> void launch_download(const KArgs<R> &a, double *x, double *n, double *v, double *o, double *f,
-                                       double *t, double *e, cudaStream_t st);
+                                        const double *o, int64_t k0, int64_t k1, cudaStream_t st);
+template<class R> void launch_download(const KArgs<R> &a, int64_t h0, int64_t h1, double *x, double *n, double *v,
+                                       double *o, double *f, double *t, double *e, cudaStream_t st);
 void launch_set_cond(cudaGraphConditionalHandle h, Scalars *S, cudaStream_t st);
 void launch_morton(const double *p3, int64_t n, const double *bsize3, uint32_t *keys, cudaStream_t st);
 // LSD radix sort of (key, index) pairs, stable; returns the buffer index (0/1) holding the result.

@@ -338,6 +338,10 @@ template<class R> class Engine : public EngineBase {
         if (ev1) cudaEventDestroy(ev1);
         for (cudaEvent_t &e : fpack)
             if (e) cudaEventDestroy(e);
+        for (cudaEvent_t &e : xev)
+            if (e) cudaEventDestroy(e);
+        for (cudaEvent_t &e : pev)
+            if (e) cudaEventDestroy(e);
         if (cs) cudaStreamDestroy(cs);
         if (st) cudaStreamDestroy(st);
     }
@@ -350,6 +354,8 @@ template<class R> class Engine : public EngineBase {
         CK(cudaEventCreate(&ev0));
         CK(cudaEventCreate(&ev1));
         for (cudaEvent_t &e : fpack) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        for (cudaEvent_t &e : xev) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        for (cudaEvent_t &e : pev) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
         CK(cudaGetDevice(&device));
         return ORBC_OK;
     }
@@ -658,14 +664,23 @@ template<class R> class Engine : public EngineBase {
     int set_state(const double *x3, const double *n3, const double *v3, const double *o3) override {
         if (!uploaded) return fail(ORBC_ERR_STATE, "set_state before upload");
         if (!x3 || !n3 || !v3 || !o3) return fail(ORBC_ERR_ARG, "set_state: all four arrays are required");
-        const size_t bytes = size_t(nhome) * 3 * sizeof(double);
         double *d = stage.p;
-        CK(cudaMemcpyAsync(d, x3, bytes, cudaMemcpyHostToDevice, st));
-        CK(cudaMemcpyAsync(d + 3 * nhome, n3, bytes, cudaMemcpyHostToDevice, st));
-        CK(cudaMemcpyAsync(d + 6 * nhome, v3, bytes, cudaMemcpyHostToDevice, st));
-        CK(cudaMemcpyAsync(d + 9 * nhome, o3, bytes, cudaMemcpyHostToDevice, st));
-        launch_set_state<R>(a, d, d + 3 * nhome, d + 6 * nhome, d + 9 * nhome, nhome, st);
+        const double *src[4] = {x3, n3, v3, o3};
+        // chunked: the copy stream moves chunk c + 1 while the step stream converts chunk c
+        const int nch = nhome >= (int64_t(1) << 20) ? NXCH : 1;
+        CK(cudaEventRecord(pev[0], st));  // earlier work on the staging buffer
+        CK(cudaStreamWaitEvent(cs, pev[0], 0));
+        for (int c = 0; c < nch; ++c) {
+            const int64_t k0 = nhome * c / nch, k1 = nhome * (c + 1) / nch;
+            for (int q = 0; q < 4; ++q)
+                CK(cudaMemcpyAsync(d + 3 * (nhome * q + k0), src[q] + 3 * k0, size_t(k1 - k0) * 3 * sizeof(double),
+                                   cudaMemcpyHostToDevice, cs));
+            CK(cudaEventRecord(xev[c], cs));
+            CK(cudaStreamWaitEvent(st, xev[c], 0));
+            launch_set_state<R>(a, d, d + 3 * nhome, d + 6 * nhome, d + 9 * nhome, k0, k1, st);
+        }
         launch_vcom<R>(a, st);  // temperature and lipid mean of the new velocities
+        CK(cudaStreamSynchronize(cs));  // the caller may reuse its arrays on return
         CK(cudaGetLastError());
         nh_primed = false;
         vcom_valid = true;
@@ -859,7 +874,7 @@ template<class R> class Engine : public EngineBase {
         const int carried = (P.integrator == ORBC_INT_NOSE_HOOVER && nh_primed) ? 1 : 0;
         if (carried) {
             double *dd = stage.p;
-            launch_download<R>(a, nullptr, nullptr, nullptr, nullptr, dd, dd + m, nullptr, st);
+            launch_download<R>(a, 0, nhome, nullptr, nullptr, nullptr, nullptr, dd, dd + m, nullptr, st);
             CK(cudaGetLastError());
             CK(cudaMemcpyAsync(buf.data() + 4 * m, dd, 2 * m * sizeof(double), cudaMemcpyDeviceToHost, st));
         }
@@ -961,8 +976,10 @@ template<class R> class Engine : public EngineBase {
     }
     int rebuild_launches() const { return 1 + 3 * passes + 1 + 1; }
 
-    int capture_graph(int steps_per_graph) {
-        drop_graph();
+    /* Capture steps_per_graph steps into *exec (cond: the rebuild sits behind
+     * a conditional node; otherwise the rebuild kernels are device-gated). */
+    int capture_graph(int steps_per_graph, cudaGraphExec_t *exec, bool *cond) {
+        cudaGraphExec_t gexec = nullptr;
         cudaGraph_t g = nullptr;
         // conditional rebuild: [pre] -> set_cond -> IF{rebuild} -> [mesh] -> step kernel
         bool ok = cudaGraphCreate(&g, 0) == cudaSuccess;
@@ -978,11 +995,11 @@ template<class R> class Engine : public EngineBase {
                 }
                 if (P.integrator == ORBC_INT_NOSE_HOOVER) launch_nh_initial<R>(a, st);
                 launch_set_cond(hc, a.S, st);
-                cudaStreamCaptureStatus cs;
+                cudaStreamCaptureStatus cst;
                 cudaGraph_t cg;
                 const cudaGraphNode_t *deps = nullptr;
                 size_t nd = 0;
-                if (cudaStreamGetCaptureInfo(st, &cs, nullptr, &cg, &deps, nullptr, &nd) != cudaSuccess) {
+                if (cudaStreamGetCaptureInfo(st, &cst, nullptr, &cg, &deps, nullptr, &nd) != cudaSuccess) {
                     ok = false;
                     break;
                 }
@@ -1023,15 +1040,15 @@ template<class R> class Engine : public EngineBase {
         cudaGetLastError();
         if (g) cudaGraphDestroy(g);
         if (ok) {
-            graph_cond = true;
-            graph_steps = steps_per_graph;
+            *exec = gexec;
+            *cond = true;
             return ORBC_OK;
         }
         // fallback: plain capture with device-gated rebuild kernels
         if (gexec) cudaGraphExecDestroy(gexec);
         gexec = nullptr;
-        cudaStreamCaptureStatus cs;
-        if (cudaStreamIsCapturing(st, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone) {
+        cudaStreamCaptureStatus cst;
+        if (cudaStreamIsCapturing(st, &cst) == cudaSuccess && cst != cudaStreamCaptureStatusNone) {
             cudaGraph_t junk;
             cudaStreamEndCapture(st, &junk);
             if (junk) cudaGraphDestroy(junk);
@@ -1043,8 +1060,8 @@ template<class R> class Engine : public EngineBase {
         CK(cudaStreamEndCapture(st, &g));
         CK(cudaGraphInstantiate(&gexec, g, 0));
         cudaGraphDestroy(g);
-        graph_cond = false;
-        graph_steps = steps_per_graph;
+        *exec = gexec;
+        *cond = false;
         return ORBC_OK;
     }
 
@@ -1071,14 +1088,20 @@ template<class R> class Engine : public EngineBase {
         }
         CK(cudaEventRecord(ev0, st));
         if (P.use_graph && nsteps > 0) {
-            const int G = 4;
+            const int G = 4;  // steps per graph launch; single steps use a one-step graph
             if (!gexec) {
-                int rc = capture_graph(G);
+                int rc = capture_graph(G, &gexec, &graph_cond);
+                if (rc) return rc;
+                graph_steps = G;
+            }
+            if (nsteps % G && !gexec1) {
+                bool c1 = false;
+                int rc = capture_graph(1, &gexec1, &c1);
                 if (rc) return rc;
             }
             int k = 0;
             for (; k + graph_steps <= nsteps; k += graph_steps) CK(cudaGraphLaunch(gexec, st));
-            for (; k < nsteps; ++k) enqueue_step(true);
+            for (; k < nsteps; ++k) CK(cudaGraphLaunch(gexec1, st));
         } else {
             for (int k = 0; k < nsteps; ++k) enqueue_step(true);
         }
@@ -1111,14 +1134,22 @@ template<class R> class Engine : public EngineBase {
         if (!uploaded) return fail(ORBC_ERR_STATE, "download before upload");
         double *d = stage.p;
         const size_t m = size_t(nhome) * 3;
-        launch_download<R>(a, x3 ? d : nullptr, n3 ? d + m : nullptr, v3 ? d + 2 * m : nullptr,
-                           o3 ? d + 3 * m : nullptr, nullptr, nullptr, nullptr, st);
-        CK(cudaGetLastError());
-        if (x3) CK(cudaMemcpyAsync(x3, d, m * sizeof(double), cudaMemcpyDeviceToHost, st));
-        if (n3) CK(cudaMemcpyAsync(n3, d + m, m * sizeof(double), cudaMemcpyDeviceToHost, st));
-        if (v3) CK(cudaMemcpyAsync(v3, d + 2 * m, m * sizeof(double), cudaMemcpyDeviceToHost, st));
-        if (o3) CK(cudaMemcpyAsync(o3, d + 3 * m, m * sizeof(double), cudaMemcpyDeviceToHost, st));
-        CK(cudaStreamSynchronize(st));
+        double *dst[4] = {x3, n3, v3, o3};
+        // chunked: the copy stream moves chunk c to the host while the step stream converts chunk c + 1
+        const int nch = nhome >= (int64_t(1) << 20) ? NXCH : 1;
+        for (int c = 0; c < nch; ++c) {
+            const int64_t h0 = nhome * c / nch, h1 = nhome * (c + 1) / nch;
+            launch_download<R>(a, h0, h1, x3 ? d : nullptr, n3 ? d + m : nullptr, v3 ? d + 2 * m : nullptr,
+                               o3 ? d + 3 * m : nullptr, nullptr, nullptr, nullptr, st);
+            CK(cudaGetLastError());
+            CK(cudaEventRecord(xev[c], st));
+            CK(cudaStreamWaitEvent(cs, xev[c], 0));
+            for (int q = 0; q < 4; ++q)
+                if (dst[q])
+                    CK(cudaMemcpyAsync(dst[q] + 3 * h0, d + m * q + 3 * h0, size_t(h1 - h0) * 3 * sizeof(double),
+                                       cudaMemcpyDeviceToHost, cs));
+        }
+        CK(cudaStreamSynchronize(cs));
         return ORBC_OK;
     }
 
@@ -1130,7 +1161,7 @@ template<class R> class Engine : public EngineBase {
         CK(cudaGetLastError());
         double *d = stage.p;
         const size_t m = size_t(nhome) * 3;
-        launch_download<R>(a, nullptr, nullptr, nullptr, nullptr, d, d + m, d + 2 * m, st);
+        launch_download<R>(a, 0, nhome, nullptr, nullptr, nullptr, nullptr, d, d + m, d + 2 * m, st);
         CK(cudaGetLastError());
         if (f3) CK(cudaMemcpyAsync(f3, d, m * sizeof(double), cudaMemcpyDeviceToHost, st));
         if (t3) CK(cudaMemcpyAsync(t3, d + m, m * sizeof(double), cudaMemcpyDeviceToHost, st));
@@ -1275,7 +1306,7 @@ template<class R> class Engine : public EngineBase {
             centre[k] = 0.5 * (d.lo[k] + d.hi[k]);
             L[k] = d.periodic[k] ? d.hi[k] - d.lo[k] : 0.0;
         }
-        launch_download<R>(a, stage.p, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, st);
+        launch_download<R>(a, 0, nhome, stage.p, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, st);
         CK(cudaGetLastError());
         DevBuf<int> td;
         DevBuf<T4> work;
@@ -1643,18 +1674,22 @@ template<class R> class Engine : public EngineBase {
 
     void drop_graph() {
         if (gexec) cudaGraphExecDestroy(gexec);
+        if (gexec1) cudaGraphExecDestroy(gexec1);
         gexec = nullptr;
+        gexec1 = nullptr;
         graph_cond = false;
     }
 
     cudaStream_t st = nullptr, cs = nullptr;  // step stream, frame-copy stream
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, fpack[2] = {nullptr, nullptr};
+    static constexpr int NXCH = 4;  // chunks of the host <-> device state transfers
+    cudaEvent_t xev[NXCH] = {}, pev[1] = {};
     int device = 0;
     FrameWriter fw;
     DevBuf<char> fstage[2];
     DevBuf<int> fmap;                                    // file position of each upload index
     std::shared_ptr<const std::vector<int32_t>> ident;  // (tag, type) pairs in file order
-    cudaGraphExec_t gexec = nullptr;
+    cudaGraphExec_t gexec = nullptr, gexec1 = nullptr;
     bool graph_cond = false;
     int graph_steps = 0;
     bool uploaded = false, nh_primed = false, has_mesh = false, vcom_valid = false;
