@@ -340,8 +340,8 @@ def main():
             "config": {"workload": f"rbc-evans-fung-{n}", "n_particles": n, "n_lipid": args.n_lipid,
                        "anchors": n - args.n_lipid, "bonds": int(len(w["bonds"])), "faces": int(len(w["faces"])),
                        "integrator": "langevin", "dt": DT, "kT": KT,
-                       "skin": tune["chosen"]["skin"] if tune else SKIN,
-                       "kernel_form": tune["chosen"]["variant"] if tune else 0, "precision": "mixed",
+                       "skin": tune["chosen"]["skin"] if tune else (args.skin if args.skin is not None else SKIN),
+                       "kernel_form": tune["chosen"]["variant"] if tune else args.form, "precision": "mixed",
                        "l2": "inputs larger than L2 (state + neighbour list > 1 GB)",
                        "parallelism": f"replicas x{ws}"},
             "fp64": fp64, "mixed_over_fp64": (value / ws / fp64["value"]) if fp64 else None,

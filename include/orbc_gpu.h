@@ -84,11 +84,12 @@ typedef struct {
     double bond_K[ORBC_MAX_BOND_TYPES];
     double bond_r0[ORBC_MAX_BOND_TYPES];
     double bond_R[ORBC_MAX_BOND_TYPES];
-    /* kernel forms 0..7: bit 0 = software-pipelined neighbour pass
+    /* kernel forms 0..15: bit 0 = software-pipelined neighbour pass
        (else 2-way unrolled), bit 1 = non-lipid pair path inlined (else
-       called), bit 2 = neighbour list built by per-particle 27-cell sweeps
-       (else one sweep per warp of its cells' neighbourhood);
-       orbc_gpu_autotune picks it per workload */
+       called), bit 2 = Langevin step kernel compiled for 20 resident blocks
+       per SM (48 registers; else 16 blocks, 64 registers), bit 3 = neighbour
+       list built by per-particle 27-cell sweeps (else per cell of a warp,
+       32 candidates at a time); orbc_gpu_autotune picks it per workload */
     int kernel_variant;
     /* 1: remove each system's mean lipid velocity between the force
        evaluation and the integrator every step, as the disabled call

@@ -414,6 +414,9 @@ template<class R> __global__ void __launch_bounds__(128) k_nlist(KArgs<R> a, int
                         const int gi = i - lane + il;
                         int qin = __shfl_sync(0xffffffffu, cin, il), qout = __shfl_sync(0xffffffffu, cout, il);
                         int qtot = __shfl_sync(0xffffffffu, ctot, il);
+                        uint32_t *col = a.nbr + nbr_index(gi, 0, a.cap);  // row k of gi at col[32 k]
+                        // lipid-lipid pairs (the bulk) take their cutoffs from registers
+                        const float rl2_ll = rl2s[ti * 16], ri2_ll = ri2s[ti * 16];
                         for (int b0 = 0; b0 < nch; b0 += 32) {
                             const int t = b0 + lane;
                             bool acc = false, inner = false;
@@ -422,12 +425,12 @@ template<class R> __global__ void __launch_bounds__(128) k_nlist(KArgs<R> a, int
                                 const int j = s_j[warp][t];
                                 const T4 q = s_pos[warp][t];
                                 const int tj = w_type(wbits(q.w));
-                                const float rl2 = rl2s[ti * 16 + tj];
+                                const float rl2 = tj == 0 ? rl2_ll : rl2s[ti * 16 + tj];
                                 if (j != gi && rl2 > 0.f) {
                                     const R r2 = dist2(pi, q);
                                     if (r2 < R(rl2)) {
                                         acc = true;
-                                        inner = r2 < R(ri2s[ti * 16 + tj]);
+                                        inner = r2 < R(tj == 0 ? ri2_ll : ri2s[ti * 16 + tj]);
                                         ent = uint32_t(j) | (uint32_t(s_code[warp][t]) << NB_SHIFT);
                                     }
                                 }
@@ -435,15 +438,17 @@ template<class R> __global__ void __launch_bounds__(128) k_nlist(KArgs<R> a, int
                             const unsigned ma = __ballot_sync(0xffffffffu, acc);
                             const unsigned mi = __ballot_sync(0xffffffffu, acc && inner);
                             // entries past the capacity are counted, not written
-                            const bool wr = acc && qin + qout + __popc(ma & lt) < a.cap;
-                            const unsigned mw = __ballot_sync(0xffffffffu, wr);
-                            if (wr) {
+                            unsigned mw = ma;
+                            if (qin + qout + __popc(ma) > a.cap)
+                                mw = __ballot_sync(0xffffffffu, acc && qin + qout + __popc(ma & lt) < a.cap);
+                            if ((mw >> lane) & 1u) {
                                 const int row = inner ? qin + __popc(mi & mw & lt)
                                                       : a.cap - 1 - (qout + __popc(~mi & mw & lt));
-                                a.nbr[nbr_index(gi, row, a.cap)] = ent;
+                                col[32 * row] = ent;
                             }
-                            qin += __popc(mi & mw);
-                            qout += __popc(~mi & mw);
+                            const int win = __popc(mi & mw);
+                            qin += win;
+                            qout += __popc(mw) - win;
                             qtot += __popc(ma);
                         }
                         if (lane == il) {

@@ -404,6 +404,7 @@ template<class R> class Engine : public EngineBase {
 
         // ---- per-system grid and slot layout
         hsys.assign(size_t(nsys), SysDev());
+        ngroups_total = 0;
         std::vector<int> sys_of(static_cast<size_t>(n));
         int64_t off = 0;
         uint64_t cbase = 0;
@@ -459,6 +460,9 @@ template<class R> class Engine : public EngineBase {
             }
             const int64_t ns = e - b;
             const int64_t npad_s = std::max<int64_t>(SYS_PAD, (ns + SYS_PAD - 1) / SYS_PAD * SYS_PAD);
+            sd.gbase = ngroups_total;
+            sd.ngrp = int((npad_s / STEP_BS + FIN_GROUP - 1) / FIN_GROUP);
+            ngroups_total += sd.ngrp;
             sd.off = int(off);
             sd.npad = int(npad_s);
             sd.nreal = int(ns);
@@ -599,7 +603,8 @@ template<class R> class Engine : public EngineBase {
         }
         ntiles = sort_tiles(npad);
         if (epart.alloc(size_t(npad)) || faces.alloc(hfaces.size()) || ranges.alloc(size_t(total_cells)) ||
-            soh.alloc(size_t(n)) || blk_sys.alloc(size_t(nb256)) || partial.alloc(size_t(nblk) * NPART) ||
+            soh.alloc(size_t(n)) || blk_sys.alloc(size_t(nb256)) || partial.alloc(size_t(nblk) * NPART) || gpartial.alloc(size_t(ngroups_total) * NPART) ||
+            gcount.alloc(size_t(ngroups_total)) ||
             Sd.alloc(1) || sysd.alloc(size_t(nsys)) || ssd.alloc(size_t(nsys)) || counts.alloc(size_t(256) * ntiles) ||
             dtot.alloc(256) || invd.alloc(size_t(npad)) || ffd.alloc(1) || nnb.alloc(size_t(npad)) ||
             stage.alloc(size_t(n) * 12) || mesh_bs.alloc(hmbs.size()) || mesh_part.alloc(hmbs.size() * 2 + 2))
@@ -629,6 +634,8 @@ template<class R> class Engine : public EngineBase {
         CK(cudaMemcpyAsync(sysd.p, hsys.data(), hsys.size() * sizeof(SysDev), cudaMemcpyHostToDevice, st));
         CK(cudaMemsetAsync(ranges.p, 0, size_t(total_cells) * sizeof(int2), st));
         CK(cudaMemsetAsync(partial.p, 0, size_t(nblk) * NPART * sizeof(double), st));
+        CK(cudaMemsetAsync(gpartial.p, 0, size_t(ngroups_total) * NPART * sizeof(double), st));
+        CK(cudaMemsetAsync(gcount.p, 0, size_t(ngroups_total) * sizeof(unsigned), st));
         CK(cudaMemsetAsync(epart.p, 0, size_t(npad) * sizeof(double), st));
         CK(cudaMemsetAsync(nnb.p, 0, size_t(npad) * sizeof(int), st));
         // other parity copies start equal (gather overwrites them before use)
@@ -1459,12 +1466,14 @@ template<class R> class Engine : public EngineBase {
             }
             return ORBC_OK;
         };
-        // skin x force-kernel form (bits 0-1), then the list-build form (bit 2) at the best pair
-        const int list_form = P.kernel_variant & 4;
+        // skin x force-kernel form (bits 0-1), then at the best pair the
+        // occupancy form (bit 2) and the list-build form (bit 3)
+        const int rest = P.kernel_variant & 12;
         for (double sk : skins)
             for (int var = 0; var < 4; ++var)
-                if ((rc = trial(sk, var | list_form))) return rc;
+                if ((rc = trial(sk, var | rest))) return rc;
         if ((rc = trial(best_skin, best_var ^ 4))) return rc;
+        if ((rc = trial(best_skin, best_var ^ 8))) return rc;
         if (ntrials) *ntrials = nt;
         P.skin = best_skin;
         P.kernel_variant = best_var;
@@ -1604,6 +1613,9 @@ template<class R> class Engine : public EngineBase {
         a.slot_of_home = soh.p;
         a.blk_sys = blk_sys.p;
         a.partial = partial.p;
+        a.gpartial = gpartial.p;
+        a.gcount = gcount.p;
+        a.ngroups = ngroups_total;
         a.S = Sd.p;
         a.sys = sysd.p;
         a.ss = ssd.p;
@@ -1620,8 +1632,8 @@ template<class R> class Engine : public EngineBase {
         a.skin_half2 = R(0.25 * P.skin * P.skin);
         a.seed = P.seed;
         a.rebuild_every = P.rebuild_every;
-        a.variant = P.kernel_variant & 3;
-        a.nlist_lane = (P.kernel_variant >> 2) & 1;
+        a.variant = P.kernel_variant & 7;
+        a.nlist_lane = (P.kernel_variant >> 3) & 1;
         a.carry_forces = P.integrator == ORBC_INT_NOSE_HOOVER ? 1 : 0;
         a.zero_bulk = P.zero_bulk ? 1 : 0;
         a.ff = ffd.p;
@@ -1703,7 +1715,9 @@ template<class R> class Engine : public EngineBase {
     DevBuf<int2> fslot[2];
     DevBuf<uint32_t> skey[2];
     DevBuf<int> sval[2];
-    DevBuf<double> epart, partial, stage;
+    DevBuf<double> epart, partial, stage, gpartial;
+    DevBuf<unsigned> gcount;
+    int ngroups_total = 0;
     DevBuf<int4> faces;
     DevBuf<int2> ranges;
     DevBuf<int> soh, blk_sys, counts, dtot, invd, nnb, mesh_bs;
@@ -1764,7 +1778,7 @@ int orbc_gpu_create(const orbc_params *p, orbc_handle **out) {
     *out = nullptr;
     if (!(p->dt > 0) || p->skin < 0 || (p->precision != ORBC_PREC_FP64 && p->precision != ORBC_PREC_MIXED) ||
         (p->integrator != ORBC_INT_LANGEVIN && p->integrator != ORBC_INT_NOSE_HOOVER) ||
-        (p->kernel_variant < 0 || p->kernel_variant > 7) || (p->zero_bulk != 0 && p->zero_bulk != 1)) {
+        (p->kernel_variant < 0 || p->kernel_variant > 15) || (p->zero_bulk != 0 && p->zero_bulk != 1)) {
         g_last_error = "create: invalid parameters";
         return ORBC_ERR_ARG;
     }

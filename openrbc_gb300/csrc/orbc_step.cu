@@ -410,133 +410,133 @@ __device__ __forceinline__ void bounce_walls(const SysDev &sd, int c, typename V
 
 enum { MODE_LANGEVIN = 0, MODE_NH_FINAL = 1, MODE_NH_INITIAL = 2, MODE_FORCES = 3, MODE_VCOM = 4 };
 
-/* Block partial sums -> per-system totals in the last block (fixed order). */
+/* Block partial sums -> per-system totals, deterministically and without a
+ * serial tail: each block writes its partial; the last block of each group of
+ * FIN_GROUP consecutive blocks of a system (group ticket) sums the group's
+ * partials in block order; the last group to finish (global ticket) sums each
+ * system's group partials in group order and updates the thermostat, the
+ * rebuild flag, the step counter and the buffer parity.  Partial layout:
+ * ke2, epot, max displacement^2, error flags, lipid sum v (3). */
 template<class R>
 __device__ __forceinline__ void finish(const KArgs<R> &a, double ke, double ep, float md2, int flags, int mode,
                                        int count_step, double vx = 0, double vy = 0, double vz = 0) {
-    __shared__ double sk[8], se[8], sv[8][3];
-    __shared__ float sm[8];
-    __shared__ int sf[8];
-    __shared__ bool last;
+    __shared__ double sv[STEP_WARPS][NPART];
+    __shared__ double red[NPART][FIN_GROUP];
+    __shared__ int last, gflags;
+    __shared__ double gmax;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    double v[7] = {ke, ep, double(md2), double(flags), vx, vy, vz};
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-        ke += __shfl_xor_sync(0xffffffffu, ke, o);
-        ep += __shfl_xor_sync(0xffffffffu, ep, o);
-        md2 = fmaxf(md2, __shfl_xor_sync(0xffffffffu, md2, o));
-        flags |= __shfl_xor_sync(0xffffffffu, flags, o);
-        vx += __shfl_xor_sync(0xffffffffu, vx, o);
-        vy += __shfl_xor_sync(0xffffffffu, vy, o);
-        vz += __shfl_xor_sync(0xffffffffu, vz, o);
+        v[0] += __shfl_xor_sync(0xffffffffu, v[0], o);
+        v[1] += __shfl_xor_sync(0xffffffffu, v[1], o);
+        v[2] = fmax(v[2], __shfl_xor_sync(0xffffffffu, v[2], o));
+        v[3] = double(int(v[3]) | int(__shfl_xor_sync(0xffffffffu, v[3], o)));
+        v[4] += __shfl_xor_sync(0xffffffffu, v[4], o);
+        v[5] += __shfl_xor_sync(0xffffffffu, v[5], o);
+        v[6] += __shfl_xor_sync(0xffffffffu, v[6], o);
     }
-    if (lane == 0) {
-        sk[warp] = ke;
-        se[warp] = ep;
-        sm[warp] = md2;
-        sf[warp] = flags;
-        sv[warp][0] = vx;
-        sv[warp][1] = vy;
-        sv[warp][2] = vz;
-    }
+    if (lane == 0)
+        for (int k = 0; k < 7; ++k) sv[warp][k] = v[k];
     __syncthreads();
+    const int blk = blockIdx.x;
+    const int s = a.blk_sys[(blk * STEP_BS) / SYS_PAD];
+    const SysDev &sd = a.sys[s];
+    const int b0 = sd.off / STEP_BS, nbs = sd.npad / STEP_BS;
+    const int gl = (blk - b0) / FIN_GROUP;              // group within the system
+    const int g = sd.gbase + gl;                        // global group
+    const int gb0 = b0 + gl * FIN_GROUP, gn = min(FIN_GROUP, nbs - gl * FIN_GROUP);
+    auto combine = [](int k, double x, double y) {
+        return k == 2 ? fmax(x, y) : (k == 3 ? double(int(x) | int(y)) : x + y);
+    };
     if (threadIdx.x == 0) {
-        double k = 0, e = 0, v0 = 0, v1 = 0, v2 = 0;
-        float m = 0;
-        int fl = 0;
-        for (int w = 0; w < STEP_WARPS; ++w) {
-            k += sk[w];
-            e += se[w];
-            m = fmaxf(m, sm[w]);
-            fl |= sf[w];
-            v0 += sv[w][0];
-            v1 += sv[w][1];
-            v2 += sv[w][2];
-        }
-        double *p = a.partial + int64_t(blockIdx.x) * NPART;
-        p[0] = k;
-        p[1] = e;
-        p[2] = double(m);
-        p[3] = double(fl);
-        p[4] = v0;
-        p[5] = v1;
-        p[6] = v2;
+        double w[7];
+        for (int k = 0; k < 7; ++k) w[k] = sv[0][k];
+        for (int q = 1; q < STEP_WARPS; ++q)
+            for (int k = 0; k < 7; ++k) w[k] = combine(k, w[k], sv[q][k]);
+        double *p = a.partial + int64_t(blk) * NPART;
+        for (int k = 0; k < 7; ++k) p[k] = w[k];
         __threadfence();
-        const unsigned ticket = atomicAdd(&a.S->blk_counter, 1u);
-        last = (ticket == gridDim.x - 1);
+        last = atomicAdd(&a.gcount[g], 1u) == unsigned(gn - 1);
     }
     __syncthreads();
     if (!last) return;
     __threadfence();
-    // per system: one warp per system, lanes stride over the system's blocks
-    for (int s = warp; s < a.nsys; s += STEP_WARPS) {
-        const SysDev &sd = a.sys[s];
-        const int b0 = sd.off / STEP_BS, b1 = (sd.off + sd.npad) / STEP_BS;
-        double k = 0, e = 0, v0 = 0, v1 = 0, v2 = 0;
-        for (int b = b0 + lane; b < b1; b += 32) {
-            k += __ldcg(a.partial + int64_t(b) * NPART);
-            e += __ldcg(a.partial + int64_t(b) * NPART + 1);
-            v0 += __ldcg(a.partial + int64_t(b) * NPART + 4);
-            v1 += __ldcg(a.partial + int64_t(b) * NPART + 5);
-            v2 += __ldcg(a.partial + int64_t(b) * NPART + 6);
+    // group: thread t < gn loads block gb0 + t; fixed-shape tree over FIN_GROUP slots
+    for (int k = 0; k < 7; ++k)
+        for (int t = threadIdx.x; t < FIN_GROUP; t += blockDim.x)
+            red[k][t] = t < gn ? __ldcg(a.partial + int64_t(gb0 + t) * NPART + k) : (k == 2 || k == 3 ? 0.0 : 0.0);
+    __syncthreads();
+    for (int h = FIN_GROUP / 2; h > 0; h >>= 1) {
+        for (int t = threadIdx.x; t < h * 7; t += blockDim.x) {
+            const int k = t / h, u = t % h;
+            red[k][u] = combine(k, red[k][u], red[k][u + h]);
         }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            k += __shfl_xor_sync(0xffffffffu, k, o);
-            e += __shfl_xor_sync(0xffffffffu, e, o);
-            v0 += __shfl_xor_sync(0xffffffffu, v0, o);
-            v1 += __shfl_xor_sync(0xffffffffu, v1, o);
-            v2 += __shfl_xor_sync(0xffffffffu, v2, o);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        double *gp = a.gpartial + int64_t(g) * NPART;
+        for (int k = 0; k < 7; ++k) gp[k] = red[k][0];
+        a.gcount[g] = 0;
+        __threadfence();
+        last = atomicAdd(&a.S->blk_counter, 1u) == unsigned(a.ngroups - 1);
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    // per system: its groups in order (strided sums, then the same tree)
+    for (int q = 0; q < a.nsys; ++q) {
+        const SysDev &sq = a.sys[q];
+        for (int k = 0; k < 7; ++k)
+            for (int t = threadIdx.x; t < FIN_GROUP; t += blockDim.x) {
+                double acc = k == 2 || k == 3 ? 0.0 : 0.0;
+                for (int u = t; u < sq.ngrp; u += FIN_GROUP)
+                    acc = combine(k, acc, __ldcg(a.gpartial + int64_t(sq.gbase + u) * NPART + k));
+                red[k][t] = acc;
+            }
+        __syncthreads();
+        for (int h = FIN_GROUP / 2; h > 0; h >>= 1) {
+            for (int t = threadIdx.x; t < h * 7; t += blockDim.x) {
+                const int k = t / h, u = t % h;
+                red[k][u] = combine(k, red[k][u], red[k][u + h]);
+            }
+            __syncthreads();
         }
-        if (lane == 0) {
-            SysState &ss = a.ss[s];
-            if ((mode == MODE_LANGEVIN || mode == MODE_NH_INITIAL || mode == MODE_VCOM) && sd.nlipid > 0) {
-                ss.vcom[0] = v0 / double(sd.nlipid);
-                ss.vcom[1] = v1 / double(sd.nlipid);
-                ss.vcom[2] = v2 / double(sd.nlipid);
+        if (threadIdx.x == 0) {
+            SysState &ss = a.ss[q];
+            const double k2 = red[0][0], e = red[1][0];
+            if ((mode == MODE_LANGEVIN || mode == MODE_NH_INITIAL || mode == MODE_VCOM) && sq.nlipid > 0) {
+                ss.vcom[0] = red[4][0] / double(sq.nlipid);
+                ss.vcom[1] = red[5][0] / double(sq.nlipid);
+                ss.vcom[2] = red[6][0] / double(sq.nlipid);
             }
             if (mode == MODE_VCOM) {
-                ss.ke2 = k;
+                ss.ke2 = k2;
             } else if (mode == MODE_LANGEVIN || mode == MODE_FORCES) {
-                if (mode == MODE_LANGEVIN) ss.ke2 = k;
+                if (mode == MODE_LANGEVIN) ss.ke2 = k2;
                 ss.epot = e;
             } else {
                 // zeta += dt/2Q (sum m v^2 / 2 - 3/2 N kT)  (src/integrate_nh.h:182-185, :241-244)
-                const double nreal = double(sd.nreal);
-                const double Q = sd.Q > 0 ? sd.Q : 0.01 * nreal;
-                ss.zeta += 0.5 * a.dt / Q * (0.5 * k - 0.5 * 3.0 * nreal * a.kBT);
-                ss.ke2 = k;
+                const double nreal = double(sq.nreal);
+                const double Q = sq.Q > 0 ? sq.Q : 0.01 * nreal;
+                ss.zeta += 0.5 * a.dt / Q * (0.5 * k2 - 0.5 * 3.0 * nreal * a.kBT);
+                ss.ke2 = k2;
                 if (mode == MODE_NH_FINAL) ss.epot = e;
             }
+            // system max displacement and flags feed the global decision
+            gmax = q == 0 ? red[2][0] : fmax(gmax, red[2][0]);
+            gflags = (q == 0 ? 0 : gflags) | int(red[3][0]);
         }
+        __syncthreads();
     }
-    // global max displacement and error flags
-    float m = 0.f;
-    int fl = 0;
-    for (int b = threadIdx.x; b < a.nblk; b += blockDim.x) {
-        m = fmaxf(m, float(__ldcg(a.partial + int64_t(b) * NPART + 2)));
-        fl |= int(__ldcg(a.partial + int64_t(b) * NPART + 3));
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-        fl |= __shfl_xor_sync(0xffffffffu, fl, o);
-    }
-    __syncthreads();
-    if (lane == 0) {
-        sm[warp] = m;
-        sf[warp] = fl;
-    }
-    __syncthreads();
     if (threadIdx.x == 0) {
-        for (int w = 0; w < STEP_WARPS; ++w) {
-            m = fmaxf(m, sm[w]);
-            fl |= sf[w];
-        }
+        const double m = gmax;
+        const int fl = gflags;
         Scalars *S = a.S;
         S->error |= fl;
         if (mode == MODE_LANGEVIN || mode == MODE_NH_INITIAL) {
             S->since_rebuild += 1;
-            if (double(m) > double(a.skin_half2) || (a.rebuild_every > 0 && S->since_rebuild >= a.rebuild_every))
+            if (m > double(a.skin_half2) || (a.rebuild_every > 0 && S->since_rebuild >= a.rebuild_every))
                 S->rebuild = 1;
         }
         if (mode == MODE_LANGEVIN) {
@@ -652,7 +652,7 @@ template<class R, bool E, int V> __global__ void __launch_bounds__(STEP_BS, (V &
  * k_advance flips the buffers after the kernel.  The temperature is reduced on
  * demand (k_vcom). */
 template<class R, int V>
-__global__ void __launch_bounds__(LITE_BS, 16) k_step_langevin_lite(KArgs<R> a) {
+__global__ void __launch_bounds__(LITE_BS, (V & 4) ? 20 : 16) k_step_langevin_lite(KArgs<R> a) {
     using T4 = typename Vec<R>::T4;
     __shared__ T4 sh[27];
     init_shift<R>(sh);
@@ -1040,9 +1040,9 @@ template<class R> __global__ void __launch_bounds__(256) k_mesh(KArgs<R> a) {
  * to 85 registers, instead of called).  The autotuner picks one per workload. */
 template<class R, int V> void step_langevin_v(const KArgs<R> &a, cudaStream_t st, bool energy) {
     if (energy) {
-        k_step_langevin<R, true, V><<<a.nblk, STEP_BS, 0, st>>>(a);
+        k_step_langevin<R, true, V & 3><<<a.nblk, STEP_BS, 0, st>>>(a);
     } else if (a.zero_bulk) {
-        k_step_langevin<R, false, V><<<a.nblk, STEP_BS, 0, st>>>(a);
+        k_step_langevin<R, false, V & 3><<<a.nblk, STEP_BS, 0, st>>>(a);
     } else {
         k_step_langevin_lite<R, V><<<a.npad / LITE_BS, LITE_BS, 0, st>>>(a);
         k_advance<<<1, 1, 0, st>>>(a.S, a.rebuild_every, 1);
@@ -1055,15 +1055,19 @@ template<class R, int V> void nh_final_v(const KArgs<R> &a, cudaStream_t st, boo
         k_nh_final<R, false, V><<<a.nblk, STEP_BS, 0, st>>>(a, 1);
 }
 template<class R> void launch_step_langevin(const KArgs<R> &a, cudaStream_t st, bool energy) {
-    switch (a.variant) {
+    switch (a.variant & 7) {
         case 1: step_langevin_v<R, 1>(a, st, energy); break;
         case 2: step_langevin_v<R, 2>(a, st, energy); break;
         case 3: step_langevin_v<R, 3>(a, st, energy); break;
+        case 4: step_langevin_v<R, 4>(a, st, energy); break;
+        case 5: step_langevin_v<R, 5>(a, st, energy); break;
+        case 6: step_langevin_v<R, 6>(a, st, energy); break;
+        case 7: step_langevin_v<R, 7>(a, st, energy); break;
         default: step_langevin_v<R, 0>(a, st, energy); break;
     }
 }
 template<class R> void launch_nh_final(const KArgs<R> &a, cudaStream_t st, bool energy) {
-    switch (a.variant) {
+    switch (a.variant & 3) {
         case 1: nh_final_v<R, 1>(a, st, energy); break;
         case 2: nh_final_v<R, 2>(a, st, energy); break;
         case 3: nh_final_v<R, 3>(a, st, energy); break;
@@ -1087,7 +1091,7 @@ template<class R, int V> void minimize_v(const KArgs<R> &a, double dr_opt, doubl
     k_advance<<<1, 1, 0, st>>>(a.S, a.rebuild_every, 0);
 }
 template<class R> void launch_minimize(const KArgs<R> &a, double dr_opt, double dn_opt, cudaStream_t st) {
-    switch (a.variant) {
+    switch (a.variant & 3) {
         case 1: minimize_v<R, 1>(a, dr_opt, dn_opt, st); break;
         case 2: minimize_v<R, 2>(a, dr_opt, dn_opt, st); break;
         case 3: minimize_v<R, 3>(a, dr_opt, dn_opt, st); break;

@@ -267,10 +267,10 @@ def test_nose_hoover_mixed_tracks_fp64():
     assert abs(res["mixed"]["temperature"] - res["fp64"]["temperature"]) < 1e-3 * res["fp64"]["temperature"]
 
 
-@pytest.mark.parametrize("variant", [1, 2, 3, 4, 7])
+@pytest.mark.parametrize("variant", [1, 2, 3, 4, 7, 8, 15])
 def test_force_kernel_forms_agree(variant):
     """The force-kernel forms evaluate the same pairs in the same order; the
-    two list-build forms (bit 2) find the same pairs, in another order."""
+    two list-build forms (bit 3) find the same pairs."""
     from openrbc_gb300 import RTParameter
     from openrbc_gb300 import Simulation
     w, table = small_rbc("wlc")
@@ -290,7 +290,7 @@ def test_list_build_forms_find_the_same_pairs():
     from openrbc_gb300 import RTParameter, Simulation
     w, table = small_rbc("wlc")
     sets = []
-    for v in (0, 4):
+    for v in (0, 8):
         p = RTParameter(init="lipid", kBT=1.0, precision="mixed", rseed=5)
         with Simulation(p, bond_table=table, kernel_variant=v) as s:
             upload_rbc(s, w)
@@ -314,7 +314,7 @@ def test_autotune_restores_state_and_keeps_stepping():
         step0 = s.thermo()["step"]
         trials = s.autotune(trial_steps=4)
         after = s.download()
-        assert len(trials) == 21 and all(t["ms_per_step"] > 0 for t in trials)  # 5 skins x 4 forms + list form
+        assert len(trials) == 22 and all(t["ms_per_step"] > 0 for t in trials)  # 5 skins x 4 forms + 2 forms
         assert s.thermo()["step"] == step0
         d = min_image_diff(after[0], before[0], box, (1, 1, 0))
         assert np.abs(d).max() < 1e-5
