@@ -418,26 +418,34 @@ enum { MODE_LANGEVIN = 0, MODE_NH_FINAL = 1, MODE_NH_INITIAL = 2, MODE_FORCES = 
  * rebuild flag, the step counter and the buffer parity.  Partial layout:
  * ke2, epot, max displacement^2, error flags, lipid sum v (3). */
 template<class R>
-__device__ __forceinline__ void finish(const KArgs<R> &a, double ke, double ep, float md2, int flags, int mode,
-                                       int count_step, double vx = 0, double vy = 0, double vz = 0) {
+__device__ __forceinline__ void finish(const KArgs<R> &a, R ke, R ep, float md2, int flags, int mode, int count_step,
+                                       R vx = R(0), R vy = R(0), R vz = R(0)) {
     __shared__ double sv[STEP_WARPS][NPART];
     __shared__ double red[NPART][FIN_GROUP];
     __shared__ int last, gflags;
     __shared__ double gmax;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    double v[7] = {ke, ep, double(md2), double(flags), vx, vy, vz};
+    // Warp level in the working precision (in mixed mode the FP64 pipe would
+    // cost more than the whole force loop) with the maximum and the flags on
+    // integers; from the warp partials on, FP64 in a fixed order.
+    R v[5] = {ke, ep, vx, vy, vz};
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-        v[0] += __shfl_xor_sync(0xffffffffu, v[0], o);
-        v[1] += __shfl_xor_sync(0xffffffffu, v[1], o);
-        v[2] = fmax(v[2], __shfl_xor_sync(0xffffffffu, v[2], o));
-        v[3] = double(int(v[3]) | int(__shfl_xor_sync(0xffffffffu, v[3], o)));
-        v[4] += __shfl_xor_sync(0xffffffffu, v[4], o);
-        v[5] += __shfl_xor_sync(0xffffffffu, v[5], o);
-        v[6] += __shfl_xor_sync(0xffffffffu, v[6], o);
+#pragma unroll
+        for (int k = 0; k < 5; ++k) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
     }
-    if (lane == 0)
-        for (int k = 0; k < 7; ++k) sv[warp][k] = v[k];
+    // md2 >= 0 (or NaN, flagged separately): the bit order is the value order
+    const unsigned wmax = __reduce_max_sync(0xffffffffu, __float_as_uint(md2));
+    const int wfl = int(__reduce_or_sync(0xffffffffu, unsigned(flags)));
+    if (lane == 0) {
+        sv[warp][0] = double(v[0]);
+        sv[warp][1] = double(v[1]);
+        sv[warp][2] = double(__uint_as_float(wmax));
+        sv[warp][3] = double(wfl);
+        sv[warp][4] = double(v[2]);
+        sv[warp][5] = double(v[3]);
+        sv[warp][6] = double(v[4]);
+    }
     __syncthreads();
     const int blk = blockIdx.x;
     const int s = a.blk_sys[(blk * STEP_BS) / SYS_PAD];
@@ -557,9 +565,8 @@ __device__ __forceinline__ void finish(const KArgs<R> &a, double ke, double ep, 
 template<class R, bool E, int V>
 __device__ __forceinline__ void langevin_particle(const KArgs<R> &a, const FFDev<R> &F, const typename Vec<R>::T4 *sh,
                                                   int i, int s, int cur, int lp, long long step,
-                                                  const typename Vec<R>::T4 &pi, int w, bool zero_bulk, double &ke,
-                                                  double &ep, float &md2, int &flags, double &vsx, double &vsy,
-                                                  double &vsz) {
+                                                  const typename Vec<R>::T4 &pi, int w, bool zero_bulk, R &ke, R &ep,
+                                                  float &md2, int &flags, R &vsx, R &vsy, R &vsz) {
     using T4 = typename Vec<R>::T4;
     const int ty = w_type(w);
     const SysDev &sd = a.sys[s];
@@ -611,12 +618,12 @@ __device__ __forceinline__ void langevin_particle(const KArgs<R> &a, const FFDev
     const R ddx = p.x - xr.x, ddy = p.y - xr.y, ddz = p.z - xr.z;
     md2 = float(ddx * ddx + ddy * ddy + ddz * ddz);
     if (!isfinite(p.x + p.y + p.z + v.x + v.y + v.z)) flags |= ERRB_NAN;
-    ke = double(F.mass[ty]) * (double(v.x) * double(v.x) + double(v.y) * double(v.y) + double(v.z) * double(v.z));
-    ep = double(e);
+    ke = F.mass[ty] * (v.x * v.x + v.y * v.y + v.z * v.z);
+    ep = e;
     if (ty == 0) {
-        vsx = double(v.x);
-        vsy = double(v.y);
-        vsz = double(v.z);
+        vsx = v.x;
+        vsy = v.y;
+        vsz = v.z;
     }
 }
 
@@ -636,7 +643,7 @@ template<class R, bool E, int V> __global__ void __launch_bounds__(STEP_BS, (V &
     const T4 pi = a.pos[cur][i];
     prefetch_warp_list(a.nbr, i, a.cap, a.nnb[i]);
     const int w = wbits(pi.w);
-    double ke = 0, ep = 0, vsx = 0, vsy = 0, vsz = 0;
+    R ke = 0, ep = 0, vsx = 0, vsy = 0, vsz = 0;
     float md2 = 0.f;
     int flags = 0;
     if (w_type(w) != GHOST)
@@ -664,7 +671,7 @@ __global__ void __launch_bounds__(LITE_BS, (V & 4) ? 20 : 16) k_step_langevin_li
     const T4 pi = a.pos[cur][i];
     prefetch_warp_list(a.nbr, i, a.cap, a.nnb[i]);
     const int w = wbits(pi.w);
-    double ke = 0, ep = 0, vsx = 0, vsy = 0, vsz = 0;
+    R ke = 0, ep = 0, vsx = 0, vsy = 0, vsz = 0;
     float md2 = 0.f;
     int flags = 0;
     if (w_type(w) != GHOST)
@@ -767,7 +774,7 @@ template<class R, bool E, int V> __global__ void __launch_bounds__(STEP_BS, (V &
     prefetch_warp_list(a.nbr, i, a.cap, a.nnb[i]);
     const int w = wbits(pi.w);
     const int ty = w_type(w);
-    double ke = 0, ep = 0;
+    R ke = 0, ep = 0;
     int flags = 0;
     if (ty != GHOST) {
         const T4 ni = a.nrm[cur][i];
@@ -802,8 +809,8 @@ template<class R, bool E, int V> __global__ void __launch_bounds__(STEP_BS, (V &
         a.frc[lp][i] = fo;
         a.trq[lp][i] = tq;
         if (!isfinite(v.x + v.y + v.z)) flags |= ERRB_NAN;
-        ke = double(F.mass[ty]) * (double(v.x) * double(v.x) + double(v.y) * double(v.y) + double(v.z) * double(v.z));
-        ep = double(e);
+        ke = F.mass[ty] * (v.x * v.x + v.y * v.y + v.z * v.z);
+        ep = e;
     }
     finish<R>(a, ke, ep, 0.f, flags, MODE_NH_FINAL, count_step);
 }
@@ -817,7 +824,7 @@ template<class R> __global__ void __launch_bounds__(STEP_BS) k_nh_initial(KArgs<
     T4 p = a.pos[cur][i];
     const int w = wbits(p.w);
     const int ty = w_type(w);
-    double ke = 0, vsx = 0, vsy = 0, vsz = 0;
+    R ke = 0, vsx = 0, vsy = 0, vsz = 0;
     float md2 = 0.f;
     int flags = 0;
     if (ty != GHOST) {
@@ -834,11 +841,11 @@ template<class R> __global__ void __launch_bounds__(STEP_BS) k_nh_initial(KArgs<
         p.z += v.z * dt;
         // bounce back at the walls (src/integrate_nh.h:199-208), in the cell frame
         bounce_walls<R>(sd, a.cell[lp][i], p, v);
-        ke = double(a.ff->mass[ty]) * (double(v.x) * double(v.x) + double(v.y) * double(v.y) + double(v.z) * double(v.z));
+        ke = a.ff->mass[ty] * (v.x * v.x + v.y * v.y + v.z * v.z);
         if (ty == 0) {
-            vsx = double(v.x);
-            vsy = double(v.y);
-            vsz = double(v.z);
+            vsx = v.x;
+            vsy = v.y;
+            vsz = v.z;
         }
         o.x += R(0.5) * dt * t.x;
         o.y += R(0.5) * dt * t.y;
@@ -860,7 +867,7 @@ template<class R> __global__ void __launch_bounds__(STEP_BS) k_nh_initial(KArgs<
         md2 = float(ddx * ddx + ddy * ddy + ddz * ddz);
         if (!isfinite(p.x + p.y + p.z)) flags |= ERRB_NAN;
     }
-    finish<R>(a, ke, 0.0, md2, flags, MODE_NH_INITIAL, 0, vsx, vsy, vsz);
+    finish<R>(a, ke, R(0), md2, flags, MODE_NH_INITIAL, 0, vsx, vsy, vsz);
 }
 
 /* Velocity sums of each system after the velocities were replaced (upload,
@@ -870,18 +877,18 @@ template<class R> __global__ void __launch_bounds__(STEP_BS) k_vcom(KArgs<R> a) 
     using T4 = typename Vec<R>::T4;
     const int cur = __ldcg(&a.S->cur), lp = __ldcg(&a.S->lp);
     const int i = blockIdx.x * STEP_BS + threadIdx.x;
-    double ke = 0, vsx = 0, vsy = 0, vsz = 0;
+    R ke = 0, vsx = 0, vsy = 0, vsz = 0;
     const int ty = w_type(wbits(a.pos[cur][i].w));
     if (ty != GHOST) {
         const T4 v = a.vel[lp][i];
-        ke = double(a.ff->mass[ty]) * (double(v.x) * double(v.x) + double(v.y) * double(v.y) + double(v.z) * double(v.z));
+        ke = a.ff->mass[ty] * (v.x * v.x + v.y * v.y + v.z * v.z);
         if (ty == 0) {
-            vsx = double(v.x);
-            vsy = double(v.y);
-            vsz = double(v.z);
+            vsx = v.x;
+            vsy = v.y;
+            vsz = v.z;
         }
     }
-    finish<R>(a, ke, 0.0, 0.f, 0, MODE_VCOM, 0, vsx, vsy, vsz);
+    finish<R>(a, ke, R(0), 0.f, 0, MODE_VCOM, 0, vsx, vsy, vsz);
 }
 
 /* assign_temperature (src/assign_temperature.h:26-44, called at
@@ -925,7 +932,7 @@ template<class R, bool E, int V> __global__ void __launch_bounds__(STEP_BS, (V &
     const T4 pi = a.pos[cur][i];
     prefetch_warp_list(a.nbr, i, a.cap, a.nnb[i]);
     const int w = wbits(pi.w);
-    double ep = 0;
+    R ep = 0;
     int flags = 0;
     if (w_type(w) != GHOST) {
         const T4 ni = a.nrm[cur][i];
@@ -942,9 +949,9 @@ template<class R, bool E, int V> __global__ void __launch_bounds__(STEP_BS, (V &
         q.z = t.z;
         a.trq[lp][i] = q;
         a.epart[i] = double(e);
-        ep = double(e);
+        ep = e;
     }
-    finish<R>(a, 0.0, ep, 0.f, flags, MODE_FORCES, 0);
+    finish<R>(a, R(0), ep, 0.f, flags, MODE_FORCES, 0);
 }
 
 /* FP64 membrane area and enclosed volume of each system's face mesh, and
