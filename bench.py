@@ -12,8 +12,9 @@ eta = 0.01.  Seeded synthetic data (the reference ships no dataset).
 value      mixed-precision particle-steps/s, device time of K steps (inputs
            resident in HBM; working set several GB, larger than L2).
 e2e        the same metric through the C ABI the reference host would call
-           each step: orbc_gpu_set_state from pinned host buffers + one
-           orbc_gpu_step + orbc_gpu_download back to the host buffers.
+           each step with its own containers (AoS vector<real,3>, real =
+           float): orbc_gpu_set_state_f32 from pinned host buffers + one
+           orbc_gpu_step + orbc_gpu_download_f32 back to the host buffers.
 roofline   the fused step kernel: compulsory bytes (104 B per particle-step,
            mixed) / its CUDA-event time vs measured HBM bandwidth; the FP32
            ALU fraction of its algorithmic flops is reported beside it.
@@ -230,7 +231,7 @@ def main():
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default skin / kernel form")
     ap.add_argument("--skin", type=float, default=None, help="neighbour skin when not autotuning")
-    ap.add_argument("--form", type=int, default=0, help="kernel form 0..7 when not autotuning")
+    ap.add_argument("--form", type=int, default=0, help="kernel form 0..23 (orbc_params.kernel_variant) when not autotuning")
     args = ap.parse_args()
     rank, ws = dist_setup()
     if args.impl == "reference":
@@ -291,15 +292,16 @@ def main():
     e2e = None
     if not args.skip_e2e:
         import torch
-        host = [torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy() for _ in range(4)]
+        # the reference's containers: AoS float vectors of 3 (src/config_static.h:34-44)
+        host = [torch.empty((n, 3), dtype=torch.float32, pin_memory=True).numpy() for _ in range(4)]
         for h, arr in zip(host, sim.download()):
             h[:] = arr
         e2e_steps = max(10, args.steps // 10)
 
         def e2e_step():
-            N.check(L.orbc_gpu_set_state(sim.h, *[h.ctypes.data for h in host]), sim.h)
+            N.check(L.orbc_gpu_set_state_f32(sim.h, 0, n, 3, *[h.ctypes.data for h in host]), sim.h)
             N.check(L.orbc_gpu_step(sim.h, 1, None), sim.h)
-            N.check(L.orbc_gpu_download(sim.h, *[h.ctypes.data for h in host]), sim.h)
+            N.check(L.orbc_gpu_download_f32(sim.h, 0, n, 3, *[h.ctypes.data for h in host]), sim.h)
 
         for _ in range(3):  # warm-up (first use captures the one-step graph)
             e2e_step()
@@ -309,10 +311,10 @@ def main():
             e2e_step()
         e2e_s = allreduce_max(time.perf_counter() - t0, ws)
         e2e = {"value": ws * n * e2e_steps / e2e_s, "unit": "particle-steps/s",
-               "h2d_bytes_per_step": 4 * 3 * 8 * n, "d2h_bytes_per_step": 4 * 3 * 8 * n, "steps": e2e_steps,
-               "note": "per step: orbc_gpu_set_state (pinned H2D of x, n, v, o; the list is rebuilt only when a "
-                       "particle moved more than skin/2) + "
-                       "orbc_gpu_step(1) + orbc_gpu_download (D2H of x, n, v, o)"}
+               "h2d_bytes_per_step": 4 * 3 * 4 * n, "d2h_bytes_per_step": 4 * 3 * 4 * n, "steps": e2e_steps,
+               "note": "per step: orbc_gpu_set_state_f32 (pinned H2D of the x, n, v, o float containers; the "
+                       "list is rebuilt only when a particle moved more than skin/2) + "
+                       "orbc_gpu_step(1) + orbc_gpu_download_f32 (D2H of x, n, v, o)"}
         log(f"e2e: {e2e['value']:.4e} particle-steps/s")
 
     peak, peak_kind = measured_peaks()

@@ -84,12 +84,15 @@ typedef struct {
     double bond_K[ORBC_MAX_BOND_TYPES];
     double bond_r0[ORBC_MAX_BOND_TYPES];
     double bond_R[ORBC_MAX_BOND_TYPES];
-    /* kernel forms 0..15: bit 0 = software-pipelined neighbour pass
+    /* kernel forms 0..23: bit 0 = software-pipelined neighbour pass
        (else 2-way unrolled), bit 1 = non-lipid pair path inlined (else
        called), bit 2 = Langevin step kernel compiled for 20 resident blocks
-       per SM (48 registers; else 16 blocks, 64 registers), bit 3 = neighbour
-       list built by per-particle 27-cell sweeps (else per cell of a warp,
-       32 candidates at a time); orbc_gpu_autotune picks it per workload */
+       per SM (48 registers; else 16 blocks, 64 registers), bits 3-4 = how
+       the neighbour list is built: 0 per cell of a warp, 32 candidates at a
+       time, entries placed by prefix count; 1 per-particle 27-cell sweeps;
+       2 per warp in two phases (accept masks per particle, then every lane
+       writes its own column).  All forms write the same list.
+       orbc_gpu_autotune picks the forms per workload */
     int kernel_variant;
     /* 1: remove each system's mean lipid velocity between the force
        evaluation and the integrator every step, as the disabled call
@@ -155,12 +158,28 @@ int orbc_gpu_upload_batch(orbc_handle *h, int nsys, const orbc_system_desc *sys,
  * truth between steps. */
 int orbc_gpu_set_state(orbc_handle *h, const double *x3, const double *n3, const double *v3, const double *o3);
 
+/* orbc_gpu_set_state for the upload indices [first, first + count) from host
+ * arrays in the reference's own container layout: AoS vectors of
+ * `real` = float (src/config_static.h:34) with `stride` floats per particle,
+ * 3 (vector<real,3>) or 4 (the padded _VEC4 layout, src/config_static.h:36-44).
+ * The containers' x, v, n, o (src/container.h:68-72) can be passed as they
+ * are: one call for the lipid range, one for the protein range.  Half the
+ * bytes of the FP64 call cross the host link. */
+int orbc_gpu_set_state_f32(orbc_handle *h, int64_t first, int64_t count, int stride, const float *x, const float *n,
+                           const float *v, const float *o);
+
 /* nsteps of the loop body of src/openrbc.cpp:189-242 (pair forces, bonds,
  * constraint, integrator; neighbour rebuild on demand).  out may be NULL. */
 int orbc_gpu_step(orbc_handle *h, int nsteps, orbc_thermo *out);
 
 /* Current state in upload order (any pointer may be NULL). */
 int orbc_gpu_download(orbc_handle *h, double *x3, double *n3, double *v3, double *o3);
+
+/* orbc_gpu_download of the upload indices [first, first + count) into host
+ * AoS float vectors with `stride` floats per particle (3, or 4 with the
+ * fourth written as 0); the layout of orbc_gpu_set_state_f32. */
+int orbc_gpu_download_f32(orbc_handle *h, int64_t first, int64_t count, int stride, float *x, float *n, float *v,
+                          float *o);
 
 /* Parity hook: forces, torques and per-particle potential energy at the
  * current state, in upload order (compute_pairwise_fused + compute_bonded,

@@ -25,7 +25,8 @@ NOALLOC_MAX_POINTS = 262144
 # Every symbol include/*.h declares (checked by the CPU test suite).
 EXPORTS = [
     "orbc_gpu_default_params", "orbc_gpu_create", "orbc_gpu_upload", "orbc_gpu_upload_batch",
-    "orbc_gpu_set_state", "orbc_gpu_step", "orbc_gpu_download", "orbc_gpu_forces", "orbc_gpu_thermo",
+    "orbc_gpu_set_state", "orbc_gpu_set_state_f32", "orbc_gpu_step", "orbc_gpu_download", "orbc_gpu_download_f32",
+    "orbc_gpu_forces", "orbc_gpu_thermo",
     "orbc_gpu_neighbors", "orbc_gpu_cells", "orbc_gpu_rebuild", "orbc_gpu_last_timing",
     "orbc_gpu_morton_encode", "orbc_gpu_morton_order", "orbc_gpu_destroy", "orbc_gpu_error",
     "orbc_gpu_version", "orbc_gpu_profile", "orbc_gpu_morton_order_noalloc", "orbc_gpu_autotune",
@@ -114,6 +115,8 @@ def lib():
         L.orbc_gpu_set_state.argtypes = [H, vp, vp, vp, vp]
         L.orbc_gpu_step.argtypes = [H, i32, P(Thermo)]
         L.orbc_gpu_download.argtypes = [H, vp, vp, vp, vp]
+        L.orbc_gpu_set_state_f32.argtypes = [H, i64, i64, i32, vp, vp, vp, vp]
+        L.orbc_gpu_download_f32.argtypes = [H, i64, i64, i32, vp, vp, vp, vp]
         L.orbc_gpu_forces.argtypes = [H, vp, vp, vp]
         L.orbc_gpu_thermo.argtypes = [H, i32, P(Thermo)]
         L.orbc_gpu_neighbors.argtypes = [H, vp, vp, i64, P(i64)]

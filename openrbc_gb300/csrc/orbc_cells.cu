@@ -278,6 +278,38 @@ template<class R> __global__ void __launch_bounds__(256) k_ranges_gather(KArgs<R
     }
 }
 
+/* End of a list build: block max of the candidate counts -> global max and
+ * overflow flag; the last block to finish makes the new buffers current and
+ * clears the rebuild request. */
+template<class R> __device__ __forceinline__ void nlist_finalise(const KArgs<R> &a, int maxc, int cur, int lp) {
+    __shared__ int smax[8];
+    __shared__ bool last;
+    int m = maxc;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) smax[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int bm = 0;
+        for (int w = 0; w < int(blockDim.x >> 5); ++w) bm = max(bm, smax[w]);
+        atomicMax(&a.S->max_nnb, bm);
+        if (bm > a.cap) atomicOr(&a.S->error, ERRB_NBR_OVERFLOW);
+        __threadfence();
+        const unsigned ticket = atomicAdd(&a.S->blk_counter, 1u);
+        last = (ticket == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (last && threadIdx.x == 0) {
+        a.S->cur = cur;
+        a.S->lp = lp;
+        a.S->rebuild = 0;
+        a.S->rebuilds += 1;
+        a.S->since_rebuild = 0;
+        a.S->blk_counter = 0;
+        __threadfence();
+    }
+}
+
 template<class R> __global__ void __launch_bounds__(128) k_nlist(KArgs<R> a, int gated) {
     using T4 = typename Vec<R>::T4;
     if (gated && !__ldcg(&a.S->rebuild)) return;
@@ -498,33 +530,208 @@ template<class R> __global__ void __launch_bounds__(128) k_nlist(KArgs<R> a, int
         a.nnb[i] = real ? (nin | (nout << 16)) : 0;
         maxc = max(maxc, total);
     }
-    // block max -> global max; last block finalises the rebuild
-    __shared__ int smax[8];
-    __shared__ bool last;
-    int m = maxc;
+    nlist_finalise(a, maxc, cur, lp);
+}
+
+/* Form 2 of the list build (two phases per warp).  The distinct cells of a
+ * warp's particles are staged as in form 0 -- 27 lanes fetch a cell's
+ * neighbour ranges, the warp stages its candidates pre-shifted into that
+ * cell's frame -- but as many cells per pass as fit, each in its own region
+ * of shared memory (regions start on different 16-byte bank slots).
+ * Phase 1: for each particle of a cell the warp tests 32 candidates per
+ * ballot, branch-free, and the particle's own lane keeps the accept masks
+ * (in range at all / inside the interaction range) in registers.  Phase 2:
+ * every lane of the pass expands its masks in candidate order into its own
+ * column.  The candidates, their order and the arithmetic are those of
+ * forms 0 and 1, so all three forms write the same rows. */
+template<class R> __global__ void __launch_bounds__(128) k_nlist2(KArgs<R> a, int gated) {
+    using T4 = typename Vec<R>::T4;
+    if (gated && !__ldcg(&a.S->rebuild)) return;
+    constexpr int NLW = 4;                                // warps per block
+    constexpr int MB = 8;                                 // masks (32 candidates each) per region
+    constexpr int REG = 32 * MB;                          // candidates per cell region
+    constexpr int TOT = sizeof(T4) == 16 ? 512 : 288;     // staged candidates per warp and pass
+    __shared__ float2 s_cut[256];                         // (list cutoff^2, range cutoff^2) per type pair
+    __shared__ T4 s_pos[NLW][TOT];
+    __shared__ uint32_t s_ent[NLW][TOT];                  // j | shift code of its cell << NB_SHIFT
+    __shared__ int s_off[NLW][28], s_beg[NLW][27];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int k = threadIdx.x; k < 256; k += blockDim.x)
+        s_cut[k] = make_float2(__ldg(&a.ff->rlist2[k]), __ldg(&a.ff->rin2[k]));
+    __syncthreads();
+    const int cur = 1 - __ldcg(&a.S->cur), lp = 1 - __ldcg(&a.S->lp);
+    // the grid covers npad (a multiple of the block size) once
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const T4 p = a.pos[cur][i];
+    const int ty = w_type(wbits(p.w));
+    const bool real = ty != GHOST;
+    const SysDev &sd = a.sys[a.blk_sys[i / SYS_PAD]];  // one system per warp (SYS_PAD-aligned)
+    const int c = a.cell[lp][i];
+    const int cc[3] = {cx_of(c), cy_of(c), cz_of(c)};
+    const R L[3] = {R(sd.Lc[0]), R(sd.Lc[1]), R(sd.Lc[2])};
+    // the expressions of k_nlist's shifted() and dist2()
+    auto shifted = [&](const T4 &q, int dx, int dy, int dz) {
+        T4 r = q;
+        r.x = q.x + R(dx) * L[0];
+        r.y = q.y + R(dy) * L[1];
+        r.z = q.z + R(dz) * L[2];
+        return r;
+    };
+    auto dist2 = [&](const T4 &pi, const T4 &qs) {
+        const R ex = pi.x - qs.x, ey = pi.y - qs.y, ez = pi.z - qs.z;
+        return ex * ex + ey * ey + ez * ez;
+    };
+    const int kme = cc[0] | (cc[1] << 11) | (cc[2] << 22);
+    int *off = s_off[warp];
+    int *beg = s_beg[warp];
+    T4 *sp = s_pos[warp];
+    uint32_t *se = s_ent[warp];
+    uint32_t *col = a.nbr + nbr_index(i, 0, a.cap);  // row k of slot i at col[32 k]
+    const int cap = a.cap;
+    int qin = 0, qout = 0, qtot = 0;
+    // neighbour ranges of cell kd -> off/beg; returns the candidate count
+    auto fetch = [&](int kd) {
+        const int xd = kd & 2047, yd = (kd >> 11) & 2047, zd = (kd >> 22) & 1023;
+        int2 rg = make_int2(0, 0);
+        if (lane < 27) {
+            int x = xd + lane % 3 - 1, y = yd + (lane / 3) % 3 - 1, z = zd + lane / 9 - 1;
+            bool ok = true;
+            if (sd.per[0]) x = x < 0 ? x + sd.nc[0] : (x >= sd.nc[0] ? x - sd.nc[0] : x);
+            else ok = ok && x >= 0 && x < sd.nc[0];
+            if (sd.per[1]) y = y < 0 ? y + sd.nc[1] : (y >= sd.nc[1] ? y - sd.nc[1] : y);
+            else ok = ok && y >= 0 && y < sd.nc[1];
+            if (sd.per[2]) z = z < 0 ? z + sd.nc[2] : (z >= sd.nc[2] ? z - sd.nc[2] : z);
+            else ok = ok && z >= 0 && z < sd.nc[2];
+            if (ok) rg = a.ranges[sd.cell_base + cell_code(sd, x, y, z)];
+        }
+        const int cnt = rg.y > rg.x ? rg.y - rg.x : 0;
+        int inc = cnt;  // inclusive warp scan
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
-    if ((threadIdx.x & 31) == 0) smax[threadIdx.x >> 5] = m;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        int bm = 0;
-        for (int w = 0; w < int(blockDim.x >> 5); ++w) bm = max(bm, smax[w]);
-        atomicMax(&a.S->max_nnb, bm);
-        if (bm > a.cap) atomicOr(&a.S->error, ERRB_NBR_OVERFLOW);
-        __threadfence();
-        const unsigned ticket = atomicAdd(&a.S->blk_counter, 1u);
-        last = (ticket == gridDim.x - 1);
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += t;
+        }
+        __syncwarp();  // the previous cell's staging is done with off/beg
+        if (lane < 27) {
+            off[lane] = inc - cnt;
+            beg[lane] = rg.x;
+        }
+        __syncwarp();
+        return __shfl_sync(0xffffffffu, inc, 31);
+    };
+    // candidates [c0, c0 + nch) of the fetched cell -> sp/se[base ...]
+    auto stage = [&](int c0, int nch, int base) {
+#pragma unroll 4
+        for (int t = lane; t < nch; t += 32) {
+            const int idx = c0 + t;
+            int l = 0;  // last neighbour cell with off[l] <= idx
+#pragma unroll
+            for (int step = 16; step > 0; step >>= 1)
+                if (l + step < 27 && off[l + step] <= idx) l += step;
+            const int j = beg[l] + (idx - off[l]);
+            sp[base + t] = shifted(a.pos[cur][j], l % 3 - 1, (l / 3) % 3 - 1, l / 9 - 1);
+            se[base + t] = uint32_t(j) | (uint32_t(l) << NB_SHIFT);
+        }
+        __syncwarp();
+    };
+    uint32_t macc[MB], minn[MB];
+    // phase 1 for the particles grp over the region [base, base + nch), nch <= REG;
+    // ts: the owning lane's own staged index (self is not a neighbour), -1 if absent
+    auto phase1 = [&](unsigned grp, int base, int nch, int ts) {
+        for (unsigned g = grp; g; g &= g - 1u) {
+            const int il = __ffs(g) - 1;
+            T4 pi = p;
+            pi.x = __shfl_sync(0xffffffffu, p.x, il);
+            pi.y = __shfl_sync(0xffffffffu, p.y, il);
+            pi.z = __shfl_sync(0xffffffffu, p.z, il);
+            const int ti = __shfl_sync(0xffffffffu, ty, il) * 16;
+            const int tsi = __shfl_sync(0xffffffffu, ts, il);
+#pragma unroll
+            for (int b = 0; b < MB; ++b) {
+                if (b * 32 < nch) {
+                    const int t = b * 32 + lane;
+                    const bool valid = t < nch;
+                    const T4 q = sp[base + (valid ? t : 0)];
+                    const float2 cut = s_cut[ti + w_type(wbits(q.w))];
+                    const R r2 = dist2(pi, q);
+                    const bool acc = valid && t != tsi && cut.x > 0.f && r2 < R(cut.x);
+                    const unsigned ma = __ballot_sync(0xffffffffu, acc);
+                    const unsigned mi = __ballot_sync(0xffffffffu, acc && r2 < R(cut.y));
+                    if (lane == il) {
+                        macc[b] = ma;
+                        minn[b] = mi;
+                    }
+                }
+            }
+        }
+    };
+    // phase 2: this lane's accepted candidates of the region at mybase, in order
+    auto phase2 = [&](int mybase) {
+#pragma unroll
+        for (int b = 0; b < MB; ++b) {
+            unsigned m = macc[b];
+            const unsigned mi = minn[b];
+            while (m) {
+                const int bit = __ffs(m) - 1;
+                m &= m - 1u;
+                const uint32_t e = se[mybase + b * 32 + bit];
+                if (qin + qout < cap) {
+                    if ((mi >> bit) & 1u)
+                        col[32 * qin++] = e;
+                    else
+                        col[32 * (cap - 1 - qout++)] = e;
+                }
+                ++qtot;
+            }
+        }
+        __syncwarp();  // every lane is done with the regions before they are restaged
+    };
+    auto clear_masks = [&]() {
+#pragma unroll
+        for (int b = 0; b < MB; ++b) macc[b] = minn[b] = 0u;
+    };
+    unsigned todo = __ballot_sync(0xffffffffu, real);
+    while (todo) {
+        clear_masks();
+        int used = 0, ng = 0, mybase = 0, big = 0;
+        unsigned rest = todo, biggrp = 0;
+        while (rest) {
+            const int kd = __shfl_sync(0xffffffffu, kme, __ffs(rest) - 1);
+            const unsigned grp = __ballot_sync(0xffffffffu, real && kme == kd) & rest;
+            const int total_c = fetch(kd);
+            if (total_c > REG) {  // more than one region holds: in chunks, alone in its pass
+                if (used == 0) {
+                    big = total_c;
+                    biggrp = grp;
+                    rest &= ~grp;
+                }
+                break;
+            }
+            const int base = used + ((ng - used) & 7);  // bank slot ng mod 8
+            if (base + total_c > TOT) break;           // next pass
+            stage(0, total_c, base);
+            phase1(grp, base, total_c, off[13] + (i - beg[13]));
+            if ((grp >> lane) & 1u) mybase = base;
+            used = base + total_c;
+            ++ng;
+            rest &= ~grp;
+        }
+        todo = rest;
+        if (!big) {
+            phase2(mybase);
+        } else {
+            const int ts0 = off[13] + (i - beg[13]);
+            for (int c0 = 0; c0 < big; c0 += REG) {
+                const int nch = min(REG, big - c0);
+                clear_masks();
+                stage(c0, nch, 0);
+                phase1(biggrp, 0, nch, (ts0 >= c0 && ts0 < c0 + nch) ? ts0 - c0 : -1);
+                phase2(0);
+            }
+        }
     }
-    __syncthreads();
-    if (last && threadIdx.x == 0) {
-        a.S->cur = cur;
-        a.S->lp = lp;
-        a.S->rebuild = 0;
-        a.S->rebuilds += 1;
-        a.S->since_rebuild = 0;
-        a.S->blk_counter = 0;
-        __threadfence();
-    }
+    a.nnb[i] = real ? (qin | (qout << 16)) : 0;
+    nlist_finalise(a, real ? qtot : 0, cur, lp);
 }
 
 static int grid_for(int64_t n, int per_block = 256) {
@@ -547,7 +754,10 @@ template<class R> void launch_rebuild_stage(const KArgs<R> &a, cudaStream_t st, 
             k_ranges_gather<R><<<g, 256, 0, st>>>(a, a.sort_passes % 2, gated ? 1 : 0);
             break;
         default:
-            k_nlist<R><<<(a.npad + 127) / 128, 128, 0, st>>>(a, gated ? 1 : 0);
+            if (a.nlist_lane == 2)
+                k_nlist2<R><<<(a.npad + 127) / 128, 128, 0, st>>>(a, gated ? 1 : 0);
+            else
+                k_nlist<R><<<(a.npad + 127) / 128, 128, 0, st>>>(a, gated ? 1 : 0);
             break;
     }
 }
@@ -559,14 +769,19 @@ template<class R> void launch_rebuild(const KArgs<R> &a, cudaStream_t st, bool g
 /* ------------------------------------------------------------------------- */
 /* State conversion                                                          */
 /* ------------------------------------------------------------------------- */
-template<class R>
-__global__ void k_set_state(KArgs<R> a, const double *x, const double *nv, const double *v, const double *o,
-                            int64_t k0, int64_t k1) {
+/* Host state -> device slots for upload indices [k0, k1).  The staged host
+ * arrays hold the particles from upload index `first` on, `stride` values of
+ * type TH per particle (AoS; FP64 vectors of 3, or the reference's own `real`
+ * = float vectors of 3, or of 4 under its _VEC4 layout). */
+template<class R, class TH>
+__global__ void k_set_state(KArgs<R> a, const TH *x, const TH *nv, const TH *v, const TH *o, int64_t k0, int64_t k1,
+                            int64_t first, int stride) {
     using T4 = typename Vec<R>::T4;
     const int cur = __ldcg(&a.S->cur), lp = __ldcg(&a.S->lp);
     int out = 0, moved = 0;
     for (int64_t k = k0 + blockIdx.x * int64_t(blockDim.x) + threadIdx.x; k < k1; k += int64_t(gridDim.x) * blockDim.x) {
         const int p = a.slot_of_home[k];
+        const int64_t hk = (k - first) * stride;
         const SysDev &sd = a.sys[a.blk_sys[p / SYS_PAD]];
         T4 q = a.pos[cur][p];
         // A particle still within skin/2 of where the list was built keeps its
@@ -581,7 +796,7 @@ __global__ void k_set_state(KArgs<R> a, const double *x, const double *nv, const
         R md2 = 0;
         for (int d = 0; d < 3; ++d) {
             const double center = __dadd_rn(sd.lo[d], __dmul_rn(double(cc0[d]) + 0.5, sd.Lc[d]));
-            double u = __dsub_rn(x[3 * k + d], center);
+            double u = __dsub_rn(double(x[hk + d]), center);
             if (sd.per[d]) {
                 const double L = double(sd.nc[d]) * sd.Lc[d];
                 u -= L * rint(u / L);
@@ -600,7 +815,7 @@ __global__ void k_set_state(KArgs<R> a, const double *x, const double *nv, const
             int cc[3];
             R off[3];
             for (int d = 0; d < 3; ++d) {
-                const double xd = x[3 * k + d];
+                const double xd = double(x[hk + d]);
                 const int cu = int(floor(__ddiv_rn(__dsub_rn(xd, sd.lo[d]), sd.Lc[d])));
                 int c = cu;
                 if (sd.per[d]) {
@@ -623,40 +838,44 @@ __global__ void k_set_state(KArgs<R> a, const double *x, const double *nv, const
             a.cell[lp][p] = cpack(cc[0], cc[1], cc[2]);
         }
         T4 t = a.nrm[cur][p];
-        t.x = R(nv[3 * k]);
-        t.y = R(nv[3 * k + 1]);
-        t.z = R(nv[3 * k + 2]);
+        t.x = R(nv[hk]);
+        t.y = R(nv[hk + 1]);
+        t.z = R(nv[hk + 2]);
         a.nrm[cur][p] = t;
         t = a.vel[lp][p];
-        t.x = R(v[3 * k]);
-        t.y = R(v[3 * k + 1]);
-        t.z = R(v[3 * k + 2]);
+        t.x = R(v[hk]);
+        t.y = R(v[hk + 1]);
+        t.z = R(v[hk + 2]);
         a.vel[lp][p] = t;
         t = a.omg[lp][p];
-        t.x = R(o[3 * k]);
-        t.y = R(o[3 * k + 1]);
-        t.z = R(o[3 * k + 2]);
+        t.x = R(o[hk]);
+        t.y = R(o[hk + 1]);
+        t.z = R(o[hk + 2]);
         a.omg[lp][p] = t;
     }
     if (out) atomicOr(&a.S->error, ERRB_GRID);
     if (__syncthreads_or(moved) && threadIdx.x == 0) a.S->rebuild = 1;
 }
 
-template<class R> void launch_set_state(const KArgs<R> &a, const double *x, const double *n, const double *v,
-                                        const double *o, int64_t k0, int64_t k1, cudaStream_t st) {
-    k_set_state<R><<<grid_for(k1 - k0), 256, 0, st>>>(a, x, n, v, o, k0, k1);
+template<class R, class TH>
+void launch_set_state(const KArgs<R> &a, const TH *x, const TH *n, const TH *v, const TH *o, int64_t k0, int64_t k1,
+                      int64_t first, int stride, cudaStream_t st) {
+    k_set_state<R, TH><<<grid_for(k1 - k0), 256, 0, st>>>(a, x, n, v, o, k0, k1, first, stride);
 }
 
-/* Device state -> caller-order AoS doubles.  One thread per upload index (the
- * slot comes from slot_of_home), so the writes -- the side that streams to
- * the host -- are coalesced; the slot-side reads are gathers. */
-template<class R>
-__global__ void k_download(KArgs<R> a, int64_t h0, int64_t h1, double *x, double *nv, double *v, double *o,
-                           double *f, double *t, double *e) {
+/* Device state -> caller-order AoS vectors of TH for upload indices [h0, h1),
+ * written from upload index `first` on with `stride` values per particle (a
+ * fourth value, when stride is 4, is written as 0).  One thread per upload
+ * index (the slot comes from slot_of_home), so the writes -- the side that
+ * streams to the host -- are coalesced; the slot-side reads are gathers. */
+template<class R, class TH>
+__global__ void k_download(KArgs<R> a, int64_t h0, int64_t h1, int64_t first, int stride, TH *x, TH *nv, TH *v,
+                           TH *o, TH *f, TH *t, double *e) {
     using T4 = typename Vec<R>::T4;
     const int cur = __ldcg(&a.S->cur), lp = __ldcg(&a.S->lp);
     for (int64_t h = h0 + blockIdx.x * int64_t(blockDim.x) + threadIdx.x; h < h1; h += int64_t(gridDim.x) * blockDim.x) {
         const int p = a.slot_of_home[h];
+        const int64_t hk = (h - first) * stride;
         const SysDev &sd = a.sys[a.blk_sys[p / SYS_PAD]];
         if (x) {
             const T4 q = a.pos[cur][p];
@@ -664,13 +883,15 @@ __global__ void k_download(KArgs<R> a, int64_t h0, int64_t h1, double *x, double
             const int cc[3] = {cx_of(c), cy_of(c), cz_of(c)};
             const double off[3] = {double(q.x), double(q.y), double(q.z)};
             for (int d = 0; d < 3; ++d)
-                x[3 * h + d] = __dadd_rn(__dadd_rn(sd.lo[d], __dmul_rn(double(cc[d]) + 0.5, sd.Lc[d])), off[d]);
+                x[hk + d] = TH(__dadd_rn(__dadd_rn(sd.lo[d], __dmul_rn(double(cc[d]) + 0.5, sd.Lc[d])), off[d]));
+            if (stride == 4) x[hk + 3] = TH(0);
         }
-        auto put = [&](double *dst, const T4 &q) {
+        auto put = [&](TH *dst, const T4 &q) {
             if (!dst) return;
-            dst[3 * h] = double(q.x);
-            dst[3 * h + 1] = double(q.y);
-            dst[3 * h + 2] = double(q.z);
+            dst[hk] = TH(q.x);
+            dst[hk + 1] = TH(q.y);
+            dst[hk + 2] = TH(q.z);
+            if (stride == 4) dst[hk + 3] = TH(0);
         };
         if (nv) put(nv, a.nrm[cur][p]);
         if (v) put(v, a.vel[lp][p]);
@@ -681,9 +902,14 @@ __global__ void k_download(KArgs<R> a, int64_t h0, int64_t h1, double *x, double
     }
 }
 
+template<class R, class TH>
+void launch_download(const KArgs<R> &a, int64_t h0, int64_t h1, int64_t first, int stride, TH *x, TH *n, TH *v, TH *o,
+                     TH *f, TH *t, double *e, cudaStream_t st) {
+    k_download<R, TH><<<grid_for(h1 - h0), 256, 0, st>>>(a, h0, h1, first, stride, x, n, v, o, f, t, e);
+}
 template<class R> void launch_download(const KArgs<R> &a, int64_t h0, int64_t h1, double *x, double *n, double *v,
                                        double *o, double *f, double *t, double *e, cudaStream_t st) {
-    k_download<R><<<grid_for(h1 - h0), 256, 0, st>>>(a, h0, h1, x, n, v, o, f, t, e);
+    launch_download<R, double>(a, h0, h1, 0, 3, x, n, v, o, f, t, e, st);
 }
 
 __global__ void k_set_cond(cudaGraphConditionalHandle h, const Scalars *S) {
@@ -719,10 +945,16 @@ template void launch_rebuild<float>(const KArgs<float> &, cudaStream_t, bool);
 template void launch_rebuild_stage<float>(const KArgs<float> &, cudaStream_t, bool, int);
 template void launch_rebuild_stage<double>(const KArgs<double> &, cudaStream_t, bool, int);
 template void launch_rebuild<double>(const KArgs<double> &, cudaStream_t, bool);
-template void launch_set_state<float>(const KArgs<float> &, const double *, const double *, const double *,
-                                      const double *, int64_t, int64_t, cudaStream_t);
-template void launch_set_state<double>(const KArgs<double> &, const double *, const double *, const double *,
-                                       const double *, int64_t, int64_t, cudaStream_t);
+#define ORBC_IO_INST(R, TH)                                                                                    \
+    template void launch_set_state<R, TH>(const KArgs<R> &, const TH *, const TH *, const TH *, const TH *, int64_t, \
+                                          int64_t, int64_t, int, cudaStream_t);                                      \
+    template void launch_download<R, TH>(const KArgs<R> &, int64_t, int64_t, int64_t, int, TH *, TH *, TH *, TH *,    \
+                                         TH *, TH *, double *, cudaStream_t);
+ORBC_IO_INST(float, float)
+ORBC_IO_INST(float, double)
+ORBC_IO_INST(double, float)
+ORBC_IO_INST(double, double)
+#undef ORBC_IO_INST
 template void launch_download<float>(const KArgs<float> &, int64_t, int64_t, double *, double *, double *, double *,
                                      double *, double *, double *, cudaStream_t);
 template void launch_download<double>(const KArgs<double> &, int64_t, int64_t, double *, double *, double *,

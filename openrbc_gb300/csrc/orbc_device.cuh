@@ -190,7 +190,7 @@ template<class R> struct KArgs {
     int variant;             // force-kernel form (see launch_step_langevin)
     int carry_forces;        // forces / torques persist between kernels (Nose-Hoover)
     int zero_bulk;           // remove the mean lipid velocity before integrating
-    int nlist_lane;          // neighbour-list form: 0 warp box sweep, 1 per-lane 27-cell sweep
+    int nlist_lane;          // list-build form: 0 per cell of a warp, 1 per-lane 27-cell sweep, 2 two-phase
     const FFDev<R> *ff;      // force-field tables (global; staged into shared memory per block)
 };
 
@@ -221,9 +221,15 @@ cudaError_t launch_rdf(const double *x3, const int *type, int n, const double ce
                        unsigned long long *dropped, void *work, cudaStream_t st);
 template<class R> void launch_assign_temperature(const KArgs<R> &a, double kT, uint64_t seed, cudaStream_t st);
 
-// upload indices [k0, k1) of the caller-order AoS arrays (full-size base pointers)
-template<class R> void launch_set_state(const KArgs<R> &a, const double *x, const double *n, const double *v,
-                                        const double *o, int64_t k0, int64_t k1, cudaStream_t st);
+// upload indices [k0, k1) of caller-order AoS arrays that start at upload
+// index `first`, `stride` values of TH (double or float) per particle
+template<class R, class TH>
+void launch_set_state(const KArgs<R> &a, const TH *x, const TH *n, const TH *v, const TH *o, int64_t k0, int64_t k1,
+                      int64_t first, int stride, cudaStream_t st);
+template<class R, class TH>
+void launch_download(const KArgs<R> &a, int64_t h0, int64_t h1, int64_t first, int stride, TH *x, TH *n, TH *v, TH *o,
+                     TH *f, TH *t, double *e, cudaStream_t st);
+// full-size FP64 vectors of 3 (first = 0, stride = 3)
 template<class R> void launch_download(const KArgs<R> &a, int64_t h0, int64_t h1, double *x, double *n, double *v,
                                        double *o, double *f, double *t, double *e, cudaStream_t st);
 void launch_set_cond(cudaGraphConditionalHandle h, Scalars *S, cudaStream_t st);

@@ -282,6 +282,8 @@ class EngineBase {
                        const double *n3, const double *v3, const double *o3, const int *type, const int *tag, size_t n,
                        const int *bonds3, const double *bond_r0, size_t nb, const int *faces3, size_t nf) = 0;
     virtual int set_state(const double *x3, const double *n3, const double *v3, const double *o3) = 0;
+    virtual int set_state_f32(int64_t first, int64_t count, int stride, const float *x, const float *n,
+                              const float *v, const float *o) = 0;
     virtual int assign_temperature(double kT, uint64_t seed) = 0;
     virtual int minimize(int nsteps, double dr_opt, double dn_opt, orbc_thermo *out) = 0;
     virtual int save_frame(const char *path, int append, int nstep, int fields, int real_bytes, int async) = 0;
@@ -291,6 +293,7 @@ class EngineBase {
     virtual int load_checkpoint(const char *path) = 0;
     virtual int step(int nsteps, orbc_thermo *out) = 0;
     virtual int download(double *x3, double *n3, double *v3, double *o3) = 0;
+    virtual int download_f32(int64_t first, int64_t count, int stride, float *x, float *n, float *v, float *o) = 0;
     virtual int forces(double *f3, double *t3, double *e) = 0;
     virtual int thermo(int sys, orbc_thermo *out) = 0;
     virtual int neighbors(int *counts, int *list, int64_t cap, int64_t *total) = 0;
@@ -671,20 +674,36 @@ template<class R> class Engine : public EngineBase {
     int set_state(const double *x3, const double *n3, const double *v3, const double *o3) override {
         if (!uploaded) return fail(ORBC_ERR_STATE, "set_state before upload");
         if (!x3 || !n3 || !v3 || !o3) return fail(ORBC_ERR_ARG, "set_state: all four arrays are required");
-        double *d = stage.p;
-        const double *src[4] = {x3, n3, v3, o3};
-        // chunked: the copy stream moves chunk c + 1 while the step stream converts chunk c
-        const int nch = nhome >= (int64_t(1) << 20) ? NXCH : 1;
+        return set_state_t<double>(0, nhome, 3, x3, n3, v3, o3);
+    }
+    int set_state_f32(int64_t first, int64_t count, int stride, const float *x, const float *n, const float *v,
+                      const float *o) override {
+        if (!uploaded) return fail(ORBC_ERR_STATE, "set_state before upload");
+        if (!x || !n || !v || !o) return fail(ORBC_ERR_ARG, "set_state_f32: all four arrays are required");
+        if (first < 0 || count < 0 || first + count > nhome || (stride != 3 && stride != 4))
+            return fail(ORBC_ERR_ARG, "set_state_f32: need 0 <= first, first + count <= n and stride 3 or 4");
+        if (count == 0) return ORBC_OK;
+        return set_state_t<float>(first, count, stride, x, n, v, o);
+    }
+    /* upload indices [first, first + count) from host AoS arrays of TH with
+     * `stride` values per particle; chunked: the copy stream moves chunk c + 1
+     * while the step stream converts chunk c */
+    template<class TH>
+    int set_state_t(int64_t first, int64_t count, int stride, const TH *x, const TH *n, const TH *v, const TH *o) {
+        TH *d = reinterpret_cast<TH *>(stage.p);
+        const TH *src[4] = {x, n, v, o};
+        const int64_t m = count * stride;  // values per array
+        const int nch = count >= (int64_t(1) << 20) ? NXCH : 1;
         CK(cudaEventRecord(pev[0], st));  // earlier work on the staging buffer
         CK(cudaStreamWaitEvent(cs, pev[0], 0));
         for (int c = 0; c < nch; ++c) {
-            const int64_t k0 = nhome * c / nch, k1 = nhome * (c + 1) / nch;
+            const int64_t k0 = count * c / nch, k1 = count * (c + 1) / nch;
             for (int q = 0; q < 4; ++q)
-                CK(cudaMemcpyAsync(d + 3 * (nhome * q + k0), src[q] + 3 * k0, size_t(k1 - k0) * 3 * sizeof(double),
+                CK(cudaMemcpyAsync(d + m * q + k0 * stride, src[q] + k0 * stride, size_t(k1 - k0) * stride * sizeof(TH),
                                    cudaMemcpyHostToDevice, cs));
             CK(cudaEventRecord(xev[c], cs));
             CK(cudaStreamWaitEvent(st, xev[c], 0));
-            launch_set_state<R>(a, d, d + 3 * nhome, d + 6 * nhome, d + 9 * nhome, k0, k1, st);
+            launch_set_state<R, TH>(a, d, d + m, d + 2 * m, d + 3 * m, first + k0, first + k1, first, stride, st);
         }
         launch_vcom<R>(a, st);  // temperature and lipid mean of the new velocities
         CK(cudaStreamSynchronize(cs));  // the caller may reuse its arrays on return
@@ -1139,22 +1158,34 @@ template<class R> class Engine : public EngineBase {
 
     int download(double *x3, double *n3, double *v3, double *o3) override {
         if (!uploaded) return fail(ORBC_ERR_STATE, "download before upload");
-        double *d = stage.p;
-        const size_t m = size_t(nhome) * 3;
-        double *dst[4] = {x3, n3, v3, o3};
-        // chunked: the copy stream moves chunk c to the host while the step stream converts chunk c + 1
-        const int nch = nhome >= (int64_t(1) << 20) ? NXCH : 1;
+        return download_t<double>(0, nhome, 3, x3, n3, v3, o3);
+    }
+    int download_f32(int64_t first, int64_t count, int stride, float *x, float *n, float *v, float *o) override {
+        if (!uploaded) return fail(ORBC_ERR_STATE, "download before upload");
+        if (first < 0 || count < 0 || first + count > nhome || (stride != 3 && stride != 4))
+            return fail(ORBC_ERR_ARG, "download_f32: need 0 <= first, first + count <= n and stride 3 or 4");
+        if (count == 0) return ORBC_OK;
+        return download_t<float>(first, count, stride, x, n, v, o);
+    }
+    /* upload indices [first, first + count) to host AoS arrays of TH; chunked:
+     * the copy stream moves chunk c to the host while the step stream converts
+     * chunk c + 1 */
+    template<class TH> int download_t(int64_t first, int64_t count, int stride, TH *x, TH *n, TH *v, TH *o) {
+        TH *d = reinterpret_cast<TH *>(stage.p);
+        const int64_t m = count * stride;
+        TH *dst[4] = {x, n, v, o};
+        const int nch = count >= (int64_t(1) << 20) ? NXCH : 1;
         for (int c = 0; c < nch; ++c) {
-            const int64_t h0 = nhome * c / nch, h1 = nhome * (c + 1) / nch;
-            launch_download<R>(a, h0, h1, x3 ? d : nullptr, n3 ? d + m : nullptr, v3 ? d + 2 * m : nullptr,
-                               o3 ? d + 3 * m : nullptr, nullptr, nullptr, nullptr, st);
+            const int64_t h0 = count * c / nch, h1 = count * (c + 1) / nch;
+            launch_download<R, TH>(a, first + h0, first + h1, first, stride, x ? d : nullptr, n ? d + m : nullptr,
+                                   v ? d + 2 * m : nullptr, o ? d + 3 * m : nullptr, nullptr, nullptr, nullptr, st);
             CK(cudaGetLastError());
             CK(cudaEventRecord(xev[c], st));
             CK(cudaStreamWaitEvent(cs, xev[c], 0));
             for (int q = 0; q < 4; ++q)
                 if (dst[q])
-                    CK(cudaMemcpyAsync(dst[q] + 3 * h0, d + m * q + 3 * h0, size_t(h1 - h0) * 3 * sizeof(double),
-                                       cudaMemcpyDeviceToHost, cs));
+                    CK(cudaMemcpyAsync(dst[q] + h0 * stride, d + m * q + h0 * stride,
+                                       size_t(h1 - h0) * stride * sizeof(TH), cudaMemcpyDeviceToHost, cs));
         }
         CK(cudaStreamSynchronize(cs));
         return ORBC_OK;
@@ -1467,13 +1498,15 @@ template<class R> class Engine : public EngineBase {
             return ORBC_OK;
         };
         // skin x force-kernel form (bits 0-1), then at the best pair the
-        // occupancy form (bit 2) and the list-build form (bit 3)
-        const int rest = P.kernel_variant & 12;
+        // occupancy form (bit 2) and the other two list-build forms (bits 3-4)
+        const int rest = P.kernel_variant & 28;
         for (double sk : skins)
             for (int var = 0; var < 4; ++var)
                 if ((rc = trial(sk, var | rest))) return rc;
         if ((rc = trial(best_skin, best_var ^ 4))) return rc;
-        if ((rc = trial(best_skin, best_var ^ 8))) return rc;
+        const int lf = (best_var >> 3) & 3;
+        for (int f = 0; f < 3; ++f)
+            if (f != lf && (rc = trial(best_skin, (best_var & 7) | (f << 3)))) return rc;
         if (ntrials) *ntrials = nt;
         P.skin = best_skin;
         P.kernel_variant = best_var;
@@ -1633,7 +1666,7 @@ template<class R> class Engine : public EngineBase {
         a.seed = P.seed;
         a.rebuild_every = P.rebuild_every;
         a.variant = P.kernel_variant & 7;
-        a.nlist_lane = (P.kernel_variant >> 3) & 1;
+        a.nlist_lane = (P.kernel_variant >> 3) & 3;
         a.carry_forces = P.integrator == ORBC_INT_NOSE_HOOVER ? 1 : 0;
         a.zero_bulk = P.zero_bulk ? 1 : 0;
         a.ff = ffd.p;
@@ -1778,7 +1811,7 @@ int orbc_gpu_create(const orbc_params *p, orbc_handle **out) {
     *out = nullptr;
     if (!(p->dt > 0) || p->skin < 0 || (p->precision != ORBC_PREC_FP64 && p->precision != ORBC_PREC_MIXED) ||
         (p->integrator != ORBC_INT_LANGEVIN && p->integrator != ORBC_INT_NOSE_HOOVER) ||
-        (p->kernel_variant < 0 || p->kernel_variant > 15) || (p->zero_bulk != 0 && p->zero_bulk != 1)) {
+        (p->kernel_variant < 0 || p->kernel_variant > 23) || (p->zero_bulk != 0 && p->zero_bulk != 1)) {
         g_last_error = "create: invalid parameters";
         return ORBC_ERR_ARG;
     }
@@ -1837,6 +1870,14 @@ int orbc_gpu_upload_batch(orbc_handle *h, int nsys, const orbc_system_desc *sys,
 
 int orbc_gpu_set_state(orbc_handle *h, const double *x3, const double *n3, const double *v3, const double *o3) {
     return h ? h->e->set_state(x3, n3, v3, o3) : ORBC_ERR_ARG;
+}
+int orbc_gpu_set_state_f32(orbc_handle *h, int64_t first, int64_t count, int stride, const float *x, const float *n,
+                           const float *v, const float *o) {
+    return h ? h->e->set_state_f32(first, count, stride, x, n, v, o) : ORBC_ERR_ARG;
+}
+int orbc_gpu_download_f32(orbc_handle *h, int64_t first, int64_t count, int stride, float *x, float *n, float *v,
+                          float *o) {
+    return h ? h->e->download_f32(first, count, stride, x, n, v, o) : ORBC_ERR_ARG;
 }
 int orbc_gpu_step(orbc_handle *h, int nsteps, orbc_thermo *out) { return h ? h->e->step(nsteps, out) : ORBC_ERR_ARG; }
 int orbc_gpu_download(orbc_handle *h, double *x3, double *n3, double *v3, double *o3) {

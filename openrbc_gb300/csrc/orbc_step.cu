@@ -38,6 +38,28 @@ template<> __device__ __forceinline__ double4a ldg4<double>(const double4a *p) {
     return r;
 }
 
+/* Streaming (evict-first) access for data touched once per step -- the
+ * neighbour rows and the velocity / reference-position state -- so that it
+ * does not push out of L2 the positions and orientations that the next step
+ * gathers again. */
+template<class R> __device__ __forceinline__ typename Vec<R>::T4 ldcs4(const typename Vec<R>::T4 *p);
+template<> __device__ __forceinline__ float4 ldcs4<float>(const float4 *p) { return __ldcs(p); }
+template<> __device__ __forceinline__ double4a ldcs4<double>(const double4a *p) {
+    const double2 a = __ldcs(reinterpret_cast<const double2 *>(p));
+    const double2 b = __ldcs(reinterpret_cast<const double2 *>(p) + 1);
+    double4a r;
+    r.x = a.x;
+    r.y = a.y;
+    r.z = b.x;
+    r.w = b.y;
+    return r;
+}
+__device__ __forceinline__ void stcs4(float4 *p, const float4 &v) { __stcs(p, v); }
+__device__ __forceinline__ void stcs4(double4a *p, const double4a &v) {
+    __stcs(reinterpret_cast<double2 *>(p), make_double2(v.x, v.y));
+    __stcs(reinterpret_cast<double2 *>(p) + 1, make_double2(v.z, v.w));
+}
+
 __device__ __forceinline__ void inv_sqrt(float r2, float &r, float &rinv) {
     rinv = rsqrtf(r2);
     r = r2 * rinv;
@@ -275,8 +297,8 @@ __device__ __forceinline__ void particle_forces(const KArgs<R> &a, const FFDev<R
     if (V & 1) {
         /* software-pipelined: the entry two ahead and the gathers one ahead
          * are in flight while the current pair is evaluated */
-        uint32_t e1 = nin > 0 ? __ldg(nb) : 0u;
-        uint32_t e2 = nin > 1 ? __ldg(nb + stride) : 0u;
+        uint32_t e1 = nin > 0 ? __ldcs(nb) : 0u;
+        uint32_t e2 = nin > 1 ? __ldcs(nb + stride) : 0u;
         T4 pn, nn;
         if (nin > 0) {
             pn = ldg4<R>(pos + int(e1 & NB_MASK));
@@ -286,7 +308,7 @@ __device__ __forceinline__ void particle_forces(const KArgs<R> &a, const FFDev<R
             const uint32_t ent = e1;
             const T4 pj = pn, nj = nn;
             e1 = e2;
-            if (k + 2 < nin) e2 = __ldg(nb + int64_t(k + 2) * stride);
+            if (k + 2 < nin) e2 = __ldcs(nb + int64_t(k + 2) * stride);
             if (k + 1 < nin) {
                 pn = ldg4<R>(pos + int(e1 & NB_MASK));
                 nn = ldg4<R>(nrm + int(e1 & NB_MASK));
@@ -296,7 +318,7 @@ __device__ __forceinline__ void particle_forces(const KArgs<R> &a, const FFDev<R
     } else {
 #pragma unroll 2
         for (int k = 0; k < nin; ++k) {
-            const uint32_t ent = __ldg(nb + int64_t(k) * stride);
+            const uint32_t ent = __ldcs(nb + int64_t(k) * stride);
             const int j = int(ent & NB_MASK);
             pair(ent, ldg4<R>(pos + j), ldg4<R>(nrm + j));
         }
@@ -305,7 +327,7 @@ __device__ __forceinline__ void particle_forces(const KArgs<R> &a, const FFDev<R
     // the range; the orientation is only gathered for the few that came in.
 #pragma unroll 2
     for (int k = 0; k < nout; ++k) {
-        const uint32_t ent = __ldg(shell - int64_t(k) * stride);
+        const uint32_t ent = __ldcs(shell - int64_t(k) * stride);
         const int j = int(ent & NB_MASK);
         const T4 pj = ldg4<R>(pos + j);
         const T4 s = sh[ent >> NB_SHIFT];
@@ -575,7 +597,7 @@ __device__ __forceinline__ void langevin_particle(const KArgs<R> &a, const FFDev
     R e = 0;
     particle_forces<R, E, V>(a, F, i, cur, lp, w, pi, ni, sd, a.ss[s], sh, f, t, e, flags);
     const R dt = R(a.dt);
-    T4 v = a.vel[lp][i], o = a.omg[lp][i];
+    T4 v = ldcs4<R>(&a.vel[lp][i]), o = ldcs4<R>(&a.omg[lp][i]);
     if (zero_bulk && ty == 0) {  // zero_bulk_velocity on the lipids (src/zero_bulk_velocity.h:38-45)
         v.x -= R(__ldcg(&a.ss[s].vcom[0]));
         v.y -= R(__ldcg(&a.ss[s].vcom[1]));
@@ -596,7 +618,7 @@ __device__ __forceinline__ void langevin_particle(const KArgs<R> &a, const FFDev
     nn.z = gz * gi;
     // TRANSLATION: f -= gamma v + sigma r; v += f dt/m; x += v dt
     uint32_t r0, r1, r2;
-    philox3(uint32_t(a.tag[lp][i]), uint32_t(step), uint32_t((unsigned long long)step >> 32), uint32_t(s),
+    philox3(uint32_t(__ldcs(&a.tag[lp][i])), uint32_t(step), uint32_t((unsigned long long)step >> 32), uint32_t(s),
             uint32_t(a.seed), uint32_t(a.seed >> 32), r0, r1, r2);
     const R gam = F.gamma[ty], sig = F.sigma[ty];
     const R dtm = dt * F.inv_mass[ty];
@@ -612,9 +634,9 @@ __device__ __forceinline__ void langevin_particle(const KArgs<R> &a, const FFDev
     p.z += v.z * dt;
     a.pos[cur ^ 1][i] = p;
     a.nrm[cur ^ 1][i] = nn;
-    a.vel[lp][i] = v;
-    a.omg[lp][i] = o;
-    const T4 xr = a.xref[lp][i];
+    stcs4(&a.vel[lp][i], v);
+    stcs4(&a.omg[lp][i], o);
+    const T4 xr = ldcs4<R>(&a.xref[lp][i]);
     const R ddx = p.x - xr.x, ddy = p.y - xr.y, ddz = p.z - xr.z;
     md2 = float(ddx * ddx + ddy * ddy + ddz * ddz);
     if (!isfinite(p.x + p.y + p.z + v.x + v.y + v.z)) flags |= ERRB_NAN;

@@ -133,6 +133,26 @@ class Simulation:
         arrs = [_f64(a, self.n) for a in (x, n, v, o)]
         self._check(N.lib().orbc_gpu_set_state(self.h, *[_ptr(a) for a in arrs]))
 
+    def set_state_f32(self, x, n, v, o, first: int = 0):
+        """set_state from float32 arrays of shape (count, 3) or (count, 4) (the
+        reference's vector<real,3> / _VEC4 containers) for upload indices
+        [first, first + count)."""
+        arrs = [np.ascontiguousarray(a, dtype=np.float32) for a in (x, n, v, o)]
+        count, stride = arrs[0].shape
+        if any(a.shape != (count, stride) for a in arrs):
+            raise ValueError("set_state_f32: the four arrays need the same (count, 3|4) shape")
+        self._check(N.lib().orbc_gpu_set_state_f32(self.h, int(first), int(count), int(stride),
+                                                   *[a.ctypes.data for a in arrs]))
+
+    def download_f32(self, first: int = 0, count: Optional[int] = None, stride: int = 3):
+        """download into float32 arrays of shape (count, stride) for upload
+        indices [first, first + count)."""
+        count = self.n - first if count is None else count
+        out = [np.zeros((count, stride), np.float32) for _ in range(4)]
+        self._check(N.lib().orbc_gpu_download_f32(self.h, int(first), int(count), int(stride),
+                                                  *[a.ctypes.data for a in out]))
+        return tuple(out)
+
     def step(self, nsteps: int = 1) -> dict:
         th = N.Thermo()
         self._check(N.lib().orbc_gpu_step(self.h, int(nsteps), C.byref(th)))

@@ -267,10 +267,10 @@ def test_nose_hoover_mixed_tracks_fp64():
     assert abs(res["mixed"]["temperature"] - res["fp64"]["temperature"]) < 1e-3 * res["fp64"]["temperature"]
 
 
-@pytest.mark.parametrize("variant", [1, 2, 3, 4, 7, 8, 15])
+@pytest.mark.parametrize("variant", [1, 2, 3, 4, 7, 8, 15, 16, 19, 23])
 def test_force_kernel_forms_agree(variant):
     """The force-kernel forms evaluate the same pairs in the same order; the
-    two list-build forms (bit 3) find the same pairs."""
+    three list-build forms (bits 3-4) find the same pairs."""
     from openrbc_gb300 import RTParameter
     from openrbc_gb300 import Simulation
     w, table = small_rbc("wlc")
@@ -286,21 +286,33 @@ def test_force_kernel_forms_agree(variant):
     assert rel_l2(out[variant][1] - w["x"], out[0][1] - w["x"]) < 1e-4
 
 
-def test_list_build_forms_find_the_same_pairs():
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_list_build_forms_find_the_same_pairs(precision):
+    """The three list-build forms write the same rows (same entries, same
+    order) on the open whole cell and on a periodic sheet."""
     from openrbc_gb300 import RTParameter, Simulation
     w, table = small_rbc("wlc")
-    sets = []
-    for v in (0, 8):
-        p = RTParameter(init="lipid", kBT=1.0, precision="mixed", rseed=5)
-        with Simulation(p, bond_table=table, kernel_variant=v) as s:
-            upload_rbc(s, w)
-            s.step(7)
-            s.set_state(w["x"], w["n"], w["v"], w["o"])
-            s.rebuild()
-            counts, lst = s.neighbors()
-        sets.append((counts, lst))
-    assert np.array_equal(sets[0][0], sets[1][0])
-    assert np.array_equal(sets[0][1], sets[1][1])
+    lat, box = lattice_sys(n=8192, ncol=90)
+    for case in ("cell", "sheet"):
+        sets = []
+        for v in (0, 8, 16):
+            p = RTParameter(init="lipid", kBT=1.0, precision=precision, rseed=5)
+            if case == "cell":
+                with Simulation(p, bond_table=table, kernel_variant=v) as s:
+                    upload_rbc(s, w)
+                    s.step(7)
+                    s.set_state(w["x"], w["n"], w["v"], w["o"])
+                    s.rebuild()
+                    sets.append(s.neighbors())
+            else:
+                with Simulation(p, box=box, periodic=(1, 1, 0), kernel_variant=v) as s:
+                    s.upload(lat["x"], lat["n"], lat["v"], lat["o"], lat["type"], lat["tag"])
+                    s.step(9)
+                    s.rebuild()
+                    sets.append(s.neighbors())
+        for counts, lst in sets[1:]:
+            assert np.array_equal(sets[0][0], counts)
+            assert np.array_equal(sets[0][1], lst)
 
 
 def test_autotune_restores_state_and_keeps_stepping():
@@ -314,7 +326,7 @@ def test_autotune_restores_state_and_keeps_stepping():
         step0 = s.thermo()["step"]
         trials = s.autotune(trial_steps=4)
         after = s.download()
-        assert len(trials) == 22 and all(t["ms_per_step"] > 0 for t in trials)  # 5 skins x 4 forms + 2 forms
+        assert len(trials) == 23 and all(t["ms_per_step"] > 0 for t in trials)  # 5 skins x 4 forms + 3 forms
         assert s.thermo()["step"] == step0
         d = min_image_diff(after[0], before[0], box, (1, 1, 0))
         assert np.abs(d).max() < 1e-5
