@@ -210,8 +210,10 @@ def run_reference(args, rank, ws):
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * n / cb["value"], "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": f"rbc-evans-fung-{n}", "n_particles": n, "integrator": "langevin",
-                       "dt": DT, "kT": KT},
+            "config": {"workload": f"rbc-evans-fung-{n}", "n_particles": n, "n_lipid": args.n_lipid,
+                       "anchors": n - args.n_lipid, "bonds": int(len(w["bonds"])), "faces": int(len(w["faces"])),
+                       "integrator": "langevin", "dt": DT, "kT": KT, "precision": "fp32 (the reference's real)",
+                       "parallelism": f"host threads x{cb['cores']}"},
             "cpu_baseline": cb, "e2e": {"value": cb["value"], "unit": "particle-steps/s",
                                         "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)

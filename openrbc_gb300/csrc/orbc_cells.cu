@@ -196,8 +196,8 @@ template<class R> __global__ void __launch_bounds__(256) k_rebin(KArgs<R> a, int
             R o[3] = {p.x, p.y, p.z};
 #pragma unroll
             for (int d = 0; d < 3; ++d) {
-                const R L = R(sd.Lc[d]);
-                const R invL = R(1.0 / sd.Lc[d]);
+                const R L = lc_of<R>(sd, d);
+                const R invL = inv_lc_of<R>(sd, d);
                 const int k = int(floor(add_rn(mul_rn(o[d], invL), R(0.5))));
                 int nc = cc[d] + k;
                 if (sd.per[d]) {
@@ -339,7 +339,7 @@ template<class R> __global__ void __launch_bounds__(128) k_nlist(KArgs<R> a, int
         const SysDev &sd = a.sys[a.blk_sys[i / SYS_PAD]];  // one system per warp (SYS_PAD-aligned)
         const int c = a.cell[lp][i];
         const int cc[3] = {cx_of(c), cy_of(c), cz_of(c)};
-        const R L[3] = {R(sd.Lc[0]), R(sd.Lc[1]), R(sd.Lc[2])};
+        const R L[3] = {lc_of<R>(sd, 0), lc_of<R>(sd, 1), lc_of<R>(sd, 2)};
         // Entries inside the pair's interaction range fill rows 0, 1, ... of
         // this slot's column; skin-shell entries fill rows cap-1, cap-2, ...
         int nin = 0, nout = 0, total = 0;
@@ -568,7 +568,7 @@ template<class R> __global__ void __launch_bounds__(128) k_nlist2(KArgs<R> a, in
     const SysDev &sd = a.sys[a.blk_sys[i / SYS_PAD]];  // one system per warp (SYS_PAD-aligned)
     const int c = a.cell[lp][i];
     const int cc[3] = {cx_of(c), cy_of(c), cz_of(c)};
-    const R L[3] = {R(sd.Lc[0]), R(sd.Lc[1]), R(sd.Lc[2])};
+    const R L[3] = {lc_of<R>(sd, 0), lc_of<R>(sd, 1), lc_of<R>(sd, 2)};
     // the expressions of k_nlist's shifted() and dist2()
     auto shifted = [&](const T4 &q, int dx, int dy, int dz) {
         T4 r = q;

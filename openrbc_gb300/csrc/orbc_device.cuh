@@ -115,7 +115,19 @@ struct SysDev {
     int nlipid, pad1;               // lipids in the system (bulk-velocity removal)
     int gbase, ngrp;                // reduction groups of FIN_GROUP step blocks (first, count)
     double kv, V0, ka, A0, Q;
+    double invLc[3];                // 1 / Lc
+    float Lcf[3], invLcf[3];        // Lc and 1 / Lc rounded to float
 };
+
+/* Cell size and its inverse in the working precision (the FP32 kernels take
+ * them ready-made: a per-particle FP64 division or conversion would run on
+ * the FP64 pipe). */
+template<class R> __device__ __forceinline__ R lc_of(const SysDev &s, int d);
+template<> __device__ __forceinline__ float lc_of<float>(const SysDev &s, int d) { return s.Lcf[d]; }
+template<> __device__ __forceinline__ double lc_of<double>(const SysDev &s, int d) { return s.Lc[d]; }
+template<class R> __device__ __forceinline__ R inv_lc_of(const SysDev &s, int d);
+template<> __device__ __forceinline__ float inv_lc_of<float>(const SysDev &s, int d) { return s.invLcf[d]; }
+template<> __device__ __forceinline__ double inv_lc_of<double>(const SysDev &s, int d) { return s.invLc[d]; }
 
 /* Cell id inside a system: 4 x 4 x 4 tiles of cells in row-major tile
  * order, Morton (x, y, z interleaved) inside a tile.  Particles are sorted by

@@ -460,6 +460,10 @@ template<class R> class Engine : public EngineBase {
                     sd.wlo[dd] = d.lo[dd];
                     sd.whi[dd] = d.hi[dd];
                 }
+                // the kernels' copies: no FP64 division or conversion per particle
+                sd.invLc[dd] = 1.0 / sd.Lc[dd];
+                sd.Lcf[dd] = float(sd.Lc[dd]);
+                sd.invLcf[dd] = float(sd.invLc[dd]);
             }
             const int64_t ns = e - b;
             const int64_t npad_s = std::max<int64_t>(SYS_PAD, (ns + SYS_PAD - 1) / SYS_PAD * SYS_PAD);

@@ -171,9 +171,9 @@ __device__ __forceinline__ void rel_pos(const SysDev &sd, int cj, int ci, const 
     if (sd.per[0]) d0 = wrap_delta(d0, sd.nc[0]);
     if (sd.per[1]) d1 = wrap_delta(d1, sd.nc[1]);
     if (sd.per[2]) d2 = wrap_delta(d2, sd.nc[2]);
-    dx = R(d0) * R(sd.Lc[0]) + (pj.x - pi.x);
-    dy = R(d1) * R(sd.Lc[1]) + (pj.y - pi.y);
-    dz = R(d2) * R(sd.Lc[2]) + (pj.z - pi.z);
+    dx = R(d0) * lc_of<R>(sd, 0) + (pj.x - pi.x);
+    dy = R(d1) * lc_of<R>(sd, 1) + (pj.y - pi.y);
+    dz = R(d2) * lc_of<R>(sd, 2) + (pj.z - pi.z);
 }
 
 /* Bond force on i, F_i = kappa(r) (x_j - x_i):  HARMONIC is
@@ -257,7 +257,7 @@ __device__ __forceinline__ void particle_forces(const KArgs<R> &a, const FFDev<R
                                                 int &flags) {
     using T4 = typename Vec<R>::T4;
     const int ty = w_type(w);
-    const R Lx = R(sd.Lc[0]), Ly = R(sd.Lc[1]), Lz = R(sd.Lc[2]);
+    const R Lx = lc_of<R>(sd, 0), Ly = lc_of<R>(sd, 1), Lz = lc_of<R>(sd, 2);
     const T4 *__restrict__ pos = a.pos[cur];
     const T4 *__restrict__ nrm = a.nrm[cur];
     const uint32_t *__restrict__ nb = a.nbr + nbr_index(i, 0, a.cap);

@@ -334,3 +334,56 @@ def test_autotune_restores_state_and_keeps_stepping():
             assert np.abs(u - v).max() < 1e-6
         th = s.step(10)
         assert th["step"] == step0 + 10 and np.isfinite(th["temperature"])
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("rebuild_every", [1, None])
+def test_batched_cell_ensemble_matches_each_cell_alone(precision, rebuild_every):
+    """Whole-cell ensemble (several red cells, each with its own spectrin
+    network and its own volume target) in one handle: every cell evolves as it
+    does alone (Nose-Hoover, no noise), with its own thermostat, area and
+    volume.  The batch shares one rebuild decision (a rebuild re-sorts every
+    cell, which reorders the force sums of the cells that did not need it), so
+    with a list rebuilt every step the runs agree bit for bit, and with the
+    displacement rule to rounding."""
+    from openrbc_gb300 import RTParameter, Simulation, workloads
+    table = {4: {"style": 2, "K": 1.0, "r0": 1.0, "R": 2.2}}
+    cells, base = [], 0
+    for k, vf in enumerate((0.97, 1.0, 1.03)):
+        w = workloads.rbc(n_lipid=20_000, freq=5, kT=1.0, seed=40 + k)
+        shift = base - int(w["tag"].min())
+        w["tag"] = w["tag"] + shift
+        w["bonds"] = w["bonds"].copy()
+        w["bonds"][:, 1:] += shift
+        w["faces"] = w["faces"] + shift
+        base = int(w["tag"].max()) + 1
+        c = dict(w["constraint"])
+        c["V0"] *= vf
+        cells.append((w, {"lo": (-1000.0,) * 3, "hi": (1000.0,) * 3, "kv": c["kv"], "V0": c["V0"],
+                          "ka": c["ka"], "A0": c["A0"]}))
+
+    def run(group):
+        p = RTParameter(init="lipid", kBT=1.0, precision=precision, integrator="nose-hoover")
+        cat = lambda key: np.concatenate([w[key] for w, _ in group])
+        off = np.cumsum([0] + [len(w["x"]) for w, _ in group])
+        with Simulation(p, bond_table=table, rebuild_every=rebuild_every) as s:
+            s.upload_batch([d for _, d in group], cat("x"), cat("n"), cat("v"), cat("o"), cat("type"), cat("tag"),
+                           off, bonds=cat("bonds"), bond_r0=cat("bond_r0"), faces=cat("faces"))
+            s.step(12)
+            return s.download(), [s.thermo(k) for k in range(len(group))], off
+
+    state, th, off = run(cells)
+    tol = 0.0 if rebuild_every == 1 else (1e-12 if precision == "fp64" else 1e-5)
+    for k in range(len(cells)):
+        alone, th1, _ = run([cells[k]])
+        a, b = int(off[k]), int(off[k + 1])
+        w = cells[k][0]
+        if tol == 0.0:
+            for u, v in zip(state, alone):
+                assert np.array_equal(u[a:b], v)
+        else:
+            assert rel_l2(state[0][a:b] - w["x"], alone[0] - w["x"]) < tol
+            assert rel_l2(state[2][a:b], alone[2]) < tol
+        for key in ("zeta", "ke2", "area", "volume"):
+            assert abs(th[k][key] - th1[0][key]) <= tol * max(1.0, abs(th1[0][key]))
+    assert len({t["volume"] for t in th}) == len(cells)  # the volume targets differ
