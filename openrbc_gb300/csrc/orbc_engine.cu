@@ -709,11 +709,13 @@ template<class R> class Engine : public EngineBase {
             CK(cudaStreamWaitEvent(st, xev[c], 0));
             launch_set_state<R, TH>(a, d, d + m, d + 2 * m, d + 3 * m, first + k0, first + k1, first, stride, st);
         }
-        launch_vcom<R>(a, st);  // temperature and lipid mean of the new velocities
+        // temperature and lipid mean of the new velocities; the lite Langevin
+        // step needs neither (thermo() reduces them on demand)
+        vcom_valid = !lite();
+        if (vcom_valid) launch_vcom<R>(a, st);
         CK(cudaStreamSynchronize(cs));  // the caller may reuse its arrays on return
         CK(cudaGetLastError());
         nh_primed = false;
-        vcom_valid = true;
         return ORBC_OK;
     }
 
