@@ -29,7 +29,7 @@ constexpr uint32_t NB_MASK = (1u << 27) - 1u;
 constexpr int NB_SHIFT = 27;
 constexpr int MAX_SLOTS = 1 << 27;
 constexpr int NPART = 8;         // per-block partial sums: ke2, epot, maxd2, flags, lipid sum v (3), pad
-constexpr int FIN_GROUP = 64;    // step blocks per reduction group
+constexpr int RED_GROUP = 256;   // warp partials (of 32 slots) per reduction group
 constexpr int MESH_CHUNK = 1024; // faces per block of the area / volume kernel
 
 enum : int {
@@ -113,7 +113,7 @@ struct SysDev {
     int face_begin, face_end;
     int mblk_begin, mblk_end;       // blocks of the area / volume kernel (MESH_CHUNK faces each)
     int nlipid, pad1;               // lipids in the system (bulk-velocity removal)
-    int gbase, ngrp;                // reduction groups of FIN_GROUP step blocks (first, count)
+    int gbase, ngrp;                // reduction groups of RED_GROUP warps (first, count)
     double kv, V0, ka, A0, Q;
     double invLc[3];                // 1 / Lc
     float Lcf[3], invLcf[3];        // Lc and 1 / Lc rounded to float
@@ -181,9 +181,8 @@ template<class R> struct KArgs {
     int2 *ranges;            // cell -> [begin, end) of its slots
     int *slot_of_home;
     int *blk_sys;            // system of each 256-slot block
-    double *partial;         // [nblk][NPART]
-    double *gpartial;        // [ngroups][NPART]: sums of FIN_GROUP consecutive blocks of one system
-    unsigned *gcount;        // [ngroups] block tickets of each group (zero between kernels)
+    double *partial;         // [npad / 32][NPART]: warp partials
+    double *gpartial;        // [ngroups][NPART]: sums of RED_GROUP consecutive warps of one system
     int ngroups;
     Scalars *S;
     SysDev *sys;

@@ -468,7 +468,7 @@ template<class R> class Engine : public EngineBase {
             const int64_t ns = e - b;
             const int64_t npad_s = std::max<int64_t>(SYS_PAD, (ns + SYS_PAD - 1) / SYS_PAD * SYS_PAD);
             sd.gbase = ngroups_total;
-            sd.ngrp = int((npad_s / STEP_BS + FIN_GROUP - 1) / FIN_GROUP);
+            sd.ngrp = int((npad_s / 32 + RED_GROUP - 1) / RED_GROUP);
             ngroups_total += sd.ngrp;
             sd.off = int(off);
             sd.npad = int(npad_s);
@@ -610,8 +610,7 @@ template<class R> class Engine : public EngineBase {
         }
         ntiles = sort_tiles(npad);
         if (epart.alloc(size_t(npad)) || faces.alloc(hfaces.size()) || ranges.alloc(size_t(total_cells)) ||
-            soh.alloc(size_t(n)) || blk_sys.alloc(size_t(nb256)) || partial.alloc(size_t(nblk) * NPART) || gpartial.alloc(size_t(ngroups_total) * NPART) ||
-            gcount.alloc(size_t(ngroups_total)) ||
+            soh.alloc(size_t(n)) || blk_sys.alloc(size_t(nb256)) || partial.alloc(size_t(npad / 32) * NPART) || gpartial.alloc(size_t(ngroups_total) * NPART) ||
             Sd.alloc(1) || sysd.alloc(size_t(nsys)) || ssd.alloc(size_t(nsys)) || counts.alloc(size_t(256) * ntiles) ||
             dtot.alloc(256) || invd.alloc(size_t(npad)) || ffd.alloc(1) || nnb.alloc(size_t(npad)) ||
             stage.alloc(size_t(n) * 12) || mesh_bs.alloc(hmbs.size()) || mesh_part.alloc(hmbs.size() * 2 + 2))
@@ -640,9 +639,8 @@ template<class R> class Engine : public EngineBase {
         CK(cudaMemcpyAsync(blk_sys.p, hbs.data(), hbs.size() * sizeof(int), cudaMemcpyHostToDevice, st));
         CK(cudaMemcpyAsync(sysd.p, hsys.data(), hsys.size() * sizeof(SysDev), cudaMemcpyHostToDevice, st));
         CK(cudaMemsetAsync(ranges.p, 0, size_t(total_cells) * sizeof(int2), st));
-        CK(cudaMemsetAsync(partial.p, 0, size_t(nblk) * NPART * sizeof(double), st));
+        CK(cudaMemsetAsync(partial.p, 0, size_t(npad / 32) * NPART * sizeof(double), st));
         CK(cudaMemsetAsync(gpartial.p, 0, size_t(ngroups_total) * NPART * sizeof(double), st));
-        CK(cudaMemsetAsync(gcount.p, 0, size_t(ngroups_total) * sizeof(unsigned), st));
         CK(cudaMemsetAsync(epart.p, 0, size_t(npad) * sizeof(double), st));
         CK(cudaMemsetAsync(nnb.p, 0, size_t(npad) * sizeof(int), st));
         // other parity copies start equal (gather overwrites them before use)
@@ -1002,8 +1000,10 @@ template<class R> class Engine : public EngineBase {
     }
     /* Langevin without energy or bulk-velocity removal: no per-step sums */
     bool lite() const { return P.integrator == ORBC_INT_LANGEVIN && !P.energy && !P.zero_bulk; }
+    /* per step: the force kernel and k_advance (lite) or k_reduce; Nose-Hoover
+     * adds k_nh_initial and its k_reduce; the mesh kernel; the condition kernel */
     int fixed_launches_per_step() const {
-        int k = 1 + (has_mesh ? 1 : 0) + (P.integrator == ORBC_INT_NOSE_HOOVER ? 1 : 0) + (lite() ? 1 : 0);
+        int k = (P.integrator == ORBC_INT_NOSE_HOOVER ? 4 : 2) + (has_mesh ? 1 : 0);
         return k + (graph_cond ? 1 : 0);
     }
     int rebuild_launches() const { return 1 + 3 * passes + 1 + 1; }
@@ -1108,7 +1108,7 @@ template<class R> class Engine : public EngineBase {
             launch_vcom<R>(a, st);
             CK(cudaGetLastError());
             vcom_valid = true;
-            extra += 1;
+            extra += 2;  // k_vcom + k_reduce
         }
         if (P.integrator == ORBC_INT_NOSE_HOOVER && !nh_primed) {
             launch_rebuild<R>(a, st, true);
@@ -1116,7 +1116,7 @@ template<class R> class Engine : public EngineBase {
             launch_nh_prologue<R>(a, st);
             CK(cudaGetLastError());
             nh_primed = true;
-            extra += 1 + (has_mesh ? 1 : 0);
+            extra += rebuild_launches() + (has_mesh ? 1 : 0) + 2;  // gated rebuild, mesh, k_nh_final + k_reduce
         }
         CK(cudaEventRecord(ev0, st));
         if (P.use_graph && nsteps > 0) {
@@ -1653,7 +1653,6 @@ template<class R> class Engine : public EngineBase {
         a.blk_sys = blk_sys.p;
         a.partial = partial.p;
         a.gpartial = gpartial.p;
-        a.gcount = gcount.p;
         a.ngroups = ngroups_total;
         a.S = Sd.p;
         a.sys = sysd.p;
@@ -1755,7 +1754,6 @@ template<class R> class Engine : public EngineBase {
     DevBuf<uint32_t> skey[2];
     DevBuf<int> sval[2];
     DevBuf<double> epart, partial, stage, gpartial;
-    DevBuf<unsigned> gcount;
     int ngroups_total = 0;
     DevBuf<int4> faces;
     DevBuf<int2> ranges;

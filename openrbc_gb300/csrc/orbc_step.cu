@@ -227,13 +227,6 @@ __device__ __forceinline__ void prefetch_warp_list(const uint32_t *nbr, int i, i
     }
 }
 
-template<class R> __device__ __forceinline__ void stage_ff(FFDev<R> *dst, const FFDev<R> *src) {
-    const int nw = int(sizeof(FFDev<R>) / sizeof(int));
-    const int *s = reinterpret_cast<const int *>(src);
-    int *d = reinterpret_cast<int *>(dst);
-    for (int k = threadIdx.x; k < nw; k += blockDim.x) d[k] = __ldg(s + k);
-}
-
 template<class R> __device__ __forceinline__ void init_shift(typename Vec<R>::T4 *sh) {
     if (threadIdx.x < 27) {
         const int c = threadIdx.x;
@@ -406,7 +399,6 @@ __device__ __forceinline__ void philox3(uint32_t c0, uint32_t c1, uint32_t c2, u
 }
 template<class R> __device__ __forceinline__ R u11(uint32_t u) { return R(u >> 8) * R(1.0 / 8388608.0) - R(1); }
 
-constexpr int STEP_WARPS = STEP_BS / 32;
 
 /* Reflective walls (src/integrate_nh.h:124-144) on the axes where the system
  * has them (wlo < whi), applied in the frame of the particle's cell. */
@@ -432,24 +424,17 @@ __device__ __forceinline__ void bounce_walls(const SysDev &sd, int c, typename V
 
 enum { MODE_LANGEVIN = 0, MODE_NH_FINAL = 1, MODE_NH_INITIAL = 2, MODE_FORCES = 3, MODE_VCOM = 4 };
 
-/* Block partial sums -> per-system totals, deterministically and without a
- * serial tail: each block writes its partial; the last block of each group of
- * FIN_GROUP consecutive blocks of a system (group ticket) sums the group's
- * partials in block order; the last group to finish (global ticket) sums each
- * system's group partials in group order and updates the thermostat, the
- * rebuild flag, the step counter and the buffer parity.  Partial layout:
- * ke2, epot, max displacement^2, error flags, lipid sum v (3). */
+/* Per-system sums, first level.  Every warp reduces its particles' values --
+ * the sums in the working precision (in mixed mode the FP64 pipe would cost
+ * more than the force loop), the maximum and the flags on integers -- and
+ * lane 0 stores them in FP64 as the warp's partial.  No barrier, fence or
+ * atomic: k_reduce, launched next on the stream, sums each system's partials
+ * in a fixed order.  Partial layout: ke2, epot, max displacement^2, error
+ * flags, lipid sum v (3).  All 32 lanes of the warp must call it; i is the
+ * caller's slot (a warp never straddles two systems). */
 template<class R>
-__device__ __forceinline__ void finish(const KArgs<R> &a, R ke, R ep, float md2, int flags, int mode, int count_step,
-                                       R vx = R(0), R vy = R(0), R vz = R(0)) {
-    __shared__ double sv[STEP_WARPS][NPART];
-    __shared__ double red[NPART][FIN_GROUP];
-    __shared__ int last, gflags;
-    __shared__ double gmax;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    // Warp level in the working precision (in mixed mode the FP64 pipe would
-    // cost more than the whole force loop) with the maximum and the flags on
-    // integers; from the warp partials on, FP64 in a fixed order.
+__device__ __forceinline__ void warp_partials(const KArgs<R> &a, int i, R ke, R ep, float md2, int flags,
+                                              R vx = R(0), R vy = R(0), R vz = R(0)) {
     R v[5] = {ke, ep, vx, vy, vz};
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -459,86 +444,78 @@ __device__ __forceinline__ void finish(const KArgs<R> &a, R ke, R ep, float md2,
     // md2 >= 0 (or NaN, flagged separately): the bit order is the value order
     const unsigned wmax = __reduce_max_sync(0xffffffffu, __float_as_uint(md2));
     const int wfl = int(__reduce_or_sync(0xffffffffu, unsigned(flags)));
-    if (lane == 0) {
-        sv[warp][0] = double(v[0]);
-        sv[warp][1] = double(v[1]);
-        sv[warp][2] = double(__uint_as_float(wmax));
-        sv[warp][3] = double(wfl);
-        sv[warp][4] = double(v[2]);
-        sv[warp][5] = double(v[3]);
-        sv[warp][6] = double(v[4]);
+    if ((threadIdx.x & 31) == 0) {
+        double *p = a.partial + int64_t(i >> 5) * NPART;
+        p[0] = double(v[0]);
+        p[1] = double(v[1]);
+        p[2] = double(__uint_as_float(wmax));
+        p[3] = double(wfl);
+        p[4] = double(v[2]);
+        p[5] = double(v[3]);
+        p[6] = double(v[4]);
     }
-    __syncthreads();
-    const int blk = blockIdx.x;
-    const int s = a.blk_sys[(blk * STEP_BS) / SYS_PAD];
+}
+
+__device__ __forceinline__ double combine_part(int k, double x, double y) {
+    return k == 2 ? fmax(x, y) : (k == 3 ? double(int(x) | int(y)) : x + y);
+}
+
+/* Per-system sums, second and third level, after a kernel that wrote warp
+ * partials.  Block g sums the RED_GROUP warp partials of reduction group g
+ * (RED_GROUP x 32 consecutive slots of one system) in a fixed-shape tree; the
+ * last block to finish (ticket) gives each system to one warp, which adds the
+ * system's group partials in a fixed order, and applies the mode's update:
+ * thermostat, kinetic energy, potential energy, bulk velocity, rebuild rule,
+ * step counter, buffer parity. */
+template<class R> __global__ void __launch_bounds__(RED_GROUP) k_reduce(KArgs<R> a, int mode, int count_step) {
+    __shared__ double red[7][RED_GROUP];
+    __shared__ double wmax[RED_GROUP / 32];
+    __shared__ int wfl[RED_GROUP / 32];
+    __shared__ int last;
+    const int g = blockIdx.x, t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    int s = 0;
+    while (s + 1 < a.nsys && g >= a.sys[s + 1].gbase) ++s;
     const SysDev &sd = a.sys[s];
-    const int b0 = sd.off / STEP_BS, nbs = sd.npad / STEP_BS;
-    const int gl = (blk - b0) / FIN_GROUP;              // group within the system
-    const int g = sd.gbase + gl;                        // global group
-    const int gb0 = b0 + gl * FIN_GROUP, gn = min(FIN_GROUP, nbs - gl * FIN_GROUP);
-    auto combine = [](int k, double x, double y) {
-        return k == 2 ? fmax(x, y) : (k == 3 ? double(int(x) | int(y)) : x + y);
-    };
-    if (threadIdx.x == 0) {
-        double w[7];
-        for (int k = 0; k < 7; ++k) w[k] = sv[0][k];
-        for (int q = 1; q < STEP_WARPS; ++q)
-            for (int k = 0; k < 7; ++k) w[k] = combine(k, w[k], sv[q][k]);
-        double *p = a.partial + int64_t(blk) * NPART;
-        for (int k = 0; k < 7; ++k) p[k] = w[k];
-        __threadfence();
-        last = atomicAdd(&a.gcount[g], 1u) == unsigned(gn - 1);
-    }
+    const int gl = g - sd.gbase;
+    const int64_t w0 = int64_t(sd.off / 32) + int64_t(gl) * RED_GROUP;
+    const int nw = min(RED_GROUP, sd.npad / 32 - gl * RED_GROUP);
+    for (int k = 0; k < 7; ++k) red[k][t] = t < nw ? __ldcg(a.partial + (w0 + t) * NPART + k) : 0.0;
     __syncthreads();
-    if (!last) return;
-    __threadfence();
-    // group: thread t < gn loads block gb0 + t; fixed-shape tree over FIN_GROUP slots
-    for (int k = 0; k < 7; ++k)
-        for (int t = threadIdx.x; t < FIN_GROUP; t += blockDim.x)
-            red[k][t] = t < gn ? __ldcg(a.partial + int64_t(gb0 + t) * NPART + k) : (k == 2 || k == 3 ? 0.0 : 0.0);
-    __syncthreads();
-    for (int h = FIN_GROUP / 2; h > 0; h >>= 1) {
-        for (int t = threadIdx.x; t < h * 7; t += blockDim.x) {
-            const int k = t / h, u = t % h;
-            red[k][u] = combine(k, red[k][u], red[k][u + h]);
-        }
+    for (int h = RED_GROUP / 2; h > 0; h >>= 1) {
+        if (t < h)
+            for (int k = 0; k < 7; ++k) red[k][t] = combine_part(k, red[k][t], red[k][t + h]);
         __syncthreads();
     }
-    if (threadIdx.x == 0) {
+    if (t == 0) {
         double *gp = a.gpartial + int64_t(g) * NPART;
         for (int k = 0; k < 7; ++k) gp[k] = red[k][0];
-        a.gcount[g] = 0;
         __threadfence();
-        last = atomicAdd(&a.S->blk_counter, 1u) == unsigned(a.ngroups - 1);
+        last = atomicAdd(&a.S->blk_counter, 1u) == gridDim.x - 1;
     }
     __syncthreads();
     if (!last) return;
     __threadfence();
-    // per system: its groups in order (strided sums, then the same tree)
-    for (int q = 0; q < a.nsys; ++q) {
+    double mymax = 0.0;
+    int myfl = 0;
+    for (int q = warp; q < a.nsys; q += RED_GROUP / 32) {
         const SysDev &sq = a.sys[q];
-        for (int k = 0; k < 7; ++k)
-            for (int t = threadIdx.x; t < FIN_GROUP; t += blockDim.x) {
-                double acc = k == 2 || k == 3 ? 0.0 : 0.0;
-                for (int u = t; u < sq.ngrp; u += FIN_GROUP)
-                    acc = combine(k, acc, __ldcg(a.gpartial + int64_t(sq.gbase + u) * NPART + k));
-                red[k][t] = acc;
-            }
-        __syncthreads();
-        for (int h = FIN_GROUP / 2; h > 0; h >>= 1) {
-            for (int t = threadIdx.x; t < h * 7; t += blockDim.x) {
-                const int k = t / h, u = t % h;
-                red[k][u] = combine(k, red[k][u], red[k][u + h]);
-            }
-            __syncthreads();
+        double v[7];
+        for (int k = 0; k < 7; ++k) {
+            double acc = 0.0;
+            for (int u = lane; u < sq.ngrp; u += 32)
+                acc = combine_part(k, acc, __ldcg(a.gpartial + int64_t(sq.gbase + u) * NPART + k));
+            v[k] = acc;
         }
-        if (threadIdx.x == 0) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+            for (int k = 0; k < 7; ++k) v[k] = combine_part(k, v[k], __shfl_xor_sync(0xffffffffu, v[k], o));
+        if (lane == 0) {
             SysState &ss = a.ss[q];
-            const double k2 = red[0][0], e = red[1][0];
+            const double k2 = v[0], e = v[1];
             if ((mode == MODE_LANGEVIN || mode == MODE_NH_INITIAL || mode == MODE_VCOM) && sq.nlipid > 0) {
-                ss.vcom[0] = red[4][0] / double(sq.nlipid);
-                ss.vcom[1] = red[5][0] / double(sq.nlipid);
-                ss.vcom[2] = red[6][0] / double(sq.nlipid);
+                ss.vcom[0] = v[4] / double(sq.nlipid);
+                ss.vcom[1] = v[5] / double(sq.nlipid);
+                ss.vcom[2] = v[6] / double(sq.nlipid);
             }
             if (mode == MODE_VCOM) {
                 ss.ke2 = k2;
@@ -553,15 +530,22 @@ __device__ __forceinline__ void finish(const KArgs<R> &a, R ke, R ep, float md2,
                 ss.ke2 = k2;
                 if (mode == MODE_NH_FINAL) ss.epot = e;
             }
-            // system max displacement and flags feed the global decision
-            gmax = q == 0 ? red[2][0] : fmax(gmax, red[2][0]);
-            gflags = (q == 0 ? 0 : gflags) | int(red[3][0]);
+            mymax = fmax(mymax, v[2]);
+            myfl |= int(v[3]);
         }
-        __syncthreads();
     }
-    if (threadIdx.x == 0) {
-        const double m = gmax;
-        const int fl = gflags;
+    if (lane == 0) {
+        wmax[warp] = mymax;
+        wfl[warp] = myfl;
+    }
+    __syncthreads();
+    if (t == 0) {
+        double m = 0.0;
+        int fl = 0;
+        for (int w = 0; w < RED_GROUP / 32; ++w) {
+            m = fmax(m, wmax[w]);
+            fl |= wfl[w];
+        }
         Scalars *S = a.S;
         S->error |= fl;
         if (mode == MODE_LANGEVIN || mode == MODE_NH_INITIAL) {
@@ -650,18 +634,18 @@ __device__ __forceinline__ void langevin_particle(const KArgs<R> &a, const FFDev
 }
 
 /* Langevin step with the per-system sums (energy, bulk-velocity removal):
- * force-field table staged in shared memory, block partials reduced by the
- * last block. */
-template<class R, bool E, int V> __global__ void __launch_bounds__(STEP_BS, (V & 2) ? 6 : 8) k_step_langevin(KArgs<R> a) {
+ * the structure of the lite kernel below (small blocks, force-field table
+ * through the read-only path) plus warp partials, summed per system by
+ * k_reduce after the kernel. */
+template<class R, bool E, int V> __global__ void __launch_bounds__(LITE_BS, 16) k_step_langevin(KArgs<R> a) {
     using T4 = typename Vec<R>::T4;
     __shared__ T4 sh[27];
-    __shared__ FFDev<R> F;
-    stage_ff<R>(&F, a.ff);
     init_shift<R>(sh);
+    const FFDev<R> *__restrict__ Fp = a.ff;
     const int cur = __ldcg(&a.S->cur), lp = __ldcg(&a.S->lp);
     const long long step = __ldcg(&a.S->step);
-    const int i = blockIdx.x * STEP_BS + threadIdx.x;
-    const int s = a.blk_sys[(blockIdx.x * STEP_BS) / SYS_PAD];
+    const int i = blockIdx.x * LITE_BS + threadIdx.x;
+    const int s = a.blk_sys[i / SYS_PAD];
     const T4 pi = a.pos[cur][i];
     prefetch_warp_list(a.nbr, i, a.cap, a.nnb[i]);
     const int w = wbits(pi.w);
@@ -669,9 +653,9 @@ template<class R, bool E, int V> __global__ void __launch_bounds__(STEP_BS, (V &
     float md2 = 0.f;
     int flags = 0;
     if (w_type(w) != GHOST)
-        langevin_particle<R, E, V>(a, F, sh, i, s, cur, lp, step, pi, w, a.zero_bulk != 0, ke, ep, md2, flags, vsx,
+        langevin_particle<R, E, V>(a, *Fp, sh, i, s, cur, lp, step, pi, w, a.zero_bulk != 0, ke, ep, md2, flags, vsx,
                                    vsy, vsz);
-    finish<R>(a, ke, ep, md2, flags, MODE_LANGEVIN, 1, vsx, vsy, vsz);
+    warp_partials<R>(a, i, ke, ep, md2, flags, vsx, vsy, vsz);
 }
 
 /* Langevin step without per-system sums (no energy, no bulk-velocity
@@ -782,15 +766,17 @@ __global__ void __launch_bounds__(LITE_BS, (V & 2) ? 12 : 16) k_minimize(KArgs<R
     }
 }
 
-template<class R, bool E, int V> __global__ void __launch_bounds__(STEP_BS, (V & 2) ? 6 : 8) k_nh_final(KArgs<R> a, int count_step) {
+/* Nose-Hoover second half (post_toque_final_update, src/integrate_nh.h:237-273)
+ * fused with the forces: the lite structure plus warp partials for the
+ * kinetic-energy sum that k_reduce turns into the thermostat update. */
+template<class R, bool E, int V> __global__ void __launch_bounds__(LITE_BS, 16) k_nh_final(KArgs<R> a, int count_step) {
     using T4 = typename Vec<R>::T4;
     __shared__ T4 sh[27];
-    __shared__ FFDev<R> F;
-    stage_ff<R>(&F, a.ff);
     init_shift<R>(sh);
+    const FFDev<R> &F = *a.ff;
     const int cur = __ldcg(&a.S->cur), lp = __ldcg(&a.S->lp);
-    const int i = blockIdx.x * STEP_BS + threadIdx.x;
-    const int s = a.blk_sys[(blockIdx.x * STEP_BS) / SYS_PAD];
+    const int i = blockIdx.x * LITE_BS + threadIdx.x;
+    const int s = a.blk_sys[i / SYS_PAD];
     const SysDev &sd = a.sys[s];
     const T4 pi = a.pos[cur][i];
     prefetch_warp_list(a.nbr, i, a.cap, a.nnb[i]);
@@ -834,14 +820,14 @@ template<class R, bool E, int V> __global__ void __launch_bounds__(STEP_BS, (V &
         ke = F.mass[ty] * (v.x * v.x + v.y * v.y + v.z * v.z);
         ep = e;
     }
-    finish<R>(a, ke, ep, 0.f, flags, MODE_NH_FINAL, count_step);
+    warp_partials<R>(a, i, ke, ep, 0.f, flags);
 }
 
-template<class R> __global__ void __launch_bounds__(STEP_BS) k_nh_initial(KArgs<R> a) {
+template<class R> __global__ void __launch_bounds__(256) k_nh_initial(KArgs<R> a) {
     using T4 = typename Vec<R>::T4;
     const int cur = __ldcg(&a.S->cur), lp = __ldcg(&a.S->lp);
-    const int i = blockIdx.x * STEP_BS + threadIdx.x;
-    const int s = a.blk_sys[(blockIdx.x * STEP_BS) / SYS_PAD];
+    const int i = blockIdx.x * 256 + threadIdx.x;
+    const int s = a.blk_sys[i / SYS_PAD];
     const SysDev &sd = a.sys[s];
     T4 p = a.pos[cur][i];
     const int w = wbits(p.w);
@@ -889,16 +875,16 @@ template<class R> __global__ void __launch_bounds__(STEP_BS) k_nh_initial(KArgs<
         md2 = float(ddx * ddx + ddy * ddy + ddz * ddz);
         if (!isfinite(p.x + p.y + p.z)) flags |= ERRB_NAN;
     }
-    finish<R>(a, ke, R(0), md2, flags, MODE_NH_INITIAL, 0, vsx, vsy, vsz);
+    warp_partials<R>(a, i, ke, R(0), md2, flags, vsx, vsy, vsz);
 }
 
 /* Velocity sums of each system after the velocities were replaced (upload,
  * set_state, assign_temperature): sum m v^2 and the mean lipid velocity; the
  * step kernels keep both current afterwards. */
-template<class R> __global__ void __launch_bounds__(STEP_BS) k_vcom(KArgs<R> a) {
+template<class R> __global__ void __launch_bounds__(256) k_vcom(KArgs<R> a) {
     using T4 = typename Vec<R>::T4;
     const int cur = __ldcg(&a.S->cur), lp = __ldcg(&a.S->lp);
-    const int i = blockIdx.x * STEP_BS + threadIdx.x;
+    const int i = blockIdx.x * 256 + threadIdx.x;
     R ke = 0, vsx = 0, vsy = 0, vsz = 0;
     const int ty = w_type(wbits(a.pos[cur][i].w));
     if (ty != GHOST) {
@@ -910,7 +896,7 @@ template<class R> __global__ void __launch_bounds__(STEP_BS) k_vcom(KArgs<R> a) 
             vsz = v.z;
         }
     }
-    finish<R>(a, ke, R(0), 0.f, 0, MODE_VCOM, 0, vsx, vsy, vsz);
+    warp_partials<R>(a, i, ke, R(0), 0.f, 0, vsx, vsy, vsz);
 }
 
 /* assign_temperature (src/assign_temperature.h:26-44, called at
@@ -941,15 +927,14 @@ template<class R> __global__ void __launch_bounds__(256) k_assign_temperature(KA
     a.vel[lp][i] = v;
 }
 
-template<class R, bool E, int V> __global__ void __launch_bounds__(STEP_BS, (V & 2) ? 6 : 8) k_forces(KArgs<R> a) {
+template<class R, bool E, int V> __global__ void __launch_bounds__(LITE_BS, 16) k_forces(KArgs<R> a) {
     using T4 = typename Vec<R>::T4;
     __shared__ T4 sh[27];
-    __shared__ FFDev<R> F;
-    stage_ff<R>(&F, a.ff);
     init_shift<R>(sh);
+    const FFDev<R> &F = *a.ff;
     const int cur = __ldcg(&a.S->cur), lp = __ldcg(&a.S->lp);
-    const int i = blockIdx.x * STEP_BS + threadIdx.x;
-    const int s = a.blk_sys[(blockIdx.x * STEP_BS) / SYS_PAD];
+    const int i = blockIdx.x * LITE_BS + threadIdx.x;
+    const int s = a.blk_sys[i / SYS_PAD];
     const SysDev &sd = a.sys[s];
     const T4 pi = a.pos[cur][i];
     prefetch_warp_list(a.nbr, i, a.cap, a.nnb[i]);
@@ -973,7 +958,7 @@ template<class R, bool E, int V> __global__ void __launch_bounds__(STEP_BS, (V &
         a.epart[i] = double(e);
         ep = e;
     }
-    finish<R>(a, R(0), ep, 0.f, flags, MODE_FORCES, 0);
+    warp_partials<R>(a, i, R(0), ep, 0.f, flags);
 }
 
 /* FP64 membrane area and enclosed volume of each system's face mesh, and
@@ -1067,11 +1052,16 @@ template<class R> __global__ void __launch_bounds__(256) k_mesh(KArgs<R> a) {
  * gathers are issued before the current pair is evaluated -- instead of a
  * 2-way unrolled loop; bit 1: the rare non-lipid pair path inlined, with up
  * to 85 registers, instead of called).  The autotuner picks one per workload. */
+template<class R> void reduce_sums(const KArgs<R> &a, int mode, int count_step, cudaStream_t st) {
+    k_reduce<R><<<a.ngroups, RED_GROUP, 0, st>>>(a, mode, count_step);
+}
 template<class R, int V> void step_langevin_v(const KArgs<R> &a, cudaStream_t st, bool energy) {
     if (energy) {
-        k_step_langevin<R, true, V & 3><<<a.nblk, STEP_BS, 0, st>>>(a);
+        k_step_langevin<R, true, V & 3><<<a.npad / LITE_BS, LITE_BS, 0, st>>>(a);
+        reduce_sums<R>(a, MODE_LANGEVIN, 1, st);
     } else if (a.zero_bulk) {
-        k_step_langevin<R, false, V & 3><<<a.nblk, STEP_BS, 0, st>>>(a);
+        k_step_langevin<R, false, V & 3><<<a.npad / LITE_BS, LITE_BS, 0, st>>>(a);
+        reduce_sums<R>(a, MODE_LANGEVIN, 1, st);
     } else {
         k_step_langevin_lite<R, V><<<a.npad / LITE_BS, LITE_BS, 0, st>>>(a);
         k_advance<<<1, 1, 0, st>>>(a.S, a.rebuild_every, 1);
@@ -1079,9 +1069,10 @@ template<class R, int V> void step_langevin_v(const KArgs<R> &a, cudaStream_t st
 }
 template<class R, int V> void nh_final_v(const KArgs<R> &a, cudaStream_t st, bool energy) {
     if (energy)
-        k_nh_final<R, true, V><<<a.nblk, STEP_BS, 0, st>>>(a, 1);
+        k_nh_final<R, true, V><<<a.npad / LITE_BS, LITE_BS, 0, st>>>(a, 1);
     else
-        k_nh_final<R, false, V><<<a.nblk, STEP_BS, 0, st>>>(a, 1);
+        k_nh_final<R, false, V><<<a.npad / LITE_BS, LITE_BS, 0, st>>>(a, 1);
+    reduce_sums<R>(a, MODE_NH_FINAL, 1, st);
 }
 template<class R> void launch_step_langevin(const KArgs<R> &a, cudaStream_t st, bool energy) {
     switch (a.variant & 7) {
@@ -1104,13 +1095,16 @@ template<class R> void launch_nh_final(const KArgs<R> &a, cudaStream_t st, bool 
     }
 }
 template<class R> void launch_nh_prologue(const KArgs<R> &a, cudaStream_t st) {
-    k_nh_final<R, true, 0><<<a.nblk, STEP_BS, 0, st>>>(a, 0);
+    k_nh_final<R, true, 0><<<a.npad / LITE_BS, LITE_BS, 0, st>>>(a, 0);
+    reduce_sums<R>(a, MODE_NH_FINAL, 0, st);
 }
 template<class R> void launch_nh_initial(const KArgs<R> &a, cudaStream_t st) {
-    k_nh_initial<R><<<a.nblk, STEP_BS, 0, st>>>(a);
+    k_nh_initial<R><<<a.npad / 256, 256, 0, st>>>(a);
+    reduce_sums<R>(a, MODE_NH_INITIAL, 0, st);
 }
 template<class R> void launch_forces(const KArgs<R> &a, cudaStream_t st) {
-    k_forces<R, true, 0><<<a.nblk, STEP_BS, 0, st>>>(a);
+    k_forces<R, true, 0><<<a.npad / LITE_BS, LITE_BS, 0, st>>>(a);
+    reduce_sums<R>(a, MODE_FORCES, 0, st);
 }
 template<class R> void launch_mesh(const KArgs<R> &a, cudaStream_t st) {
     if (a.nmblk > 0) k_mesh<R><<<a.nmblk, 256, 0, st>>>(a);
@@ -1128,7 +1122,8 @@ template<class R> void launch_minimize(const KArgs<R> &a, double dr_opt, double 
     }
 }
 template<class R> void launch_vcom(const KArgs<R> &a, cudaStream_t st) {
-    k_vcom<R><<<a.nblk, STEP_BS, 0, st>>>(a);
+    k_vcom<R><<<a.npad / 256, 256, 0, st>>>(a);
+    reduce_sums<R>(a, MODE_VCOM, 0, st);
 }
 template<class R> void launch_assign_temperature(const KArgs<R> &a, double kT, uint64_t seed, cudaStream_t st) {
     k_assign_temperature<R><<<(a.npad + 255) / 256, 256, 0, st>>>(a, kT, seed);
