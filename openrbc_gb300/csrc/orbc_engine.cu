@@ -1503,12 +1503,21 @@ template<class R> class Engine : public EngineBase {
             }
             return ORBC_OK;
         };
-        // skin x force-kernel form (bits 0-1), then at the best pair the
-        // occupancy form (bit 2) and the other two list-build forms (bits 3-4)
+        // skin x force-kernel form (bits 0-1); the skins half-way to the best
+        // one's grid neighbours; then at the best pair the occupancy form
+        // (bit 2) and the other two list-build forms (bits 3-4)
         const int rest = P.kernel_variant & 28;
         for (double sk : skins)
             for (int var = 0; var < 4; ++var)
                 if ((rc = trial(sk, var | rest))) return rc;
+        const int nsk = int(sizeof(skins) / sizeof(skins[0]));
+        int bi = 0;
+        while (bi + 1 < nsk && skins[bi] != best_skin) ++bi;
+        const double lo_sk = 0.5 * (skins[bi > 0 ? bi - 1 : 0] + best_skin);
+        const double hi_sk = 0.5 * (skins[bi + 1 < nsk ? bi + 1 : nsk - 1] + best_skin);
+        const int bv = best_var;
+        if ((rc = trial(lo_sk, bv))) return rc;
+        if ((rc = trial(hi_sk, bv))) return rc;
         if ((rc = trial(best_skin, best_var ^ 4))) return rc;
         const int lf = (best_var >> 3) & 3;
         for (int f = 0; f < 3; ++f)

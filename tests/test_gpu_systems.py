@@ -326,7 +326,7 @@ def test_autotune_restores_state_and_keeps_stepping():
         step0 = s.thermo()["step"]
         trials = s.autotune(trial_steps=4)
         after = s.download()
-        assert len(trials) == 23 and all(t["ms_per_step"] > 0 for t in trials)  # 5 skins x 4 forms + 3 forms
+        assert len(trials) == 25 and all(t["ms_per_step"] > 0 for t in trials)  # 5 skins x 4 forms, 2 skins, 3 forms
         assert s.thermo()["step"] == step0
         d = min_image_diff(after[0], before[0], box, (1, 1, 0))
         assert np.abs(d).max() < 1e-5
