@@ -356,6 +356,46 @@ int orbc_gpu_morton_order(const double *p3, int64_t n, const double *bsize3, int
 int orbc_gpu_morton_order_noalloc(const double *d_p3, int64_t n, const double *bsize3, int32_t *d_order,
                                   void *stream);
 
+/* Whole-cell initialiser: init_rbc (src/init_rbc.h:29-305) for a
+ * triangulated mesh.  The protein network is built on the host and the
+ * lipids are placed on the GPU.
+ *
+ * orbc_init_rbc_sizes: proteins (2 nvert + 20 nbond: glycophorin and actin
+ * per vertex, band-III and 19 spectrin beads per edge) and bonds
+ * (nvert + 21 nbond) of the network.
+ *
+ * orbc_init_rbc_network (host, src/init_rbc.h:66-233): rescales the mesh so
+ * that its mean edge is 80 nm in reduced units, computes face, vertex and
+ * edge normals, and writes the proteins in the reference's order.
+ *   - Proteins: x3, n3, type, tag (tags 1 .. nprotein), followed by their
+ *     bonds3 (type, tag_i, tag_j).
+ *   - face_nl: lipids per face, int(area * rho) (:262-264); nlipid: their sum.
+ *   - vert3_out, fnorm3_out: the scaled vertices and the face normals.
+ * Any output may be NULL; with x3 NULL only the sizes and mesh data are
+ * written.  The spectrin noise (+-0.05 per coordinate) comes from
+ * Philox4x32-10 keyed by `seed` with counter (edge, bead), where the
+ * reference uses its sequential generator.
+ *
+ * orbc_gpu_place_lipids (GPU, src/init_rbc.h:235-305): face f receives
+ * face_nl[f] lipids, uniform on the triangle. A lipid is redrawn until it is
+ *   - at least min_dist_lp (ForceField::reqlp[1] = 1.685 there) from the
+ *     face's first vertex and from every protein in prot3, and
+ *   - at least min_dist (0.55) from the face's earlier lipids.
+ * Its normal is the face normal.  Output is in face order: x3, n3
+ * (sum face_nl entries).  Attempt k of lipid j of face f draws from
+ * Philox4x32-10 keyed by `seed` with counter (f, j, k), and the first clean
+ * attempt wins, so the result does not depend on the parallel layout.  A
+ * lipid that finds no room after 8,192 attempts returns ORBC_ERR_ARG, where
+ * the reference would retry forever. */
+int orbc_init_rbc_sizes(int64_t nvert, int64_t nbond, int64_t *nprotein, int64_t *nbonds);
+int orbc_init_rbc_network(const double *vert3, int64_t nvert, const int *bond2, int64_t nbond, const int *face3,
+                          int64_t nface, double rho, uint64_t seed, double *vert3_out, double *fnorm3_out,
+                          double *x3, double *n3, int *type, int *tag, int *bonds3, int64_t *face_nl,
+                          int64_t *nlipid);
+int orbc_gpu_place_lipids(const double *vert3, int64_t nvert, const int *face3, const double *fnorm3, int64_t nface,
+                          const int64_t *face_nl, const double *prot3, int64_t nprot, double min_dist,
+                          double min_dist_lp, uint64_t seed, double *x3, double *n3);
+
 int orbc_gpu_destroy(orbc_handle *h);
 const char *orbc_gpu_error(orbc_handle *h);   /* NULL handle -> last create/standalone error */
 const char *orbc_gpu_version(void);

@@ -33,6 +33,7 @@ EXPORTS = [
     "orbc_gpu_assign_temperature", "orbc_gpu_rdf", "orbc_gpu_minimize", "orbc_gpu_save_frame", "orbc_gpu_flush",
     "orbc_gpu_save_checkpoint", "orbc_gpu_load_checkpoint", "orbc_gpu_cleanup", "orbc_gpu_fma_peak",
     "orbc_gen_lattice", "orbc_gen_rbc_counts", "orbc_gen_rbc", "orbc_gen_vesicle_sizes", "orbc_gen_vesicle",
+    "orbc_init_rbc_sizes", "orbc_init_rbc_network", "orbc_gpu_place_lipids",
 ]
 
 
@@ -116,6 +117,10 @@ def lib():
         L.orbc_gpu_step.argtypes = [H, i32, P(Thermo)]
         L.orbc_gpu_download.argtypes = [H, vp, vp, vp, vp]
         L.orbc_gpu_set_state_f32.argtypes = [H, i64, i64, i32, vp, vp, vp, vp]
+        L.orbc_init_rbc_sizes.argtypes = [i64, i64, P(i64), P(i64)]
+        L.orbc_init_rbc_network.argtypes = [vp, i64, vp, i64, vp, i64, d, C.c_uint64, vp, vp, vp, vp, vp, vp, vp, vp,
+                                            P(i64)]
+        L.orbc_gpu_place_lipids.argtypes = [vp, i64, vp, vp, i64, vp, vp, i64, d, d, C.c_uint64, vp, vp]
         L.orbc_gpu_download_f32.argtypes = [H, i64, i64, i32, vp, vp, vp, vp]
         L.orbc_gpu_forces.argtypes = [H, vp, vp, vp]
         L.orbc_gpu_thermo.argtypes = [H, i32, P(Thermo)]

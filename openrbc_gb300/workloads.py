@@ -75,3 +75,62 @@ def vesicles(nves=96, nmin=10_000, nmax=250_000, median=40_000, total=5_000_000,
         systems.append({"lo": (-half, -half, -half), "hi": (half, half, half), "periodic": (1, 1, 1)})
     return {"x": x, "n": nn, "v": v, "o": o, "type": ty, "tag": tg, "offsets": offsets, "systems": systems,
             "sizes": sizes}
+
+
+def init_rbc_network(vert, bond, face, rho=1.05, seed=0):
+    """The protein network init_rbc builds on a triangulated mesh
+    (orbc_init_rbc_network, src/init_rbc.h:66-233; host): rescaled vertices,
+    face normals, proteins, bonds and the lipid count of every face."""
+    vert = np.ascontiguousarray(vert, np.float64).reshape(-1, 3)
+    bond = np.ascontiguousarray(bond, np.int32).reshape(-1, 2)
+    face = np.ascontiguousarray(face, np.int32).reshape(-1, 3)
+    L = N.lib()
+    npr, nb = C.c_int64(), C.c_int64()
+    if L.orbc_init_rbc_sizes(len(vert), len(bond), C.byref(npr), C.byref(nb)):
+        raise ValueError("orbc_init_rbc_sizes failed")
+    x, nn = np.zeros((npr.value, 3)), np.zeros((npr.value, 3))
+    ty, tg = np.zeros(npr.value, np.int32), np.zeros(npr.value, np.int32)
+    b3 = np.zeros((nb.value, 3), np.int32)
+    vs, fn = np.zeros_like(vert), np.zeros((len(face), 3))
+    fnl = np.zeros(len(face), np.int64)
+    nl = C.c_int64()
+    rc = L.orbc_init_rbc_network(vert.ctypes.data, len(vert), bond.ctypes.data, len(bond), face.ctypes.data,
+                                 len(face), float(rho), int(seed) & 0xFFFFFFFFFFFFFFFF, vs.ctypes.data,
+                                 fn.ctypes.data, x.ctypes.data, nn.ctypes.data, ty.ctypes.data, tg.ctypes.data,
+                                 b3.ctypes.data, fnl.ctypes.data, C.byref(nl))
+    if rc:
+        raise ValueError(f"orbc_init_rbc_network failed ({rc})")
+    return {"x": x, "n": nn, "type": ty, "tag": tg, "bonds": b3, "vert": vs, "face": face, "face_normal": fn,
+            "face_nl": fnl, "n_lipid": nl.value}
+
+
+def place_lipids(net, min_dist=0.55, min_dist_lp=1.685, seed=0):
+    """Lipid placement of init_rbc on the GPU (orbc_gpu_place_lipids,
+    src/init_rbc.h:235-305) for a network from init_rbc_network."""
+    L = N.lib()
+    nl = int(net["face_nl"].sum())
+    x, nn = np.zeros((nl, 3)), np.zeros((nl, 3))
+    fnl = np.ascontiguousarray(net["face_nl"], np.int64)
+    prot = np.ascontiguousarray(net["x"], np.float64)
+    rc = L.orbc_gpu_place_lipids(net["vert"].ctypes.data, len(net["vert"]), net["face"].ctypes.data,
+                                 net["face_normal"].ctypes.data, len(net["face"]), fnl.ctypes.data, prot.ctypes.data,
+                                 len(prot), float(min_dist), float(min_dist_lp), int(seed) & 0xFFFFFFFFFFFFFFFF,
+                                 x.ctypes.data, nn.ctypes.data)
+    if rc:
+        raise ValueError(f"orbc_gpu_place_lipids failed ({rc})")
+    return x, nn
+
+
+def init_rbc(vert, bond, face, rho=1.05, seed=0):
+    """init_rbc (src/init_rbc.h:29-305) on a triangulated mesh: proteins from
+    the host network, lipids placed on the GPU; proteins first (tags 1 ..),
+    then lipids, zero velocities, as the reference leaves them."""
+    net = init_rbc_network(vert, bond, face, rho=rho, seed=seed)
+    xl, nl = place_lipids(net, seed=seed)
+    npr = len(net["x"])
+    x = np.concatenate([net["x"], xl])
+    n = np.concatenate([net["n"], nl])
+    ty = np.concatenate([net["type"], np.zeros(len(xl), np.int32)])
+    tg = np.concatenate([net["tag"], np.arange(npr + 1, npr + 1 + len(xl), dtype=np.int32)])
+    return {"x": x, "n": n, "v": np.zeros_like(x), "o": np.zeros_like(x), "type": ty, "tag": tg,
+            "bonds": net["bonds"], "n_protein": npr}

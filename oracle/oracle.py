@@ -304,6 +304,29 @@ def cleanup_marks(x, type, cell3, sys, nc3, L3, mingen=4, tol=2.5):
     return keep.astype(bool), int(r)
 
 
+def place_lipids(net, min_dist=0.55, min_dist_lp=1.685, seed=0):
+    """init_rbc's lipid placement (orc_place_lipids; src/init_rbc.h:235-305)
+    for a network from openrbc_gb300.workloads.init_rbc_network: the checker
+    of the GPU placement, one attempt at a time."""
+    L = lib()
+    L.orc_place_lipids.restype = C.c_int64
+    vp = C.c_void_p
+    vert = np.ascontiguousarray(net["vert"], np.float64)
+    face = np.ascontiguousarray(net["face"], np.int32)
+    fn = np.ascontiguousarray(net["face_normal"], np.float64)
+    fnl = np.ascontiguousarray(net["face_nl"], np.int64)
+    prot = np.ascontiguousarray(net["x"], np.float64)
+    nl = int(fnl.sum())
+    x, n = np.zeros((nl, 3)), np.zeros((nl, 3))
+    r = L.orc_place_lipids(vert.ctypes.data_as(vp), face.ctypes.data_as(vp), fn.ctypes.data_as(vp),
+                           C.c_int64(len(face)), fnl.ctypes.data_as(vp), prot.ctypes.data_as(vp),
+                           C.c_int64(len(prot)), C.c_double(min_dist), C.c_double(min_dist_lp),
+                           C.c_uint64(int(seed) & 0xFFFFFFFFFFFFFFFF), x.ctypes.data_as(vp), n.ctypes.data_as(vp))
+    if r != nl:
+        raise ValueError(f"orc_place_lipids: face {-r - 1} found no room")
+    return x, n
+
+
 def thermo(st: State) -> dict:
     th = OrcThermoC()
     lib().orc_thermo_f64(C.byref(st._c()), C.byref(th))

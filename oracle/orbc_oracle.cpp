@@ -1189,6 +1189,64 @@ void orc_morton_order(const double *p3, int64_t n, const double *bsize, int32_t 
 
 void orc_noise(uint64_t seed, int64_t step, int tag, int sys, double r[3]) { noise3(seed, step, tag, sys, r); }
 
+/* Lipid placement of init_rbc (src/init_rbc.h:235-305), the checker of
+ * orbc_gpu_place_lipids: face f gets face_nl[f] lipids; for lipid j the
+ * attempts k = 0, 1, 2, ... draw (r1, r2) from Philox4x32-10 keyed by the
+ * seed with counter (f, j, k, f >> 32 ^ 'LIPI') and the first candidate
+ * v1 (1 - sqrt r1) + v2 sqrt r1 (1 - r2) + v3 sqrt r1 r2 that is at least
+ * min_dist_lp from v1 and from every protein and at least min_dist from the
+ * face's earlier lipids is kept (a brute-force protein scan here, a grid
+ * there).  Returns the number of lipids placed, or -(face + 1) when a lipid
+ * of that face found no room in 8,192 attempts. */
+int64_t orc_place_lipids(const double *vert3, const int *face3, const double *fnorm3, int64_t nface,
+                         const int64_t *face_nl, const double *prot3, int64_t nprot, double min_dist,
+                         double min_dist_lp, uint64_t seed, double *x3, double *n3) {
+    const uint32_t key[2] = {uint32_t(seed), uint32_t(seed >> 32)};
+    const double md2 = min_dist * min_dist, mdlp2 = min_dist_lp * min_dist_lp;
+    auto sq3 = [](double dx, double dy, double dz) { return dx * dx + dy * dy + dz * dz; };
+    int64_t out = 0;
+    for (int64_t f = 0; f < nface; ++f) {
+        const double *v1 = vert3 + 3 * face3[3 * f], *v2 = vert3 + 3 * face3[3 * f + 1],
+                     *v3 = vert3 + 3 * face3[3 * f + 2];
+        const int64_t b0 = out;
+        for (int64_t j = 0; j < face_nl[f]; ++j) {
+            bool placed = false;
+            for (uint32_t k = 0; k < 8192u && !placed; ++k) {
+                const uint32_t ctr[4] = {uint32_t(f), uint32_t(j), k, uint32_t(uint64_t(f) >> 32) ^ 0x4C495049u};
+                uint32_t o[4];
+                philox(ctr, key, o);
+                const double r1 = double(uint64_t(o[0] >> 5) * 67108864ull + uint64_t(o[1] >> 6)) *
+                                  (1.0 / 9007199254740992.0);
+                const double r2 = double(uint64_t(o[2] >> 5) * 67108864ull + uint64_t(o[3] >> 6)) *
+                                  (1.0 / 9007199254740992.0);
+                const double s1 = std::sqrt(r1);
+                const double w1 = 1.0 - s1, w2 = s1 * (1.0 - r2), w3 = s1 * r2;
+                double r[3];
+                for (int d = 0; d < 3; ++d) r[d] = (v1[d] * w1 + v2[d] * w2) + v3[d] * w3;
+                bool clean = sq3(r[0] - v1[0], r[1] - v1[1], r[2] - v1[2]) >= mdlp2;
+                for (int64_t p = 0; p < nprot && clean; ++p) {
+                    const double *q = prot3 + 3 * p;
+                    if (sq3(r[0] - q[0], r[1] - q[1], r[2] - q[2]) < mdlp2) clean = false;
+                }
+                for (int64_t m = b0; m < b0 + j && clean; ++m) {
+                    const double *q = x3 + 3 * m;
+                    if (sq3(q[0] - r[0], q[1] - r[1], q[2] - r[2]) < md2) clean = false;
+                }
+                if (clean) {
+                    for (int d = 0; d < 3; ++d) {
+                        x3[3 * (b0 + j) + d] = r[d];
+                        n3[3 * (b0 + j) + d] = fnorm3[3 * f + d];
+                    }
+                    placed = true;
+                }
+            }
+            if (!placed) return -(f + 1);
+        }
+        out = b0 + face_nl[f];
+    }
+    return out;
+}
+
 void orc_assign_temperature(orc_system *s, double kT, uint64_t seed) {
     const FF<double> &F = ff<double>();
     for (int64_t i = 0; i < s->n; ++i) {
