@@ -6,15 +6,21 @@
 //   openrbc_gpu [-i lipid|vesicle|trimesh] [-t T] [-k dt] [-e eta] [-T kBT]
 //               [-r rho] [--random-seed s] [-Q q] [-D freq_display]
 //               [--precision mixed|fp64] [--integrator langevin|nose-hoover]
-//               [--skin s] [--n-lipid N] [--mesh-frequency F]
+//               [--skin s] [--n-lipid N] [--mesh-frequency F] [-m mesh] [-E n]
 //
 // -i lipid builds a spherical lipid vesicle of radius 100 at density rho
 // (the reference's init_random_sphere size, src/init_random.h:27-66, placed
 // with a 0.55 exclusion so that no energy minimisation is needed);
-// -i vesicle / trimesh build the synthetic Evans-Fung red-cell membrane with
-// a geodesic spectrin network (include/orbc_workloads.h).
+// -i trimesh -m PREFIX reads PREFIX.{vert,bond,face}.txt as the reference
+// does (src/init_rbc.h:44-66) and builds the cell with its init_rbc
+// (orbc_init_rbc_network on the host, orbc_gpu_place_lipids on the GPU), then
+// minimises for opt-nstep steps and assigns the temperature, as the
+// reference's main() does (src/openrbc.cpp:88-160);
+// -i vesicle / trimesh without a mesh build the synthetic Evans-Fung
+// red-cell membrane with a geodesic spectrin network (include/orbc_workloads.h).
 #include <cmath>
 #include <cstdio>
+#include <fstream>
 #include <cstdlib>
 #include <cstring>
 #include <string>
@@ -27,7 +33,8 @@
 namespace {
 
 struct Args {
-    std::string init = "vesicle", precision = "mixed", integrator = "langevin";
+    std::string init = "vesicle", precision = "mixed", integrator = "langevin", mesh;
+    int opt_nstep = 1000;
     double t_total = 10, dt = 1e-2, eta = 0.01, kBT = 0.22, rho = 1.05, Q = 0, skin = 0.4;
     int freq_display = 100, rseed = 0xBAD5EED, mesh_freq = 57;
     long long n_lipid = 4000000;
@@ -61,7 +68,22 @@ Args parse(int argc, char **argv) {
     if (take(argc, argv, "", "skin", v)) a.skin = std::atof(v.c_str());
     if (take(argc, argv, "", "n-lipid", v)) a.n_lipid = std::atoll(v.c_str());
     if (take(argc, argv, "", "mesh-frequency", v)) a.mesh_freq = std::atoi(v.c_str());
+    if (take(argc, argv, "m", "mesh", v)) a.mesh = v;
+    if (take(argc, argv, "E", "opt-nstep", v)) a.opt_nstep = std::atoi(v.c_str());
     return a;
+}
+
+/* PREFIX.vert.txt (x y z), .bond.txt (i j), .face.txt (i j k), whitespace
+ * separated, as src/init_rbc.h:44-66 reads them. */
+bool read_mesh(const std::string &prefix, std::vector<double> &vert, std::vector<int> &bond, std::vector<int> &face) {
+    std::ifstream fv(prefix + ".vert.txt"), fb(prefix + ".bond.txt"), ff(prefix + ".face.txt");
+    if (!fv || !fb || !ff) return false;
+    double x, y, z;
+    while (fv >> x >> y >> z) vert.insert(vert.end(), {x, y, z});
+    int i, j, k;
+    while (fb >> i >> j) bond.insert(bond.end(), {i, j});
+    while (ff >> i >> j >> k) face.insert(face.end(), {i, j, k});
+    return !vert.empty() && !bond.empty() && !face.empty();
 }
 
 int die(orbc_handle *h, int rc, const char *what) {
@@ -98,7 +120,35 @@ int main(int argc, char **argv) {
         sys.hi[d] = 1000;
     }
     std::printf("Initializing system ...\n");
-    if (a.init == "lipid") {
+    bool minimise = false;
+    if (a.init == "trimesh" && !a.mesh.empty()) {
+        std::vector<double> vert;
+        std::vector<int> bond, face;
+        if (!read_mesh(a.mesh, vert, bond, face)) {
+            std::printf("<OpenRBC-GPU> cannot read mesh files %s.{vert|bond|face}.txt\n", a.mesh.c_str());
+            return 1;
+        }
+        const int64_t nv = int64_t(vert.size() / 3), ne = int64_t(bond.size() / 2), nfc = int64_t(face.size() / 3);
+        int64_t np = 0, nl = 0;
+        if (orbc_init_rbc_sizes(nv, ne, &np, &nb)) return die(nullptr, ORBC_ERR_ARG, "orbc_init_rbc_sizes");
+        std::vector<double> vs(3 * nv), fn(3 * nfc);
+        std::vector<int64_t> fnl(nfc);
+        if (orbc_init_rbc_network(vert.data(), nv, bond.data(), ne, face.data(), nfc, a.rho, uint64_t(a.rseed),
+                                  vs.data(), fn.data(), nullptr, nullptr, nullptr, nullptr, nullptr, fnl.data(), &nl))
+            return die(nullptr, ORBC_ERR_ARG, "orbc_init_rbc_network");
+        N = np + nl;
+        x.assign(3 * N, 0.0), n.assign(3 * N, 0.0), v.assign(3 * N, 0.0), o.assign(3 * N, 0.0);
+        type.assign(N, 0), tag.resize(N), bonds.resize(3 * nb);
+        if (orbc_init_rbc_network(vert.data(), nv, bond.data(), ne, face.data(), nfc, a.rho, uint64_t(a.rseed),
+                                  nullptr, nullptr, x.data(), n.data(), type.data(), tag.data(), bonds.data(),
+                                  nullptr, nullptr))
+            return die(nullptr, ORBC_ERR_ARG, "orbc_init_rbc_network");
+        const int rcl = orbc_gpu_place_lipids(vs.data(), nv, face.data(), fn.data(), nfc, fnl.data(), x.data(), np,
+                                              0.55, 1.685, uint64_t(a.rseed), x.data() + 3 * np, n.data() + 3 * np);
+        if (rcl) return die(nullptr, rcl, "orbc_gpu_place_lipids");
+        for (int64_t k = np; k < N; ++k) tag[k] = int(k + 1);
+        minimise = true;
+    } else if (a.init == "lipid") {
         N = int64_t(a.rho * 4 * M_PI * 100.0 * 100.0);
         x.resize(3 * N), n.resize(3 * N), v.resize(3 * N), o.resize(3 * N), type.resize(N), tag.resize(N);
         double R;
@@ -126,9 +176,15 @@ int main(int argc, char **argv) {
     if (rc) return die(nullptr, rc, "orbc_gpu_create");
     const int64_t off[2] = {0, N};
     rc = orbc_gpu_upload_batch(h, 1, &sys, off, x.data(), n.data(), v.data(), o.data(), type.data(), tag.data(),
-                               size_t(N), nb ? bonds.data() : nullptr, nb ? r0.data() : nullptr, size_t(nb),
+                               size_t(N), nb ? bonds.data() : nullptr, r0.empty() ? nullptr : r0.data(), size_t(nb),
                                nf ? faces.data() : nullptr, size_t(nf));
     if (rc) return die(h, rc, "orbc_gpu_upload_batch");
+    if (minimise) {  // src/openrbc.cpp:88-146 and :160
+        rc = orbc_gpu_minimize(h, a.opt_nstep, 5e-2, 5e-2, nullptr);
+        if (rc) return die(h, rc, "orbc_gpu_minimize");
+        rc = orbc_gpu_assign_temperature(h, a.kBT, uint64_t(a.rseed));
+        if (rc) return die(h, rc, "orbc_gpu_assign_temperature");
+    }
     std::printf("Done: %lld particles, %lld bonds, %lld faces.\nRun ...\n", (long long)N, (long long)nb,
                 (long long)nf);
 
