@@ -21,14 +21,13 @@ namespace orbc {
 constexpr int NT = 6;            // particle types (src/forcefield_canonical.h:31-37)
 constexpr int GHOST = 15;        // type of padding slots
 constexpr int SYS_PAD = 256;     // slot padding per system
-constexpr int STEP_BS = 128;     // threads per block of the force / integrator kernels (divides SYS_PAD)
-constexpr int LITE_BS = 64;      // threads per block of the Langevin step without per-system sums
+constexpr int LITE_BS = 64;      // threads per block of the force / integrator kernels
 constexpr int MAX_BT = 8;        // bond types
 constexpr int MAX_DEG = 15;      // bonds / faces per particle (4-bit fields)
 constexpr uint32_t NB_MASK = (1u << 27) - 1u;
 constexpr int NB_SHIFT = 27;
 constexpr int MAX_SLOTS = 1 << 27;
-constexpr int NPART = 8;         // per-block partial sums: ke2, epot, maxd2, flags, lipid sum v (3), pad
+constexpr int NPART = 8;         // per-warp partial sums: ke2, epot, maxd2, flags, lipid sum v (3), pad
 constexpr int RED_GROUP = 256;   // warp partials (of 32 slots) per reduction group
 constexpr int MESH_CHUNK = 1024; // faces per block of the area / volume kernel
 
@@ -187,7 +186,7 @@ template<class R> struct KArgs {
     Scalars *S;
     SysDev *sys;
     SysState *ss;
-    int nsys, npad, nblk;    // nblk: STEP_BS-slot blocks of the force / integrator kernels
+    int nsys, npad;
     // radix sort scratch
     uint32_t *skey[2];
     int *sval[2];

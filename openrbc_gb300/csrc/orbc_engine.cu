@@ -488,7 +488,6 @@ template<class R> class Engine : public EngineBase {
         if (off >= MAX_SLOTS) return fail(ORBC_ERR_ARG, "upload: more than 2^27 particle slots");
         if (cbase >= (uint64_t(1) << 32) - 1) return fail(ORBC_ERR_ARG, "upload: more than 2^32 cells");
         npad = int(off);
-        nblk = npad / STEP_BS;
         const int nb256 = npad / SYS_PAD;
         total_cells = cbase;
 
@@ -1668,7 +1667,6 @@ template<class R> class Engine : public EngineBase {
         a.ss = ssd.p;
         a.nsys = nsys;
         a.npad = npad;
-        a.nblk = nblk;
         a.counts = counts.p;
         a.digit_total = dtot.p;
         a.inv = invd.p;
@@ -1752,7 +1750,7 @@ template<class R> class Engine : public EngineBase {
     bool graph_cond = false;
     int graph_steps = 0;
     bool uploaded = false, nh_primed = false, has_mesh = false, vcom_valid = false;
-    int nsys = 0, npad = 0, nblk = 0, cap = 0, passes = 4, ntiles = 1, maxb = 0, maxf = 0, nfaces = 0, nmblk = 0;
+    int nsys = 0, npad = 0, cap = 0, passes = 4, ntiles = 1, maxb = 0, maxf = 0, nfaces = 0, nmblk = 0;
     int64_t nhome = 0;
     uint64_t total_cells = 0;
     std::vector<SysDev> hsys;
