@@ -279,7 +279,10 @@ def main():
     fp64 = None
     ferr = None
     if not args.skip_fp64 and args.fp64_steps > 0:
-        sim64 = make_sim(w, "fp64")
+        # the mixed run's kernel forms (force loop and list build) and skin
+        form = tune["chosen"]["variant"] if tune else args.form
+        skin = tune["chosen"]["skin"] if tune else (args.skin if args.skin is not None else SKIN)
+        sim64 = make_sim(w, "fp64", skin=skin, kernel_variant=form)
         f64, _, _ = sim64.forces()
         sim64.step(2)
         sim64.step(args.fp64_steps)
@@ -287,7 +290,8 @@ def main():
         value64 = n * args.fp64_steps / (ms64 * 1e-3)
         sim64.close()
         ferr = float(np.linalg.norm(f_mixed - f64) / np.linalg.norm(f64))
-        fp64 = {"value": value64, "ms_per_step": ms64 / args.fp64_steps, "steps": args.fp64_steps}
+        fp64 = {"value": value64, "ms_per_step": ms64 / args.fp64_steps, "steps": args.fp64_steps,
+                "skin": skin, "kernel_form": form}
         log(f"fp64: {ms64 / args.fp64_steps:.4f} ms/step; mixed force rel err vs fp64 {ferr:.3e}")
 
     # ---- end to end through the C ABI with pinned host buffers

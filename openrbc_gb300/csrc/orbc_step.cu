@@ -240,6 +240,12 @@ template<class R> __device__ __forceinline__ void init_shift(typename Vec<R>::T4
     __syncthreads();
 }
 
+/* Resident blocks of LITE_BS threads asked of the force kernels: the FP32
+ * count, halved for FP64, whose doubles need twice the registers (the FP64
+ * forms are bound by the FP64 pipe, so fewer resident warps cost nothing,
+ * while spills would). */
+template<class R> constexpr int fp_blocks(int n) { return sizeof(R) == 4 ? n : n / 2; }
+
 /* All forces and torques on particle slot i: pair terms over its neighbour
  * list (variant V, see launch_step_langevin), bonds, mesh constraint. */
 template<class R, bool E, int V>
@@ -637,7 +643,8 @@ __device__ __forceinline__ void langevin_particle(const KArgs<R> &a, const FFDev
  * the structure of the lite kernel below (small blocks, force-field table
  * through the read-only path) plus warp partials, summed per system by
  * k_reduce after the kernel. */
-template<class R, bool E, int V> __global__ void __launch_bounds__(LITE_BS, 16) k_step_langevin(KArgs<R> a) {
+template<class R, bool E, int V>
+__global__ void __launch_bounds__(LITE_BS, fp_blocks<R>(16)) k_step_langevin(KArgs<R> a) {
     using T4 = typename Vec<R>::T4;
     __shared__ T4 sh[27];
     init_shift<R>(sh);
@@ -665,7 +672,7 @@ template<class R, bool E, int V> __global__ void __launch_bounds__(LITE_BS, 16) 
  * k_advance flips the buffers after the kernel.  The temperature is reduced on
  * demand (k_vcom). */
 template<class R, int V>
-__global__ void __launch_bounds__(LITE_BS, (V & 4) ? 20 : 16) k_step_langevin_lite(KArgs<R> a) {
+__global__ void __launch_bounds__(LITE_BS, fp_blocks<R>((V & 4) ? 20 : 16)) k_step_langevin_lite(KArgs<R> a) {
     using T4 = typename Vec<R>::T4;
     __shared__ T4 sh[27];
     init_shift<R>(sh);
@@ -708,7 +715,8 @@ __global__ void k_advance(Scalars *S, int rebuild_every, int count_step) {
  * orientations ping-pong like the Langevin step; the step counter (the noise
  * key) does not advance. */
 template<class R, int V>
-__global__ void __launch_bounds__(LITE_BS, (V & 2) ? 12 : 16) k_minimize(KArgs<R> a, double dr_opt, double dn_opt) {
+__global__ void __launch_bounds__(LITE_BS, fp_blocks<R>((V & 2) ? 12 : 16))
+    k_minimize(KArgs<R> a, double dr_opt, double dn_opt) {
     using T4 = typename Vec<R>::T4;
     __shared__ T4 sh[27];
     init_shift<R>(sh);
@@ -769,7 +777,8 @@ __global__ void __launch_bounds__(LITE_BS, (V & 2) ? 12 : 16) k_minimize(KArgs<R
 /* Nose-Hoover second half (post_toque_final_update, src/integrate_nh.h:237-273)
  * fused with the forces: the lite structure plus warp partials for the
  * kinetic-energy sum that k_reduce turns into the thermostat update. */
-template<class R, bool E, int V> __global__ void __launch_bounds__(LITE_BS, 16) k_nh_final(KArgs<R> a, int count_step) {
+template<class R, bool E, int V>
+__global__ void __launch_bounds__(LITE_BS, fp_blocks<R>(16)) k_nh_final(KArgs<R> a, int count_step) {
     using T4 = typename Vec<R>::T4;
     __shared__ T4 sh[27];
     init_shift<R>(sh);
@@ -927,7 +936,7 @@ template<class R> __global__ void __launch_bounds__(256) k_assign_temperature(KA
     a.vel[lp][i] = v;
 }
 
-template<class R, bool E, int V> __global__ void __launch_bounds__(LITE_BS, 16) k_forces(KArgs<R> a) {
+template<class R, bool E, int V> __global__ void __launch_bounds__(LITE_BS, fp_blocks<R>(16)) k_forces(KArgs<R> a) {
     using T4 = typename Vec<R>::T4;
     __shared__ T4 sh[27];
     init_shift<R>(sh);
