@@ -672,7 +672,7 @@ __global__ void __launch_bounds__(LITE_BS, fp_blocks<R>(16)) k_step_langevin(KAr
  * k_advance flips the buffers after the kernel.  The temperature is reduced on
  * demand (k_vcom). */
 template<class R, int V>
-__global__ void __launch_bounds__(LITE_BS, fp_blocks<R>((V & 4) ? 20 : 16)) k_step_langevin_lite(KArgs<R> a) {
+__global__ void __launch_bounds__(LITE_BS, fp_blocks<R>((V & 4) ? 18 : 16)) k_step_langevin_lite(KArgs<R> a) {
     using T4 = typename Vec<R>::T4;
     __shared__ T4 sh[27];
     init_shift<R>(sh);
