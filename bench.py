@@ -279,8 +279,9 @@ def main():
     fp64 = None
     ferr = None
     if not args.skip_fp64 and args.fp64_steps > 0:
-        # the mixed run's kernel forms (force loop and list build) and skin
-        form = tune["chosen"]["variant"] if tune else args.form
+        # the mixed run's force-loop and list-build forms and skin; the
+        # occupancy form (bit 2) is sized for FP32 registers and left out
+        form = (tune["chosen"]["variant"] if tune else args.form) & ~4
         skin = tune["chosen"]["skin"] if tune else (args.skin if args.skin is not None else SKIN)
         sim64 = make_sim(w, "fp64", skin=skin, kernel_variant=form)
         f64, _, _ = sim64.forces()
