@@ -201,7 +201,9 @@ template<class R> struct KArgs {
     int carry_forces;        // forces / torques persist between kernels (Nose-Hoover)
     int zero_bulk;           // remove the mean lipid velocity before integrating
     int nlist_lane;          // list-build form: 0 per cell of a warp, 1 per-lane 27-cell sweep, 2 two-phase
-    const FFDev<R> *ff;      // force-field tables (global; staged into shared memory per block)
+    const FFDev<R> *ff;      // force-field tables (global)
+    PairP<R> ll;             // the lipid-lipid pair, in kernel-parameter space: read as constant operands,
+                             // so the bulk pair path keeps no registers for its parameters
 };
 
 // host-side launchers (explicitly instantiated for float and double)

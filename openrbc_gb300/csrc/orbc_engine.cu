@@ -1682,6 +1682,7 @@ template<class R> class Engine : public EngineBase {
         a.carry_forces = P.integrator == ORBC_INT_NOSE_HOOVER ? 1 : 0;
         a.zero_bulk = P.zero_bulk ? 1 : 0;
         a.ff = ffd.p;
+        a.ll = hff.pair[0];
     }
 
     int build_lists(bool first) {

@@ -264,9 +264,7 @@ __device__ __forceinline__ void particle_forces(const KArgs<R> &a, const FFDev<R
     const int nin = packed & 0xffff, nout = packed >> 16;
     const uint32_t *__restrict__ shell = nb + int64_t(a.cap - 1) * 32;  // shell rows run downwards
     const int64_t stride = 32;
-    const PairP<R> &LL = F.pair[0];
-    const R ll_cutsq = LL.cutsq, ll_cut = LL.cut, ll_alpha = LL.alpha, ll_aatt = LL.aatt;
-    const R ll_rep8 = LL.rep8, ll_att4 = LL.att4, ll_rep = LL.rep, ll_att = LL.att;
+    const R ll_cutsq = a.ll.cutsq;
     auto pair = [&](uint32_t ent, const T4 &pj, const T4 &nj) {
         const T4 s = sh[ent >> NB_SHIFT];
         const R dx = (pi.x - pj.x) + s.x * Lx;
@@ -275,17 +273,8 @@ __device__ __forceinline__ void particle_forces(const KArgs<R> &a, const FFDev<R
         const R r2 = dx * dx + dy * dy + dz * dz;
         const int tj = w_type(wbits(pj.w));
         if ((ty | tj) == 0) {
-            if (r2 < ll_cutsq && r2 > R(1e-5)) {
-                PairP<R> P;
-                P.cut = ll_cut;
-                P.alpha = ll_alpha;
-                P.aatt = ll_aatt;
-                P.rep8 = ll_rep8;
-                P.att4 = ll_att4;
-                P.rep = ll_rep;
-                P.att = ll_att;
-                aniso<R, E>(P, dx, dy, dz, r2, ni.x, ni.y, ni.z, nj.x, nj.y, nj.z, f, t, e);
-            }
+            if (r2 < ll_cutsq && r2 > R(1e-5))
+                aniso<R, E>(a.ll, dx, dy, dz, r2, ni.x, ni.y, ni.z, nj.x, nj.y, nj.z, f, t, e);
         } else {
             pair_general<R, E, (V & 2) != 0>(F.pair[ty * NT + tj], dx, dy, dz, r2, ni.x, ni.y, ni.z, nj.x, nj.y,
                                              nj.z, f, t, e);
