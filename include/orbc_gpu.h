@@ -86,8 +86,8 @@ typedef struct {
     double bond_R[ORBC_MAX_BOND_TYPES];
     /* kernel forms 0..23: bit 0 = software-pipelined neighbour pass
        (else 2-way unrolled), bit 1 = non-lipid pair path inlined (else
-       called), bit 2 = Langevin step kernel compiled for 18 resident blocks
-       per SM (56 registers; else 16 blocks, 64 registers), bits 3-4 = how
+       called), bit 2 = Langevin step kernel compiled for 20 resident blocks
+       per SM (48 registers; else 16 blocks, 64 registers), bits 3-4 = how
        the neighbour list is built: 0 per cell of a warp, 32 candidates at a
        time, entries placed by prefix count; 1 per-particle 27-cell sweeps;
        2 per warp in two phases (accept masks per particle, then every lane

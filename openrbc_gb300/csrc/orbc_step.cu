@@ -227,13 +227,18 @@ __device__ __forceinline__ void prefetch_warp_list(const uint32_t *nbr, int i, i
     }
 }
 
-template<class R> __device__ __forceinline__ void init_shift(typename Vec<R>::T4 *sh) {
+/* The 27 cell shifts of the list entries, already multiplied by the block's
+ * cell size: x_i - x_j = (o_i - o_j) + sh[code] (a shift of -1, 0 or +1 cells
+ * times Lc is exact, so this rounds as the unscaled product would).  A block
+ * never straddles two systems. */
+template<class R> __device__ __forceinline__ void init_shift(const KArgs<R> &a, typename Vec<R>::T4 *sh) {
     if (threadIdx.x < 27) {
+        const SysDev &sd = a.sys[a.blk_sys[(blockIdx.x * blockDim.x) / SYS_PAD]];
         const int c = threadIdx.x;
         typename Vec<R>::T4 v;
-        v.x = R(-(c % 3 - 1));
-        v.y = R(-((c / 3) % 3 - 1));
-        v.z = R(-(c / 9 - 1));
+        v.x = R(-(c % 3 - 1)) * lc_of<R>(sd, 0);
+        v.y = R(-((c / 3) % 3 - 1)) * lc_of<R>(sd, 1);
+        v.z = R(-(c / 9 - 1)) * lc_of<R>(sd, 2);
         v.w = R(0);
         sh[c] = v;
     }
@@ -256,7 +261,6 @@ __device__ __forceinline__ void particle_forces(const KArgs<R> &a, const FFDev<R
                                                 int &flags) {
     using T4 = typename Vec<R>::T4;
     const int ty = w_type(w);
-    const R Lx = lc_of<R>(sd, 0), Ly = lc_of<R>(sd, 1), Lz = lc_of<R>(sd, 2);
     const T4 *__restrict__ pos = a.pos[cur];
     const T4 *__restrict__ nrm = a.nrm[cur];
     const uint32_t *__restrict__ nb = a.nbr + nbr_index(i, 0, a.cap);
@@ -267,9 +271,9 @@ __device__ __forceinline__ void particle_forces(const KArgs<R> &a, const FFDev<R
     const R ll_cutsq = a.ll.cutsq;
     auto pair = [&](uint32_t ent, const T4 &pj, const T4 &nj) {
         const T4 s = sh[ent >> NB_SHIFT];
-        const R dx = (pi.x - pj.x) + s.x * Lx;
-        const R dy = (pi.y - pj.y) + s.y * Ly;
-        const R dz = (pi.z - pj.z) + s.z * Lz;
+        const R dx = (pi.x - pj.x) + s.x;
+        const R dy = (pi.y - pj.y) + s.y;
+        const R dz = (pi.z - pj.z) + s.z;
         const R r2 = dx * dx + dy * dy + dz * dz;
         const int tj = w_type(wbits(pj.w));
         if ((ty | tj) == 0) {
@@ -319,9 +323,9 @@ __device__ __forceinline__ void particle_forces(const KArgs<R> &a, const FFDev<R
         const int j = int(ent & NB_MASK);
         const T4 pj = ldg4<R>(pos + j);
         const T4 s = sh[ent >> NB_SHIFT];
-        const R dx = (pi.x - pj.x) + s.x * Lx;
-        const R dy = (pi.y - pj.y) + s.y * Ly;
-        const R dz = (pi.z - pj.z) + s.z * Lz;
+        const R dx = (pi.x - pj.x) + s.x;
+        const R dy = (pi.y - pj.y) + s.y;
+        const R dz = (pi.z - pj.z) + s.z;
         const R r2 = dx * dx + dy * dy + dz * dz;
         const int tj = w_type(wbits(pj.w));
         const R lim = ((ty | tj) == 0) ? ll_cutsq : F.pair[ty * NT + tj].anysq;
@@ -636,7 +640,7 @@ template<class R, bool E, int V>
 __global__ void __launch_bounds__(LITE_BS, fp_blocks<R>(16)) k_step_langevin(KArgs<R> a) {
     using T4 = typename Vec<R>::T4;
     __shared__ T4 sh[27];
-    init_shift<R>(sh);
+    init_shift<R>(a, sh);
     const FFDev<R> *__restrict__ Fp = a.ff;
     const int cur = __ldcg(&a.S->cur), lp = __ldcg(&a.S->lp);
     const long long step = __ldcg(&a.S->step);
@@ -661,10 +665,10 @@ __global__ void __launch_bounds__(LITE_BS, fp_blocks<R>(16)) k_step_langevin(KAr
  * k_advance flips the buffers after the kernel.  The temperature is reduced on
  * demand (k_vcom). */
 template<class R, int V>
-__global__ void __launch_bounds__(LITE_BS, fp_blocks<R>((V & 4) ? 18 : 16)) k_step_langevin_lite(KArgs<R> a) {
+__global__ void __launch_bounds__(LITE_BS, fp_blocks<R>((V & 4) ? 20 : 16)) k_step_langevin_lite(KArgs<R> a) {
     using T4 = typename Vec<R>::T4;
     __shared__ T4 sh[27];
-    init_shift<R>(sh);
+    init_shift<R>(a, sh);
     const FFDev<R> *__restrict__ Fp = a.ff;
     const int cur = __ldcg(&a.S->cur), lp = __ldcg(&a.S->lp);
     const long long step = __ldcg(&a.S->step);
@@ -708,7 +712,7 @@ __global__ void __launch_bounds__(LITE_BS, fp_blocks<R>((V & 2) ? 12 : 16))
     k_minimize(KArgs<R> a, double dr_opt, double dn_opt) {
     using T4 = typename Vec<R>::T4;
     __shared__ T4 sh[27];
-    init_shift<R>(sh);
+    init_shift<R>(a, sh);
     const FFDev<R> *__restrict__ Fp = a.ff;
     const int cur = __ldcg(&a.S->cur), lp = __ldcg(&a.S->lp);
     const int i = blockIdx.x * LITE_BS + threadIdx.x;
@@ -770,7 +774,7 @@ template<class R, bool E, int V>
 __global__ void __launch_bounds__(LITE_BS, fp_blocks<R>(16)) k_nh_final(KArgs<R> a, int count_step) {
     using T4 = typename Vec<R>::T4;
     __shared__ T4 sh[27];
-    init_shift<R>(sh);
+    init_shift<R>(a, sh);
     const FFDev<R> &F = *a.ff;
     const int cur = __ldcg(&a.S->cur), lp = __ldcg(&a.S->lp);
     const int i = blockIdx.x * LITE_BS + threadIdx.x;
@@ -928,7 +932,7 @@ template<class R> __global__ void __launch_bounds__(256) k_assign_temperature(KA
 template<class R, bool E, int V> __global__ void __launch_bounds__(LITE_BS, fp_blocks<R>(16)) k_forces(KArgs<R> a) {
     using T4 = typename Vec<R>::T4;
     __shared__ T4 sh[27];
-    init_shift<R>(sh);
+    init_shift<R>(a, sh);
     const FFDev<R> &F = *a.ff;
     const int cur = __ldcg(&a.S->cur), lp = __ldcg(&a.S->lp);
     const int i = blockIdx.x * LITE_BS + threadIdx.x;
