@@ -637,7 +637,7 @@ __device__ __forceinline__ void langevin_particle(const KArgs<R> &a, const FFDev
  * through the read-only path) plus warp partials, summed per system by
  * k_reduce after the kernel. */
 template<class R, bool E, int V>
-__global__ void __launch_bounds__(LITE_BS, fp_blocks<R>(16)) k_step_langevin(KArgs<R> a) {
+__global__ void __launch_bounds__(LITE_BS, fp_blocks<R>(20)) k_step_langevin(KArgs<R> a) {
     using T4 = typename Vec<R>::T4;
     __shared__ T4 sh[27];
     init_shift<R>(a, sh);
@@ -771,7 +771,7 @@ __global__ void __launch_bounds__(LITE_BS, fp_blocks<R>((V & 2) ? 12 : 16))
  * fused with the forces: the lite structure plus warp partials for the
  * kinetic-energy sum that k_reduce turns into the thermostat update. */
 template<class R, bool E, int V>
-__global__ void __launch_bounds__(LITE_BS, fp_blocks<R>(16)) k_nh_final(KArgs<R> a, int count_step) {
+__global__ void __launch_bounds__(LITE_BS, fp_blocks<R>(20)) k_nh_final(KArgs<R> a, int count_step) {
     using T4 = typename Vec<R>::T4;
     __shared__ T4 sh[27];
     init_shift<R>(a, sh);
