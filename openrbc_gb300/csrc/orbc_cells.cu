@@ -544,13 +544,15 @@ template<class R> __global__ void __launch_bounds__(128) k_nlist(KArgs<R> a, int
  * every lane of the pass expands its masks in candidate order into its own
  * column.  The candidates, their order and the arithmetic are those of
  * forms 0 and 1, so all three forms write the same rows. */
-template<class R> __global__ void __launch_bounds__(128) k_nlist2(KArgs<R> a, int gated) {
+// 7 resident blocks per SM: the regions below (about 28 KB per block in FP32)
+// and at most 72 registers; more warps in flight beat fewer passes per warp
+template<class R> __global__ void __launch_bounds__(128, 7) k_nlist2(KArgs<R> a, int gated) {
     using T4 = typename Vec<R>::T4;
     if (gated && !__ldcg(&a.S->rebuild)) return;
     constexpr int NLW = 4;                                // warps per block
     constexpr int MB = 8;                                 // masks (32 candidates each) per region
     constexpr int REG = 32 * MB;                          // candidates per cell region
-    constexpr int TOT = sizeof(T4) == 16 ? 512 : 288;     // staged candidates per warp and pass
+    constexpr int TOT = sizeof(T4) == 16 ? 320 : 288;     // staged candidates per warp and pass
     __shared__ float2 s_cut[256];                         // (list cutoff^2, range cutoff^2) per type pair
     __shared__ T4 s_pos[NLW][TOT];
     __shared__ uint32_t s_ent[NLW][TOT];                  // j | shift code of its cell << NB_SHIFT
