@@ -534,28 +534,28 @@ template<class R> __global__ void __launch_bounds__(128) k_nlist(KArgs<R> a, int
 }
 
 /* Form 2 of the list build (two phases per warp).  The distinct cells of a
- * warp's particles are staged as in form 0 -- 27 lanes fetch a cell's
- * neighbour ranges, the warp stages its candidates pre-shifted into that
- * cell's frame -- but as many cells per pass as fit, each in its own region
- * of shared memory (regions start on different 16-byte bank slots).
- * Phase 1: for each particle of a cell the warp tests 32 candidates per
- * ballot, branch-free, and the particle's own lane keeps the accept masks
- * (in range at all / inside the interaction range) in registers.  Phase 2:
- * every lane of the pass expands its masks in candidate order into its own
- * column.  The candidates, their order and the arithmetic are those of
+ * warp's particles are fetched as in form 0 -- 27 lanes fetch a cell's
+ * neighbour ranges -- and each cell's candidates are staged pre-shifted into
+ * that cell's frame.  Phase 1: for each particle of the cell the warp tests
+ * 32 candidates per ballot, branch-free, and the particle's own lane keeps
+ * the accept masks (in range at all / inside the interaction range) in
+ * registers.  The candidates' list entries stay staged in shared memory for
+ * as many cells as fit, so that phase 2 -- every lane expands its masks in
+ * candidate order into its own column -- runs for most warps once, with all
+ * their lanes.  The candidates, their order and the arithmetic are those of
  * forms 0 and 1, so all three forms write the same rows. */
-// 7 resident blocks per SM: the regions below (about 28 KB per block in FP32)
+// 7 resident blocks per SM: the staging below (about 31 KB per block in FP32)
 // and at most 72 registers; more warps in flight beat fewer passes per warp
 template<class R> __global__ void __launch_bounds__(128, 7) k_nlist2(KArgs<R> a, int gated) {
     using T4 = typename Vec<R>::T4;
     if (gated && !__ldcg(&a.S->rebuild)) return;
     constexpr int NLW = 4;                                // warps per block
     constexpr int MB = 8;                                 // masks (32 candidates each) per region
-    constexpr int REG = 32 * MB;                          // candidates per cell region
-    constexpr int TOT = sizeof(T4) == 16 ? 320 : 288;     // staged candidates per warp and pass
+    constexpr int REG = 32 * MB;                          // candidates of one cell (or chunk) per phase 1
+    constexpr int SE = sizeof(T4) == 16 ? 768 : 512;      // list entries staged per warp until phase 2
     __shared__ float2 s_cut[256];                         // (list cutoff^2, range cutoff^2) per type pair
-    __shared__ T4 s_pos[NLW][TOT];
-    __shared__ uint32_t s_ent[NLW][TOT];                  // j | shift code of its cell << NB_SHIFT
+    __shared__ T4 s_pos[NLW][REG];                        // the current cell's candidates
+    __shared__ uint32_t s_ent[NLW][SE];                   // j | shift code of its cell << NB_SHIFT
     __shared__ int s_off[NLW][28], s_beg[NLW][27];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (int k = threadIdx.x; k < 256; k += blockDim.x)
@@ -621,8 +621,8 @@ template<class R> __global__ void __launch_bounds__(128, 7) k_nlist2(KArgs<R> a,
         __syncwarp();
         return __shfl_sync(0xffffffffu, inc, 31);
     };
-    // candidates [c0, c0 + nch) of the fetched cell -> sp/se[base ...]
-    auto stage = [&](int c0, int nch, int base) {
+    // candidates [c0, c0 + nch) of the fetched cell -> sp[0 ...] and se[ebase ...]
+    auto stage = [&](int c0, int nch, int ebase) {
 #pragma unroll 4
         for (int t = lane; t < nch; t += 32) {
             const int idx = c0 + t;
@@ -631,15 +631,15 @@ template<class R> __global__ void __launch_bounds__(128, 7) k_nlist2(KArgs<R> a,
             for (int step = 16; step > 0; step >>= 1)
                 if (l + step < 27 && off[l + step] <= idx) l += step;
             const int j = beg[l] + (idx - off[l]);
-            sp[base + t] = shifted(a.pos[cur][j], l % 3 - 1, (l / 3) % 3 - 1, l / 9 - 1);
-            se[base + t] = uint32_t(j) | (uint32_t(l) << NB_SHIFT);
+            sp[t] = shifted(a.pos[cur][j], l % 3 - 1, (l / 3) % 3 - 1, l / 9 - 1);
+            se[ebase + t] = uint32_t(j) | (uint32_t(l) << NB_SHIFT);
         }
         __syncwarp();
     };
     uint32_t macc[MB], minn[MB];
-    // phase 1 for the particles grp over the region [base, base + nch), nch <= REG;
+    // phase 1 for the particles grp over the staged candidates [0, nch), nch <= REG;
     // ts: the owning lane's own staged index (self is not a neighbour), -1 if absent
-    auto phase1 = [&](unsigned grp, int base, int nch, int ts) {
+    auto phase1 = [&](unsigned grp, int nch, int ts) {
         for (unsigned g = grp; g; g &= g - 1u) {
             const int il = __ffs(g) - 1;
             T4 pi = p;
@@ -653,7 +653,7 @@ template<class R> __global__ void __launch_bounds__(128, 7) k_nlist2(KArgs<R> a,
                 if (b * 32 < nch) {
                     const int t = b * 32 + lane;
                     const bool valid = t < nch;
-                    const T4 q = sp[base + (valid ? t : 0)];
+                    const T4 q = sp[valid ? t : 0];
                     const float2 cut = s_cut[ti + w_type(wbits(q.w))];
                     const R r2 = dist2(pi, q);
                     const bool acc = valid && t != tsi && cut.x > 0.f && r2 < R(cut.x);
@@ -667,8 +667,9 @@ template<class R> __global__ void __launch_bounds__(128, 7) k_nlist2(KArgs<R> a,
             }
         }
     };
-    // phase 2: this lane's accepted candidates of the region at mybase, in order
-    auto phase2 = [&](int mybase) {
+    int mybase = 0;  // where this lane's candidates start in se
+    // phase 2: this lane's accepted candidates, in order; the masks are cleared
+    auto phase2 = [&]() {
 #pragma unroll
         for (int b = 0; b < MB; ++b) {
             unsigned m = macc[b];
@@ -677,61 +678,54 @@ template<class R> __global__ void __launch_bounds__(128, 7) k_nlist2(KArgs<R> a,
                 const int bit = __ffs(m) - 1;
                 m &= m - 1u;
                 const uint32_t e = se[mybase + b * 32 + bit];
+                const bool in = (mi >> bit) & 1u;
                 if (qin + qout < cap) {
-                    if ((mi >> bit) & 1u)
-                        col[32 * qin++] = e;
-                    else
-                        col[32 * (cap - 1 - qout++)] = e;
+                    col[32 * (in ? qin : cap - 1 - qout)] = e;
+                    qin += in;
+                    qout += !in;
                 }
                 ++qtot;
             }
+            macc[b] = minn[b] = 0u;
         }
-        __syncwarp();  // every lane is done with the regions before they are restaged
+        __syncwarp();  // every lane is done with se before it is restaged
     };
-    auto clear_masks = [&]() {
 #pragma unroll
-        for (int b = 0; b < MB; ++b) macc[b] = minn[b] = 0u;
-    };
+    for (int b = 0; b < MB; ++b) macc[b] = minn[b] = 0u;
     unsigned todo = __ballot_sync(0xffffffffu, real);
+    unsigned pend = 0u;  // lanes whose masks refer to se
+    int eused = 0;       // entries staged in se
     while (todo) {
-        clear_masks();
-        int used = 0, ng = 0, mybase = 0, big = 0;
-        unsigned rest = todo, biggrp = 0;
-        while (rest) {
-            const int kd = __shfl_sync(0xffffffffu, kme, __ffs(rest) - 1);
-            const unsigned grp = __ballot_sync(0xffffffffu, real && kme == kd) & rest;
-            const int total_c = fetch(kd);
-            if (total_c > REG) {  // more than one region holds: in chunks, alone in its pass
-                if (used == 0) {
-                    big = total_c;
-                    biggrp = grp;
-                    rest &= ~grp;
-                }
-                break;
-            }
-            const int base = used + ((ng - used) & 7);  // bank slot ng mod 8
-            if (base + total_c > TOT) break;           // next pass
-            stage(0, total_c, base);
-            phase1(grp, base, total_c, off[13] + (i - beg[13]));
-            if ((grp >> lane) & 1u) mybase = base;
-            used = base + total_c;
-            ++ng;
-            rest &= ~grp;
-        }
-        todo = rest;
-        if (!big) {
-            phase2(mybase);
-        } else {
-            const int ts0 = off[13] + (i - beg[13]);
-            for (int c0 = 0; c0 < big; c0 += REG) {
-                const int nch = min(REG, big - c0);
-                clear_masks();
+        const int kd = __shfl_sync(0xffffffffu, kme, __ffs(todo) - 1);
+        const unsigned grp = __ballot_sync(0xffffffffu, real && kme == kd) & todo;
+        const int total_c = fetch(kd);
+        todo &= ~grp;
+        const int ts = off[13] + (i - beg[13]);
+        if (total_c > REG) {  // in chunks of REG, each placed at once
+            if (pend) phase2();
+            pend = 0u;
+            eused = 0;
+            mybase = 0;
+            for (int c0 = 0; c0 < total_c; c0 += REG) {
+                const int nch = min(REG, total_c - c0);
                 stage(c0, nch, 0);
-                phase1(biggrp, 0, nch, (ts0 >= c0 && ts0 < c0 + nch) ? ts0 - c0 : -1);
-                phase2(0);
+                phase1(grp, nch, (ts >= c0 && ts < c0 + nch) ? ts - c0 : -1);
+                phase2();
             }
+            continue;
         }
+        if (eused + total_c > SE) {  // se is full: place what it holds
+            phase2();
+            pend = 0u;
+            eused = 0;
+        }
+        stage(0, total_c, eused);
+        phase1(grp, total_c, ts);
+        if ((grp >> lane) & 1u) mybase = eused;
+        eused += total_c;
+        pend |= grp;
     }
+    if (pend) phase2();
     a.nnb[i] = real ? (qin | (qout << 16)) : 0;
     nlist_finalise(a, real ? qtot : 0, cur, lp);
 }
