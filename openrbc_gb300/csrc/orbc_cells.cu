@@ -236,23 +236,30 @@ template<class R> __global__ void __launch_bounds__(256) k_ranges_gather(KArgs<R
     const int *sv = a.sval[fin];
     const int n = a.npad;
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+        // every load of the slot before its first store: the stores may alias
+        // the loads as far as the compiler knows, and would serialise them
         const uint32_t k = sk[p];
-        if (p == 0 || sk[p - 1] != k) a.ranges[k].x = p;
-        if (p == n - 1 || sk[p + 1] != k) a.ranges[k].y = p + 1;
+        const bool first = p == 0 || sk[p - 1] != k, last = p == n - 1 || sk[p + 1] != k;
         const int src = sv[p];
         const auto ps = a.pos[cur][src];
-        a.pos[nc][p] = ps;
-        a.nrm[nc][p] = a.nrm[cur][src];
-        a.vel[nl][p] = a.vel[lp][src];
-        a.omg[nl][p] = a.omg[lp][src];
+        const auto ns = a.nrm[cur][src];
+        const auto vs = a.vel[lp][src];
+        const auto os = a.omg[lp][src];
+        const int cs = a.cell[lp][src], ts = a.tag[lp][src], h = a.home[lp][src];
         if (a.carry_forces) {  // Nose-Hoover carries f and t from one half-step to the next
-            a.frc[nl][p] = a.frc[lp][src];
-            a.trq[nl][p] = a.trq[lp][src];
+            const auto fs = a.frc[lp][src], qs = a.trq[lp][src];
+            a.frc[nl][p] = fs;
+            a.trq[nl][p] = qs;
         }
+        if (first) a.ranges[k].x = p;
+        if (last) a.ranges[k].y = p + 1;
+        a.pos[nc][p] = ps;
+        a.nrm[nc][p] = ns;
+        a.vel[nl][p] = vs;
+        a.omg[nl][p] = os;
         a.xref[nl][p] = ps;  // the list about to be built is referenced to these positions
-        a.cell[nl][p] = a.cell[lp][src];
-        a.tag[nl][p] = a.tag[lp][src];
-        const int h = a.home[lp][src];
+        a.cell[nl][p] = cs;
+        a.tag[nl][p] = ts;
         a.home[nl][p] = h;
         if (h >= 0) a.slot_of_home[h] = p;
         const int w = wbits(ps.w);
