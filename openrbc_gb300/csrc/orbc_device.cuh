@@ -29,7 +29,7 @@ constexpr int NB_SHIFT = 27;
 constexpr int MAX_SLOTS = 1 << 27;
 constexpr int NPART = 8;         // per-warp partial sums: ke2, epot, maxd2, flags, lipid sum v (3), pad
 constexpr int RED_GROUP = 256;   // warp partials (of 32 slots) per reduction group
-constexpr int MESH_CHUNK = 1024; // faces per block of the area / volume kernel
+constexpr int MESH_CHUNK = 256;  // faces per block of the area / volume kernel (one per thread: the FP64 work spreads over all SMs)
 
 enum : int {
     ERRB_NBR_OVERFLOW = 1,  // a neighbour list overflowed its capacity

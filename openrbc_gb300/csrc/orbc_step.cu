@@ -994,10 +994,10 @@ template<class R> __global__ void __launch_bounds__(256) k_mesh(KArgs<R> a) {
             const double e2[3] = {P[2][0] - P[0][0], P[2][1] - P[0][1], P[2][2] - P[0][2]};
             const double nx = e1[1] * e2[2] - e1[2] * e2[1], ny = e1[2] * e2[0] - e1[0] * e2[2],
                          nz = e1[0] * e2[1] - e1[1] * e2[0];
-            ar += 0.5 * sqrt(nx * nx + ny * ny + nz * nz);
+            ar += sqrt(nx * nx + ny * ny + nz * nz);  // twice the area
             const double bx = P[1][1] * P[2][2] - P[1][2] * P[2][1], by = P[1][2] * P[2][0] - P[1][0] * P[2][2],
                          bz = P[1][0] * P[2][1] - P[1][1] * P[2][0];
-            vol += (P[0][0] * bx + P[0][1] * by + P[0][2] * bz) / 6.0;
+            vol += P[0][0] * bx + P[0][1] * by + P[0][2] * bz;  // six times the volume
         }
     }
 #pragma unroll
@@ -1038,6 +1038,8 @@ template<class R> __global__ void __launch_bounds__(256) k_mesh(KArgs<R> a) {
             V += __shfl_xor_sync(0xffffffffu, V, o);
         }
         if (lane == 0) {
+            A *= 0.5;  // the FP64 division once per system, not per face
+            V /= 6.0;
             SysState &ss = a.ss[q];
             ss.area = A;
             ss.volume = V;
