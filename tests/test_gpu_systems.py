@@ -315,6 +315,52 @@ def test_list_build_forms_find_the_same_pairs(precision):
             assert np.array_equal(sets[0][1], lst)
 
 
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+@pytest.mark.parametrize("density", [0.15, 0.9])
+def test_list_build_forms_on_periodic_3d_gases(precision, density):
+    """Uniform gases in a periodic cube, against brute-force minimum-image
+    pairs.  At density 0.15 a warp's 32 particles span about seven cells of
+    about 150 candidates each, more than form 2 keeps staged at once; at 0.9
+    every cell has more than 256 candidates and form 2 takes them in chunks.
+    The three forms must still write the same rows."""
+    from openrbc_gb300 import RTParameter, Simulation
+    n, skin = 4000, 0.4
+    L = (n / density) ** (1.0 / 3.0)
+    rng = np.random.default_rng(21)
+    x = rng.uniform(0.0, L, (n, 3))
+    nv = rng.normal(size=(n, 3))
+    nv /= np.linalg.norm(nv, axis=1, keepdims=True)
+    zero = np.zeros((n, 3))
+    ty = np.zeros(n, np.int32)
+    tag = np.arange(1, n + 1, dtype=np.int32)
+    sets = []
+    for v in (0, 8, 16):
+        p = RTParameter(init="lipid", kBT=1.0, precision=precision, rseed=5)
+        with Simulation(p, box=((0.0, L),) * 3, periodic=(1, 1, 1), skin=skin, kernel_variant=v) as s:
+            s.upload(x, nv, zero, zero, ty, tag)
+            sets.append(s.neighbors())
+    for counts, lst in sets[1:]:
+        assert np.array_equal(sets[0][0], counts)
+        assert np.array_equal(sets[0][1], lst)
+    counts, lst = sets[0]
+    rl2 = (2.6 + skin) ** 2
+    ref = set()
+    for a in range(0, n, 500):
+        d = x[a:a + 500, None, :] - x[None, :, :]
+        d -= L * np.round(d / L)
+        r2 = (d * d).sum(-1)
+        ii, jj = np.nonzero(r2 < rl2)
+        ref.update((int(i) + a, int(j)) for i, j in zip(ii, jj) if int(i) + a != int(j))
+    rows = np.repeat(np.arange(n), counts)
+    got = set(zip(rows.tolist(), lst.tolist()))
+    assert len(got) == len(lst)  # no pair twice
+    tol = 1e-9 if precision == "fp64" else 2e-6
+    for i, j in got ^ ref:  # only pairs on the cutoff sphere may differ
+        d = x[i] - x[j]
+        d -= L * np.round(d / L)
+        assert abs((d * d).sum() - rl2) < tol * rl2, (i, j)
+
+
 def test_autotune_restores_state_and_keeps_stepping():
     from openrbc_gb300 import RTParameter, Simulation
     w, box = lattice_sys(n=8192, ncol=90)
