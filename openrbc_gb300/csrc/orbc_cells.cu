@@ -557,7 +557,7 @@ template<class R> __global__ void __launch_bounds__(128, 7) k_nlist2(KArgs<R> a,
     using T4 = typename Vec<R>::T4;
     if (gated && !__ldcg(&a.S->rebuild)) return;
     constexpr int NLW = 4;                                // warps per block
-    constexpr int MB = 8;                                 // masks (32 candidates each) per region
+    constexpr int MB = 8;                                 // accept masks (32 candidates each) per lane
     constexpr int REG = 32 * MB;                          // candidates of one cell (or chunk) per phase 1
     constexpr int SE = sizeof(T4) == 16 ? 768 : 512;      // list entries staged per warp until phase 2
     __shared__ float2 s_cut[256];                         // (list cutoff^2, range cutoff^2) per type pair
