@@ -339,6 +339,7 @@ template<class R> class Engine : public EngineBase {
         drop_graph();
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
+        if (hsc) cudaFreeHost(hsc);
         for (cudaEvent_t &e : fpack)
             if (e) cudaEventDestroy(e);
         for (cudaEvent_t &e : xev)
@@ -356,6 +357,7 @@ template<class R> class Engine : public EngineBase {
         CK(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
         CK(cudaEventCreate(&ev0));
         CK(cudaEventCreate(&ev1));
+        CK(cudaMallocHost(&hsc, 2 * sizeof(Scalars)));
         for (cudaEvent_t &e : fpack) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
         for (cudaEvent_t &e : xev) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
         for (cudaEvent_t &e : pev) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
@@ -1099,9 +1101,22 @@ template<class R> class Engine : public EngineBase {
     int step(int nsteps, orbc_thermo *out) override {
         if (!uploaded) return fail(ORBC_ERR_STATE, "step before upload");
         if (nsteps < 0) return fail(ORBC_ERR_ARG, "step: negative step count");
-        Scalars before;
-        CK(cudaMemcpyAsync(&before, Sd.p, sizeof(Scalars), cudaMemcpyDeviceToHost, st));
-        CK(cudaStreamSynchronize(st));
+        const int G = 4;  // steps per graph launch; single steps use a one-step graph
+        if (P.use_graph && nsteps > 0) {
+            if (!gexec) {
+                int rc = capture_graph(G, &gexec, &graph_cond);
+                if (rc) return rc;
+                graph_steps = G;
+            }
+            if (nsteps % G && !gexec1) {
+                bool c1 = false;
+                int rc = capture_graph(1, &gexec1, &c1);
+                if (rc) return rc;
+            }
+        }
+        // the counters before and after come back through pinned memory, with
+        // one wait at the end of the call
+        CK(cudaMemcpyAsync(&hsc[0], Sd.p, sizeof(Scalars), cudaMemcpyDeviceToHost, st));
         int64_t extra = 0;
         if (P.zero_bulk && P.integrator == ORBC_INT_LANGEVIN && !vcom_valid) {
             launch_vcom<R>(a, st);
@@ -1119,17 +1134,6 @@ template<class R> class Engine : public EngineBase {
         }
         CK(cudaEventRecord(ev0, st));
         if (P.use_graph && nsteps > 0) {
-            const int G = 4;  // steps per graph launch; single steps use a one-step graph
-            if (!gexec) {
-                int rc = capture_graph(G, &gexec, &graph_cond);
-                if (rc) return rc;
-                graph_steps = G;
-            }
-            if (nsteps % G && !gexec1) {
-                bool c1 = false;
-                int rc = capture_graph(1, &gexec1, &c1);
-                if (rc) return rc;
-            }
             int k = 0;
             for (; k + graph_steps <= nsteps; k += graph_steps) CK(cudaGraphLaunch(gexec, st));
             for (; k < nsteps; ++k) CK(cudaGraphLaunch(gexec1, st));
@@ -1138,12 +1142,12 @@ template<class R> class Engine : public EngineBase {
         }
         CK(cudaGetLastError());
         CK(cudaEventRecord(ev1, st));
-        CK(cudaEventSynchronize(ev1));
+        CK(cudaMemcpyAsync(&hsc[1], Sd.p, sizeof(Scalars), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
         float ms = 0;
         CK(cudaEventElapsedTime(&ms, ev0, ev1));
         last_ms = ms;
-        Scalars hs;
-        CK(cudaMemcpy(&hs, Sd.p, sizeof(Scalars), cudaMemcpyDeviceToHost));
+        const Scalars before = hsc[0], hs = hsc[1];
         const int64_t nreb = hs.rebuilds - before.rebuilds;
         const int per_step = P.use_graph && gexec ? fixed_launches_per_step() : (fixed_launches_per_step() - (graph_cond ? 1 : 0) + rebuild_launches());
         last_launches = extra + int64_t(nsteps) * per_step + (P.use_graph && graph_cond ? nreb * rebuild_launches() : 0);
@@ -1740,6 +1744,7 @@ template<class R> class Engine : public EngineBase {
 
     cudaStream_t st = nullptr, cs = nullptr;  // step stream, frame-copy stream
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, fpack[2] = {nullptr, nullptr};
+    Scalars *hsc = nullptr;  // pinned: the counters before and after step()
     static constexpr int NXCH = 4;  // chunks of the host <-> device state transfers
     cudaEvent_t xev[NXCH] = {}, pev[1] = {};
     int device = 0;
