@@ -18,9 +18,14 @@ e2e        the same metric through the C ABI the reference host would call
 roofline   the fused step kernel: compulsory bytes (104 B per particle-step,
            mixed) / its CUDA-event time vs measured HBM bandwidth; the FP32
            ALU fraction of its algorithmic flops is reported beside it.
-cpu_baseline  the oracle's FP32 port of the reference's CPU step on the
-           host cores, bounded sample.
---impl reference  times that CPU implementation for the same metric.
+cpu_baseline  the oracle's CPU baseline -- the reference's FP32 step organised
+           as its production loop, measured within a few per cent of the
+           reference's own main loop on x86 (oracle/port_vs_reference.py) --
+           on the host cores, a bounded sample; it also checks the GPU's
+           mixed-precision forces against the oracle's FP64 forces.
+--impl reference  times that CPU implementation for the same metric on the
+           same workload, exactly --warmup + --steps steps, without loading
+           the GPU library.
 """
 from __future__ import annotations
 
@@ -48,10 +53,22 @@ BYTES_PER_PSTEP = 104.0
 FLOP_PER_PAIR = 106.0
 
 
-def workload(n_lipid=N_LIPID):
+def workload(n_lipid=N_LIPID, lib=None):
+    """The membrane; `lib` is the library that generates it (default the GPU
+    library; the CPU-only reference arm passes the oracle's build of the same
+    host generators, so that it never loads the GPU library)."""
     from openrbc_gb300 import workloads
     freq = FREQ if n_lipid == N_LIPID else max(4, int(round(FREQ * (n_lipid / N_LIPID) ** 0.5)))
-    return workloads.rbc(n_lipid=n_lipid, freq=freq, kT=KT, seed=2)
+    return workloads.rbc(n_lipid=n_lipid, freq=freq, kT=KT, seed=2, lib=lib)
+
+
+def bench_config(w, n_lipid):
+    """The workload description, identical in both arms."""
+    n = len(w["x"])
+    return {"workload": f"rbc-evans-fung-{n}", "n_particles": n, "n_lipid": n_lipid, "anchors": n - n_lipid,
+            "bonds": int(len(w["bonds"])), "faces": int(len(w["faces"])), "integrator": "langevin", "dt": DT,
+            "kT": KT, "eta": 0.01, "reduced_volume": 0.64,
+            "l2": "inputs larger than L2 (state + neighbour list > 1 GB)", "parallelism": "one system per rank"}
 
 
 def log(*a):
@@ -151,24 +168,46 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def cpu_baseline(w, nsteps=2, precision="f32"):
-    """The oracle's port of the reference CPU step on all host cores."""
-    from oracle import oracle as orc
+CPU_SKIN = 0.6  # neighbour skin of the CPU baseline's Verlet list
+
+
+def oracle_state(w, orc):
     st = orc.State(x=w["x"], nrm=w["n"], v=w["v"], o=w["o"], type=w["type"], tag=w["tag"], bonds=w["bonds"],
                    bond_r0=w["bond_r0"], faces=w["faces"], kBT=KT, dt=DT, eta=0.01, seed=0xBAD5EED,
                    kv=w["constraint"]["kv"], V0=w["constraint"]["V0"], ka=w["constraint"]["ka"],
                    A0=w["constraint"]["A0"])
     st.bstyle[4], st.bK[4], st.br0[4], st.bR[4] = 2, 1.0, 1.0, 2.2
+    return st
+
+
+CPU_KIND = ("the oracle's CPU baseline (orc_run_langevin_fast_f32): the reference's FP32 Langevin step "
+            "(src/compute_pairwise_fused.h, src/compute_bonded.h, src/integrate_langevin.h) organised as its "
+            "production loop -- cell-sorted particles, Verlet list, Newton's third law inside each thread's "
+            "range -- built with the reference's -O3 -ffast-math native flags; on x86 it runs within a few "
+            "per cent of the reference's own main loop on the same states (oracle/port_vs_reference.py)")
+
+
+def cpu_baseline(w, nsteps=20, f_mixed=None):
+    """The oracle's CPU baseline on all host cores (bounded sample), and --
+    as the checker -- the oracle's FP64 forces of the same state against the
+    GPU's mixed-precision forces."""
+    from oracle import oracle as orc
     threads = os.cpu_count() or 1
     orc.set_threads(threads)
+    out = {}
+    if f_mixed is not None:
+        f64, _, _, _ = orc.forces(oracle_state(w, orc), "f64")
+        out["force_rel_err_mixed_vs_oracle_fp64"] = float(np.linalg.norm(f_mixed - f64) / np.linalg.norm(f64))
+    st = oracle_state(w, orc)
+    orc.cpu_baseline_run(st, 1, CPU_SKIN)  # warm-up
     t0 = time.perf_counter()
-    orc.langevin(st, nsteps, precision, fast=True)
+    th = orc.cpu_baseline_run(st, nsteps, CPU_SKIN)
     dt = time.perf_counter() - t0
     n = len(w["x"])
-    return {"value": n * nsteps / dt, "unit": "particle-steps/s", "cores": orc.get_threads(), "kind": "port",
-            "sample": f"{nsteps} Langevin steps of the full {n}-particle membrane, FP32, oracle port of "
-                      f"src/compute_pairwise_fused.h + src/integrate_langevin.h built with the reference's "
-                      f"-O3 -ffast-math native flags"}
+    out.update({"value": n * nsteps / dt, "unit": "particle-steps/s", "cores": orc.get_threads(), "kind": "port",
+                "sample": f"{nsteps} Langevin steps of the full {n}-particle membrane ({th['npairs']} list builds), "
+                          f"FP32; " + CPU_KIND})
+    return out
 
 
 def dist_setup():
@@ -197,25 +236,34 @@ def allreduce_max(v, ws):
 
 
 def run_reference(args, rank, ws):
+    """The reference arm: the oracle's CPU baseline (the reference's CPU step,
+    see CPU_KIND) on the host cores, exactly --warmup untimed then --steps
+    timed steps of the same workload.  Loads no GPU library: the workload
+    comes from the oracle's build of the host generators."""
     if rank != 0:
         return 0
-    w = workload(args.n_lipid)
     from oracle import oracle as orc
     orc.build()
+    w = workload(args.n_lipid, lib=orc.workloads_lib())
     n = len(w["x"])
-    for _ in range(args.warmup):
-        pass  # the CPU port has no warm-up state; warm-up steps are skipped to bound the run
-    cb = cpu_baseline(w, nsteps=max(1, args.steps // 10))
-    line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": "particle-steps/s",
-            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": 1e3 * n / cb["value"], "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": f"rbc-evans-fung-{n}", "n_particles": n, "n_lipid": args.n_lipid,
-                       "anchors": n - args.n_lipid, "bonds": int(len(w["bonds"])), "faces": int(len(w["faces"])),
-                       "integrator": "langevin", "dt": DT, "kT": KT, "precision": "fp32 (the reference's real)",
-                       "parallelism": f"host threads x{cb['cores']}"},
-            "cpu_baseline": cb, "e2e": {"value": cb["value"], "unit": "particle-steps/s",
-                                        "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    threads = os.cpu_count() or 1
+    orc.set_threads(threads)
+    st = oracle_state(w, orc)
+    if args.warmup > 0:
+        orc.cpu_baseline_run(st, args.warmup, CPU_SKIN)
+    t0 = time.perf_counter()
+    th = orc.cpu_baseline_run(st, args.steps, CPU_SKIN)
+    secs = time.perf_counter() - t0
+    value = n * args.steps / secs
+    cb = {"value": value, "unit": "particle-steps/s", "cores": orc.get_threads(), "kind": "port",
+          "sample": f"the full workload: {args.warmup} warm-up + {args.steps} timed Langevin steps "
+                    f"({th['npairs']} list builds in the timed steps), FP32; " + CPU_KIND}
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "particle-steps/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "precision": "fp32 (the reference's real)", "config": bench_config(w, args.n_lipid),
+            "cpu_baseline": cb, "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
+                                        "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
 
@@ -303,7 +351,7 @@ def main():
         host = [torch.empty((n, 3), dtype=torch.float32, pin_memory=True).numpy() for _ in range(4)]
         for h, arr in zip(host, sim.download()):
             h[:] = arr
-        e2e_steps = max(10, args.steps // 10)
+        e2e_steps = max(100, args.steps)
 
         def e2e_step():
             N.check(L.orbc_gpu_set_state_f32(sim.h, 0, n, 3, *[h.ctypes.data for h in host]), sim.h)
@@ -346,20 +394,19 @@ def main():
     line = {"metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": f"rbc-evans-fung-{n}", "n_particles": n, "n_lipid": args.n_lipid,
-                       "anchors": n - args.n_lipid, "bonds": int(len(w["bonds"])), "faces": int(len(w["faces"])),
-                       "integrator": "langevin", "dt": DT, "kT": KT,
-                       "skin": tune["chosen"]["skin"] if tune else (args.skin if args.skin is not None else SKIN),
-                       "kernel_form": tune["chosen"]["variant"] if tune else args.form, "precision": "mixed",
-                       "l2": "inputs larger than L2 (state + neighbour list > 1 GB)",
-                       "parallelism": f"replicas x{ws}"},
+            "precision": "mixed (FP32 pair / bond arithmetic, positions as int32 cell + FP32 offset, FP64 "
+                         "area / volume / kinetic-energy sums)",
+            "config": bench_config(w, args.n_lipid),
+            "tuning": {"skin": tune["chosen"]["skin"] if tune else (args.skin if args.skin is not None else SKIN),
+                       "kernel_form": tune["chosen"]["variant"] if tune else args.form},
             "fp64": fp64, "mixed_over_fp64": (value / ws / fp64["value"]) if fp64 else None,
             "force_rel_err_mixed_vs_fp64": ferr, "rebuilds_in_timed_region": th["rebuilds"] - th0["rebuilds"],
             "roofline": roof, "e2e": e2e, "gpu_launches": launches, "clocks": clk.summary(), "profile": prof,
             "autotune": tune}
     sim.close()
     if rank == 0 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(w)
+        line["cpu_baseline"] = cpu_baseline(w, f_mixed=f_mixed)
+        line["force_rel_err_mixed_vs_oracle_fp64"] = line["cpu_baseline"].pop("force_rel_err_mixed_vs_oracle_fp64")
         log(f"cpu baseline: {line['cpu_baseline']}")
     if rank == 0:
         print(json.dumps(line), flush=True)

@@ -346,8 +346,12 @@ int orbc_gpu_morton_order(const double *p3, int64_t n, const double *bsize3, int
  * about 3.1 MB in the library's device memory, present on every GPU that
  * loads the library until the process exits; nothing is allocated per call.
  * n above ORBC_NOALLOC_MAX_POINTS returns ORBC_ERR_ARG.  The first call on a
- * device looks up that array's device address (with the device current);
- * make that first call before any stream capture.  Work is queued on
+ * device looks up that array's device address (with the device current) and
+ * caches it with the context's id, so a call after cudaDeviceReset looks it up
+ * again; make the first call on a device (and the first after a reset) before
+ * any stream capture.  A CUDA error already pending when the call starts is
+ * reported (ORBC_ERR_CUDA) and left pending; orbc_gpu_error(NULL) gives the
+ * message of any failure.  Work is queued on
  * `stream` (a cudaStream_t, NULL for the default stream) and the call returns
  * without waiting.  All calls share the one scratch array: calls whose work
  * overlaps on the GPU (other streams, other host threads) race and corrupt

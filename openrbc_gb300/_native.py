@@ -146,15 +146,22 @@ def lib():
         L.orbc_gpu_error.argtypes = [H]
         L.orbc_gpu_error.restype = C.c_char_p
         L.orbc_gpu_version.restype = C.c_char_p
-        # workload generators (host code)
-        L.orbc_gen_lattice.argtypes = [i64, i32, d, d, d, d, C.c_uint64, vp, vp, vp, vp, vp, vp]
-        L.orbc_gen_rbc_counts.argtypes = [i64, i32, P(i64), P(i64), P(i64)]
-        L.orbc_gen_rbc.argtypes = [i64, i32, d, C.c_uint64, vp, vp, vp, vp, vp, vp, vp, vp, vp, P(d), P(d),
-                                   P(d)]
-        L.orbc_gen_vesicle_sizes.argtypes = [i32, i64, i64, i64, i64, C.c_uint64, vp]
-        L.orbc_gen_vesicle.argtypes = [i64, d, d, C.c_uint64, i32, vp, vp, vp, vp, vp, vp, P(d)]
+        declare_generators(L)
         _lib = L
         return L
+
+
+def declare_generators(L):
+    """Argument types of the host-only workload generators
+    (include/orbc_workloads.h) on a library that exports them."""
+    vp, i64, i32, d = C.c_void_p, C.c_int64, C.c_int, C.c_double
+    P = C.POINTER
+    L.orbc_gen_lattice.argtypes = [i64, i32, d, d, d, d, C.c_uint64, vp, vp, vp, vp, vp, vp]
+    L.orbc_gen_rbc_counts.argtypes = [i64, i32, P(i64), P(i64), P(i64)]
+    L.orbc_gen_rbc.argtypes = [i64, i32, d, C.c_uint64, vp, vp, vp, vp, vp, vp, vp, vp, vp, P(d), P(d), P(d)]
+    L.orbc_gen_vesicle_sizes.argtypes = [i32, i64, i64, i64, i64, C.c_uint64, vp]
+    L.orbc_gen_vesicle.argtypes = [i64, d, d, C.c_uint64, i32, vp, vp, vp, vp, vp, vp, P(d)]
+    return L
 
 
 def check(rc, handle=None):

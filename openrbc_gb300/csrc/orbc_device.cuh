@@ -251,5 +251,7 @@ int radix_sort_pairs(uint32_t *keys[2], int *vals[2], int *counts, int *digit_to
                      int passes, int ntiles, const int *gate, cudaStream_t st);
 int sort_tiles(int64_t n);
 constexpr int SORT_TILE = 4096;
+// message of the handle-less entry points, read back by orbc_gpu_error(NULL)
+void set_standalone_error(const char *what, const char *detail);
 
 }  // namespace orbc

@@ -1789,6 +1789,12 @@ struct orbc_handle {
     std::unique_ptr<EngineBase> e;
 };
 
+namespace orbc {
+void set_standalone_error(const char *what, const char *detail) {
+    g_last_error = std::string(what) + ": " + detail;
+}
+}  // namespace orbc
+
 extern "C" {
 
 void orbc_gpu_default_params(orbc_params *p) {

@@ -11,10 +11,14 @@
 //   k_forces          forces only (parity hook)
 //   k_mesh            FP64 membrane area and enclosed volume per system
 //
-// Each step kernel ends with a deterministic reduction: every 256-slot block
-// writes its partial sums, the last block to finish (ticket counter) adds them
-// per system in a fixed order and updates the thermostat, the rebuild flag,
-// the step counter and the buffer parity.
+// Per-system sums are deterministic and take two launches: each warp of a
+// step kernel reduces its 32 particles with shuffles and stores one warp
+// partial (warp_partials); k_reduce, launched next on the stream, adds the
+// warp partials of each reduction group in a fixed tree, and its last block
+// adds each system's group sums in a fixed order and applies the thermostat,
+// the rebuild rule, the step counter and the buffer parity.  The lite Langevin
+// kernel keeps no sums: each warp raises the rebuild flag itself and
+// k_advance flips the buffers.
 #include "orbc_device.cuh"
 
 namespace orbc {

@@ -4,6 +4,10 @@ lattice     flat jittered lipid lattice (the plain small workload)
 rbc         whole red-cell membrane: Evans-Fung surface, lipids by area,
             geodesic spectrin mesh with WLC-POW bonds and area/volume mesh
 vesicles    a batch of spherical vesicles with log-normal sizes
+
+The generators are host code.  Each function takes an optional `lib`: any
+ctypes library that exports them (declared with _native.declare_generators);
+the default is liborbc_gpu.so, which contains them.
 """
 from __future__ import annotations
 
@@ -18,18 +22,22 @@ from . import _native as N
 RBC_BOND_TABLE = {4: {"style": N.BOND_WLC_POW, "K": 1.0, "r0": 1.0, "R": 2.2}}
 
 
-def lattice(n=32768, ncol=182, spacing=1.1, jitter=0.05, tilt=0.05, kT=1.0, seed=1):
+def _gen(lib):
+    return lib if lib is not None else N.lib()
+
+
+def lattice(n=32768, ncol=182, spacing=1.1, jitter=0.05, tilt=0.05, kT=1.0, seed=1, lib=None):
     x, nn, v, o = (np.zeros((n, 3)) for _ in range(4))
     ty, tg = np.zeros(n, np.int32), np.zeros(n, np.int32)
-    rc = N.lib().orbc_gen_lattice(n, ncol, spacing, jitter, tilt, kT, seed, x.ctypes.data, nn.ctypes.data,
+    rc = _gen(lib).orbc_gen_lattice(n, ncol, spacing, jitter, tilt, kT, seed, x.ctypes.data, nn.ctypes.data,
                                   v.ctypes.data, o.ctypes.data, ty.ctypes.data, tg.ctypes.data)
     if rc:
         raise ValueError("orbc_gen_lattice failed")
     return {"x": x, "n": nn, "v": v, "o": o, "type": ty, "tag": tg}
 
 
-def rbc(n_lipid=4_000_000, freq=57, kT=1.0, seed=2, reduced_volume=0.64, kv=10.0, ka=10.0):
-    L = N.lib()
+def rbc(n_lipid=4_000_000, freq=57, kT=1.0, seed=2, reduced_volume=0.64, kv=10.0, ka=10.0, lib=None):
+    L = _gen(lib)
     nt, nb, nf = C.c_int64(), C.c_int64(), C.c_int64()
     L.orbc_gen_rbc_counts(n_lipid, freq, C.byref(nt), C.byref(nb), C.byref(nf))
     n = nt.value
@@ -52,8 +60,9 @@ def rbc(n_lipid=4_000_000, freq=57, kT=1.0, seed=2, reduced_volume=0.64, kv=10.0
             "constraint": {"kv": kv, "V0": V0, "ka": ka, "A0": area}}
 
 
-def vesicles(nves=96, nmin=10_000, nmax=250_000, median=40_000, total=5_000_000, kT=1.0, seed=4, rho=1.05):
-    L = N.lib()
+def vesicles(nves=96, nmin=10_000, nmax=250_000, median=40_000, total=5_000_000, kT=1.0, seed=4, rho=1.05,
+             lib=None):
+    L = _gen(lib)
     sizes = np.zeros(nves, np.int64)
     if L.orbc_gen_vesicle_sizes(nves, nmin, nmax, median, total, seed, sizes.ctypes.data):
         raise ValueError("orbc_gen_vesicle_sizes failed")

@@ -20,8 +20,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "liborbc_oracle.so")
 LIB_FAST = os.path.join(HERE, "liborbc_oracle_fast.so")
+LIB_WORKLOADS = os.path.join(HERE, "liborbc_workloads.so")
 REF_DIR = os.path.join(HERE, "_ref")
-DEFAULT_REF_SRC = "/root/reference/src"
 
 BOND_HARMONIC, BOND_FENE, BOND_WLC_POW = 0, 1, 2
 MAX_BOND_TYPES = 8
@@ -30,13 +30,17 @@ _lock = threading.Lock()
 _lib = None
 _lib_fast = None
 _ref = {}
+_workloads = None
 
 
 def build(ref_src: Optional[str] = None) -> None:
-    """Compile the oracle (and the reference harness when its source exists)."""
-    subprocess.run(["make", "-s", "-C", HERE, "liborbc_oracle.so", "liborbc_oracle_fast.so"], check=True)
-    src = ref_src or os.environ.get("ORBC_REF_SRC", DEFAULT_REF_SRC)
-    if os.path.isdir(src):
+    """Compile the oracle, and the reference harness when the reference's
+    source directory is given (argument, or the ORBC_REF_SRC environment
+    variable) and exists."""
+    subprocess.run(["make", "-s", "-C", HERE, "liborbc_oracle.so", "liborbc_oracle_fast.so", "liborbc_workloads.so"],
+                   check=True)
+    src = ref_src or os.environ.get("ORBC_REF_SRC")
+    if src and os.path.isdir(src):
         subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={src}"], check=True,
                        stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
 
@@ -180,6 +184,7 @@ def lib(fast: bool = False):
                 getattr(L, name).argtypes = [P(OrcSystemC), C.c_void_p, C.c_void_p, C.c_void_p, P(OrcThermoC)]
             for name in ("orc_step_langevin_f64", "orc_step_langevin_f32", "orc_step_nh_f64"):
                 getattr(L, name).argtypes = [P(OrcSystemC), C.c_int, P(OrcThermoC)]
+            L.orc_run_langevin_fast_f32.argtypes = [P(OrcSystemC), C.c_int, C.c_double, P(OrcThermoC)]
             L.orc_nh_prologue_f64.argtypes = [P(OrcSystemC), P(OrcThermoC)]
             L.orc_thermo_f64.argtypes = [P(OrcSystemC), P(OrcThermoC)]
             L.orc_pairs.argtypes = [P(OrcSystemC), C.c_void_p, C.c_void_p, C.c_int64]
@@ -196,6 +201,21 @@ def lib(fast: bool = False):
             else:
                 _lib = L
     return _lib_fast if fast else _lib
+
+
+def workloads_lib():
+    """The library's host-only input generators built by this directory's
+    Makefile (same sources and flags as the library), so that a CPU-only
+    process makes the benchmark's inputs without loading the GPU library.
+    Pass it as `lib=` to openrbc_gb300.workloads."""
+    global _workloads
+    with _lock:
+        if _workloads is None:
+            if not os.path.exists(LIB_WORKLOADS):
+                subprocess.run(["make", "-s", "-C", HERE, "liborbc_workloads.so"], check=True)
+            from openrbc_gb300._native import declare_generators
+            _workloads = declare_generators(C.CDLL(LIB_WORKLOADS))
+    return _workloads
 
 
 def _thermo(th: OrcThermoC) -> dict:
@@ -234,6 +254,20 @@ def langevin(st: State, nsteps: int, precision: str = "f64", fast: bool = False)
     th = OrcThermoC()
     fn = L.orc_step_langevin_f64 if precision == "f64" else L.orc_step_langevin_f32
     fn(C.byref(c), int(nsteps), C.byref(th))
+    _sync_back(st, c)
+    return _thermo(th)
+
+
+def cpu_baseline_run(st: State, nsteps: int, skin: float = 0.4) -> dict:
+    """nsteps FP32 Langevin steps organised as the reference's production
+    loop runs (orc_run_langevin_fast_f32, built with the reference's
+    optimisation flags): the timed CPU baseline.  thermo['npairs'] holds the
+    number of neighbour-list builds."""
+    L = lib(True)
+    c = st._c()
+    th = OrcThermoC()
+    if L.orc_run_langevin_fast_f32(C.byref(c), int(nsteps), float(skin), C.byref(th)):
+        raise ValueError("orc_run_langevin_fast_f32: bad argument")
     _sync_back(st, c)
     return _thermo(th)
 

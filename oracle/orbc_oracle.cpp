@@ -824,6 +824,477 @@ void nh_initial(orc_system *s) {
     s->zeta += 0.5 * s->dt / s->Q * (ke - 0.5 * 3.0 * double(n) * s->kBT);  // :182-185
 }
 
+/* ------------------------------------------------------------------ */
+/* The timed CPU baseline.                                             */
+/* ------------------------------------------------------------------ */
+/* Langevin steps with the physics of langevin_impl<float> -- pair, bond and
+ * mesh-constraint forces, then src/integrate_langevin.h:105-146 with the
+ * counter-based noise -- organised the way the reference's default build runs
+ * its main loop (src/openrbc.cpp:189-256), so that its speed stands for the
+ * reference's own CPU path:
+ *  - particles stay sorted by cell and are re-sorted at every list build, as
+ *    the reference re-sorts them every freq_voronoi steps (src/reorder.h:113-149);
+ *  - pairs come from a Verlet list (cutoff + skin), rebuilt when a particle has
+ *    moved more than skin/2 since the last build, in place of the reference's
+ *    Voronoi cell list re-tessellated on a fixed cadence;
+ *  - Newton's third law inside each thread's contiguous range of sorted
+ *    particles, both sides across ranges (src/compute_pairwise_fused.h:262-275);
+ *  - FP32 state and arithmetic (real = float, src/config_static.h:34); mesh
+ *    area and volume in FP64.
+ * Only the order of each particle's sums differs from langevin_impl<float>. */
+struct FastRun {
+    int64_t n = 0;
+    int T = 1;
+    Box b;
+    float L[3] = {0, 0, 0};
+    float skin = 0.4f;
+    std::vector<int> src;      // sorted slot -> caller index
+    std::vector<int> slot_of;  // caller index -> sorted slot
+    std::vector<float> x, nr, v, o, f, t, xref;
+    std::vector<int> ty, tg;
+    std::vector<int64_t> nbeg;
+    std::vector<int> nl;
+    std::vector<int> cid, perm, cs, s1;  // list-build scratch, kept between builds
+    std::vector<float> s3;
+    std::vector<int64_t> start, cnt;
+    std::vector<std::vector<int>> part;
+    float rl2[NT * NT];
+    float cut2[NT * NT];  // largest interaction range^2 of each type pair
+    int64_t builds = 0;
+
+    int64_t range_begin(int r) const { return n * r / T; }
+    int range_of(int64_t k) const {
+        int r = int((k * T) / std::max<int64_t>(n, 1));
+        while (r + 1 < T && k >= range_begin(r + 1)) ++r;
+        while (r > 0 && k < range_begin(r)) --r;
+        return r;
+    }
+
+    void load(const orc_system *s, int threads, double skin_) {
+        n = s->n;
+        T = std::max(1, threads);
+        b = box_of(s);
+        for (int d = 0; d < 3; ++d) L[d] = float(b.L[d]);
+        skin = float(skin_);
+        src.resize(size_t(n));
+        slot_of.resize(size_t(n));
+        x.resize(size_t(3 * n));
+        nr.resize(size_t(3 * n));
+        v.resize(size_t(3 * n));
+        o.resize(size_t(3 * n));
+        f.assign(size_t(3 * n), 0.f);
+        t.assign(size_t(3 * n), 0.f);
+        xref.resize(size_t(3 * n));
+        ty.resize(size_t(n));
+        tg.resize(size_t(n));
+#pragma omp parallel for schedule(static) num_threads(T)
+        for (int64_t i = 0; i < n; ++i) {
+            src[size_t(i)] = int(i);
+            for (int d = 0; d < 3; ++d) {
+                x[size_t(3 * i + d)] = float(s->x[3 * i + d]);
+                nr[size_t(3 * i + d)] = float(s->nrm[3 * i + d]);
+                v[size_t(3 * i + d)] = float(s->v[3 * i + d]);
+                o[size_t(3 * i + d)] = float(s->o[3 * i + d]);
+            }
+            ty[size_t(i)] = s->type[i];
+            tg[size_t(i)] = s->tag[i];
+        }
+        const FF<double> &F = ff<double>();
+        for (int k = 0; k < NT * NT; ++k) {
+            const double c = F.cut_pair[k];
+            rl2[k] = c > 0 ? float((c + skin_) * (c + skin_)) : 0.f;
+            cut2[k] = float(c * c);
+        }
+    }
+
+    float dxw(float d, int dim) const { return b.per[dim] ? d - L[dim] * std::nearbyint(d / L[dim]) : d; }
+
+    /* re-sort by cell of side (largest cutoff + skin) and rebuild the list */
+    void rebuild(double cmax) {
+        const double w0 = cmax + skin;
+        double lo[3], w[3];
+        int nc[3];
+        for (int d = 0; d < 3; ++d) {
+            double mn = b.lo[d], mx = b.lo[d] + b.L[d];
+            if (!b.per[d]) {
+                float fmn = 3e38f, fmx = -3e38f;
+#pragma omp parallel for schedule(static) num_threads(T) reduction(min : fmn) reduction(max : fmx)
+                for (int64_t k = 0; k < n; ++k) {
+                    fmn = std::min(fmn, x[size_t(3 * k + d)]);
+                    fmx = std::max(fmx, x[size_t(3 * k + d)]);
+                }
+                mn = double(fmn) - 1e-3;
+                mx = double(fmx) + 1e-3;
+            }
+            nc[d] = std::max(1, int(std::floor((mx - mn) / w0)));
+            if (b.per[d] && nc[d] < 3) nc[d] = 1;  // too small to wrap: one cell, all pairs
+            nc[d] = std::min(nc[d], 1024);
+            lo[d] = mn;
+            w[d] = (mx - mn) / nc[d];
+        }
+        const int64_t ncell = int64_t(nc[0]) * nc[1] * nc[2];
+        cid.resize(size_t(n));
+        auto coord = [&](double val, int d) {
+            int c = int(std::floor((val - lo[d]) / w[d]));
+            if (b.per[d]) {
+                c %= nc[d];
+                if (c < 0) c += nc[d];
+            } else {
+                c = std::min(std::max(c, 0), nc[d] - 1);
+            }
+            return c;
+        };
+#pragma omp parallel for schedule(static) num_threads(T)
+        for (int64_t k = 0; k < n; ++k)
+            cid[size_t(k)] = coord(x[size_t(3 * k)], 0) +
+                             nc[0] * (coord(x[size_t(3 * k + 1)], 1) + nc[1] * coord(x[size_t(3 * k + 2)], 2));
+        start.assign(size_t(ncell + 1), 0);
+        for (int64_t k = 0; k < n; ++k) start[size_t(cid[size_t(k)] + 1)]++;
+        for (int64_t c = 0; c < ncell; ++c) start[size_t(c + 1)] += start[size_t(c)];
+        perm.resize(size_t(n));
+        {
+            std::vector<int64_t> fill(start.begin(), start.end() - 1);
+            for (int64_t k = 0; k < n; ++k) perm[size_t(fill[size_t(cid[size_t(k)])]++)] = int(k);
+        }
+        // gather every per-particle array into the new order (through one
+        // scratch buffer per element type, kept between builds)
+        auto g3 = [&](std::vector<float> &a) {
+            s3.resize(a.size());
+#pragma omp parallel for schedule(static) num_threads(T)
+            for (int64_t k = 0; k < n; ++k)
+                for (int d = 0; d < 3; ++d) s3[size_t(3 * k + d)] = a[size_t(3 * perm[size_t(k)] + d)];
+            a.swap(s3);
+        };
+        auto g1 = [&](std::vector<int> &a) {
+            s1.resize(a.size());
+#pragma omp parallel for schedule(static) num_threads(T)
+            for (int64_t k = 0; k < n; ++k) s1[size_t(k)] = a[size_t(perm[size_t(k)])];
+            a.swap(s1);
+        };
+        g3(x);
+        g3(nr);
+        g3(v);
+        g3(o);
+        g1(ty);
+        g1(tg);
+        g1(src);
+        cs.resize(size_t(n));
+#pragma omp parallel for schedule(static) num_threads(T)
+        for (int64_t k = 0; k < n; ++k) {
+            slot_of[size_t(src[size_t(k)])] = int(k);
+            cs[size_t(k)] = cid[size_t(perm[size_t(k)])];
+        }
+        // one pass over the 27 neighbour cells; each thread collects the lists
+        // of its own range of slots, which are then laid out in slot order
+        // Each thread walks its own range of slots cell by cell: the candidates of
+        // the 27 cells around the current cell are staged once (shifted by the
+        // periodic image they were reached through), then every particle of the
+        // cell is tested against them.  Its lists land in slot order.
+        bool wrap_each = false;  // a periodic axis of one or two cells: minimum image per candidate
+        for (int d = 0; d < 3; ++d)
+            if (b.per[d] && nc[d] < 3) wrap_each = true;
+        part.resize(size_t(T));
+        cnt.resize(size_t(n) + 1);
+        cnt[0] = 0;
+#pragma omp parallel num_threads(T)
+        {
+            const int r = omp_get_thread_num();
+            const int64_t rb = range_begin(r), re = range_begin(r + 1);
+            std::vector<int> &mine = part[size_t(r)];  // kept between builds: no fresh pages
+            mine.clear();
+            std::vector<float> sx;
+            std::vector<int> sj, st;
+            int cur = -1;
+            for (int64_t k = rb; k < re; ++k) {
+                const int c = cs[size_t(k)];
+                if (c != cur) {
+                    cur = c;
+                    sx.clear();
+                    sj.clear();
+                    st.clear();
+                    const int cc[3] = {c % nc[0], (c / nc[0]) % nc[1], c / (nc[0] * nc[1])};
+                    int lo3[3], hi3[3];
+                    for (int d = 0; d < 3; ++d) {
+                        if (nc[d] < 3 && b.per[d]) {
+                            lo3[d] = 0;
+                            hi3[d] = nc[d] - 1;  // every cell of the axis once
+                        } else if (b.per[d]) {
+                            lo3[d] = -1;
+                            hi3[d] = 1;
+                        } else {
+                            lo3[d] = cc[d] > 0 ? -1 : 0;
+                            hi3[d] = cc[d] < nc[d] - 1 ? 1 : 0;
+                        }
+                    }
+                    for (int dz = lo3[2]; dz <= hi3[2]; ++dz)
+                        for (int dy = lo3[1]; dy <= hi3[1]; ++dy)
+                            for (int dx_ = lo3[0]; dx_ <= hi3[0]; ++dx_) {
+                                const int dd[3] = {dx_, dy, dz};
+                                int q[3];
+                                float sh[3] = {0.f, 0.f, 0.f};
+                                for (int d = 0; d < 3; ++d) {
+                                    q[d] = (nc[d] < 3 && b.per[d]) ? dd[d] : cc[d] + dd[d];
+                                    if (b.per[d] && nc[d] >= 3) {
+                                        if (q[d] < 0) {
+                                            q[d] += nc[d];
+                                            sh[d] = -L[d];
+                                        } else if (q[d] >= nc[d]) {
+                                            q[d] -= nc[d];
+                                            sh[d] = L[d];
+                                        }
+                                    }
+                                }
+                                const int64_t cell = q[0] + int64_t(nc[0]) * (q[1] + int64_t(nc[1]) * q[2]);
+                                for (int64_t j = start[size_t(cell)]; j < start[size_t(cell + 1)]; ++j) {
+                                    for (int d = 0; d < 3; ++d) sx.push_back(x[size_t(3 * j + d)] + sh[d]);
+                                    sj.push_back(int(j));
+                                    st.push_back(ty[size_t(j)]);
+                                }
+                            }
+                }
+                const float *rl2k = &rl2[ty[size_t(k)] * NT];
+                const float xk0 = x[size_t(3 * k)], xk1 = x[size_t(3 * k + 1)], xk2 = x[size_t(3 * k + 2)];
+                const size_t before = mine.size();
+                const int m = int(sj.size());
+                mine.resize(before + size_t(m));
+                int *out = mine.data() + before;
+                int acc = 0;
+                for (int u = 0; u < m; ++u) {  // branch-free: every candidate is written, the count advances on a hit
+                    const int j = sj[size_t(u)];
+                    float e0 = xk0 - sx[size_t(3 * u)], e1 = xk1 - sx[size_t(3 * u + 1)], e2 = xk2 - sx[size_t(3 * u + 2)];
+                    if (wrap_each) {
+                        e0 = dxw(e0, 0);
+                        e1 = dxw(e1, 1);
+                        e2 = dxw(e2, 2);
+                    }
+                    // Newton on inside the range: j after k there, any j outside (never k itself)
+                    const bool keep = (int64_t(j) > k || int64_t(j) < rb) & (e0 * e0 + e1 * e1 + e2 * e2 < rl2k[st[size_t(u)]]);
+                    out[acc] = j;
+                    acc += keep ? 1 : 0;
+                }
+                mine.resize(before + size_t(acc));
+                cnt[size_t(k + 1)] = acc;
+            }
+        }
+        nbeg.assign(size_t(n) + 1, 0);
+        for (int64_t k = 0; k < n; ++k) nbeg[size_t(k + 1)] = nbeg[size_t(k)] + cnt[size_t(k + 1)];
+        nl.resize(size_t(nbeg[size_t(n)]));
+#pragma omp parallel num_threads(T)
+        {
+            const int r = omp_get_thread_num();
+            std::copy(part[size_t(r)].begin(), part[size_t(r)].end(), nl.begin() + nbeg[size_t(range_begin(r))]);
+        }
+        xref = x;
+        ++builds;
+    }
+
+    float max_disp2() const {
+        float m = 0.f;
+#pragma omp parallel for schedule(static) num_threads(T) reduction(max : m)
+        for (int64_t k = 0; k < n; ++k) {
+            float d2 = 0.f;
+            for (int d = 0; d < 3; ++d) {
+                const float e = x[size_t(3 * k + d)] - xref[size_t(3 * k + d)];
+                d2 += e * e;
+            }
+            m = std::max(m, d2);
+        }
+        return m;
+    }
+};
+
+int fast_langevin_f32(orc_system *s, int nsteps, double skin, orc_thermo *th) {
+    using R = float;
+    const FF<R> &F = ff<R>();
+    FastRun z;
+    z.load(s, g_threads > 0 ? g_threads : omp_get_max_threads(), skin);
+    const int64_t n = z.n;
+    const double cmax = present_cut_max(s);
+    R gamma[NT], sigma[NT];
+    for (int i = 0; i < NT; ++i) {  // src/integrate_langevin.h:110-114
+        gamma[i] = R(6.0 * M_PI * double(R(s->eta)) * double(F.radius[i]));
+        sigma[i] = R(double(std::sqrt(R(2 * R(s->kBT) * gamma[i]))) * std::sqrt(3.0 / s->dt));
+    }
+    const R dt = R(s->dt);
+    TagMap tm;
+    tm.build(s->tag, n);
+    int flags = 0;
+    for (int st = 0; st < nsteps; ++st) {
+        if (z.builds == 0 || z.max_disp2() > 0.25f * z.skin * z.skin) z.rebuild(cmax);
+        std::fill(z.f.begin(), z.f.end(), 0.f);
+        std::fill(z.t.begin(), z.t.end(), 0.f);
+#pragma omp parallel num_threads(z.T)
+        {
+            const int r = omp_get_thread_num();
+            const int64_t beg = z.range_begin(r), end = z.range_begin(r + 1);
+            const bool anyper = z.b.per[0] || z.b.per[1] || z.b.per[2];
+            const R llcut = F.cutlp[0], llcutsq = F.cutsqlp[0], llrep = F.replp[0], llatt = F.attlp[0],
+                    llalpha = F.alphalp[0];
+            constexpr int QB = 64;  // list entries filtered per batch
+            int qj[QB];
+            R qd[QB][3], qr2[QB];
+            for (int64_t k = beg; k < end; ++k) {
+                const int tk = z.ty[size_t(k)];
+                R fk[3] = {0, 0, 0}, tq[3] = {0, 0, 0};
+                const float *xk = &z.x[size_t(3 * k)], *nk = &z.nr[size_t(3 * k)];
+                const R *cut2k = &z.cut2[size_t(tk * NT)];
+                for (int64_t q0 = z.nbeg[size_t(k)]; q0 < z.nbeg[size_t(k + 1)]; q0 += QB) {
+                    // the partners inside their pair's range first (branch-free), then their forces
+                    const int m = int(std::min<int64_t>(QB, z.nbeg[size_t(k + 1)] - q0));
+                    int h = 0;
+                    for (int u = 0; u < m; ++u) {
+                        const int j = z.nl[size_t(q0 + u)];
+                        R d3[3];
+                        if (anyper)
+                            for (int d = 0; d < 3; ++d) d3[d] = z.dxw(xk[d] - z.x[size_t(3 * j + d)], d);
+                        else
+                            for (int d = 0; d < 3; ++d) d3[d] = xk[d] - z.x[size_t(3 * j + d)];
+                        const R r2 = d3[0] * d3[0] + d3[1] * d3[1] + d3[2] * d3[2];
+                        qj[h] = j;
+                        qd[h][0] = d3[0];
+                        qd[h][1] = d3[1];
+                        qd[h][2] = d3[2];
+                        qr2[h] = r2;
+                        h += (r2 < cut2k[z.ty[size_t(j)]]) ? 1 : 0;
+                    }
+                    for (int u = 0; u < h; ++u) {
+                        const int64_t j = qj[u];
+                        const R r2 = qr2[u];
+                        const bool inside = j >= beg && j < end;
+                        const int tj = z.ty[size_t(j)];
+                        if ((tk | tj) == 0) {  // lipid-lipid (src/compute_pairwise_fused.h:109,134)
+                            if (r2 > R(1e-5))
+                                aniso<R>(qd[u], r2, nk, &z.nr[size_t(3 * j)], llcut, llrep, llatt, llalpha, fk, tq,
+                                         nullptr, inside ? &z.f[size_t(3 * j)] : nullptr,
+                                         inside ? &z.t[size_t(3 * j)] : nullptr, nullptr);
+                        } else {
+                            pair_force<R>(tk, tj, qd[u], r2, nk, &z.nr[size_t(3 * j)], fk, tq, nullptr,
+                                          inside ? &z.f[size_t(3 * j)] : nullptr,
+                                          inside ? &z.t[size_t(3 * j)] : nullptr, nullptr);
+                        }
+                    }
+                }
+                for (int d = 0; d < 3; ++d) {  // partners earlier in the range added theirs already
+                    z.f[size_t(3 * k + d)] += fk[d];
+                    z.t[size_t(3 * k + d)] += tq[d];
+                }
+            }
+        }
+        // bonds (src/compute_bonded.h:89-146)
+        for (int64_t l = 0; l < s->nb; ++l) {
+            const int type = s->bonds[3 * l];
+            const int i1 = tm[s->bonds[3 * l + 1]], i2 = tm[s->bonds[3 * l + 2]];
+            if (i1 < 0 || i2 < 0 || type < 0 || type >= ORC_MAX_BOND_TYPES) continue;
+            const int p1 = z.slot_of[size_t(i1)], p2 = z.slot_of[size_t(i2)];
+            R d3[3];
+            for (int d = 0; d < 3; ++d) d3[d] = z.dxw(z.x[size_t(3 * p2 + d)] - z.x[size_t(3 * p1 + d)], d);
+            const R rr = std::sqrt(d3[0] * d3[0] + d3[1] * d3[1] + d3[2] * d3[2]);
+            const R r0 = s->bond_r0 ? R(s->bond_r0[l]) : R(s->br0[type]);
+            const R kap = bond_kappa<R>(s->bstyle[type], R(s->bK[type]), r0, R(s->bR[type]), rr, nullptr, &flags);
+            for (int d = 0; d < 3; ++d) {
+                z.f[size_t(3 * p1 + d)] += kap * d3[d];
+                z.f[size_t(3 * p2 + d)] -= kap * d3[d];
+            }
+        }
+        // area / volume constraint (FP64, as in forces_impl)
+        if (s->nface > 0 && (s->kv != 0 || s->ka != 0)) {
+            const int ref = z.slot_of[size_t(tm[s->faces[0]])];
+            auto rel = [&](int p, double *out) {
+                for (int d = 0; d < 3; ++d)
+                    out[d] = min_image(double(z.x[size_t(3 * p + d)]) - double(z.x[size_t(3 * ref + d)]), z.b.L[d],
+                                       z.b.per[d]);
+            };
+            auto slot = [&](int64_t k, int c) { return z.slot_of[size_t(tm[s->faces[3 * k + c]])]; };
+            double area = 0, volume = 0;
+            for (int64_t k = 0; k < s->nface; ++k) {
+                double A[3], B[3], C[3], e1[3], e2[3], N[3], bc[3];
+                rel(slot(k, 0), A);
+                rel(slot(k, 1), B);
+                rel(slot(k, 2), C);
+                for (int d = 0; d < 3; ++d) {
+                    e1[d] = B[d] - A[d];
+                    e2[d] = C[d] - A[d];
+                }
+                cross3(e1, e2, N);
+                cross3(B, C, bc);
+                area += 0.5 * std::sqrt(dot3(N, N));
+                volume += dot3(A, bc) / 6.0;
+            }
+            const double cv = (s->kv != 0 && s->V0 != 0) ? -s->kv * (volume - s->V0) / s->V0 : 0.0;
+            const double ca = (s->ka != 0 && s->A0 != 0) ? -s->ka * (area - s->A0) / s->A0 : 0.0;
+            for (int64_t k = 0; k < s->nface; ++k) {
+                const int p[3] = {slot(k, 0), slot(k, 1), slot(k, 2)};
+                double P[3][3];
+                for (int q = 0; q < 3; ++q) rel(p[q], P[q]);
+                double e1[3], e2[3], N[3];
+                for (int d = 0; d < 3; ++d) {
+                    e1[d] = P[1][d] - P[0][d];
+                    e2[d] = P[2][d] - P[0][d];
+                }
+                cross3(e1, e2, N);
+                const double nn = std::sqrt(dot3(N, N));
+                const double nh[3] = {N[0] / nn, N[1] / nn, N[2] / nn};
+                for (int q = 0; q < 3; ++q) {
+                    const double *a = P[q], *bb = P[(q + 1) % 3], *cc = P[(q + 2) % 3];
+                    double ba[3], ca_[3], gV[3], bmc[3], gA[3];
+                    for (int d = 0; d < 3; ++d) {
+                        ba[d] = bb[d] - a[d];
+                        ca_[d] = cc[d] - a[d];
+                        bmc[d] = bb[d] - cc[d];
+                    }
+                    cross3(ba, ca_, gV);
+                    cross3(bmc, nh, gA);
+                    for (int d = 0; d < 3; ++d) z.f[size_t(3 * p[q] + d)] += R(cv * gV[d] / 6.0 + ca * gA[d] * 0.5);
+                }
+            }
+        }
+        // src/integrate_langevin.h:105-146
+        const int64_t step = s->step;
+#pragma omp parallel for schedule(static) num_threads(z.T)
+        for (int64_t k = 0; k < n; ++k) {
+            R *xk = &z.x[size_t(3 * k)], *nn = &z.nr[size_t(3 * k)], *vk = &z.v[size_t(3 * k)],
+              *ok = &z.o[size_t(3 * k)], *fk = &z.f[size_t(3 * k)];
+            R tk[3], tmp[3];
+            cross3(nn, &z.t[size_t(3 * k)], tk);
+            for (int d = 0; d < 3; ++d) ok[d] += dt * tk[d];
+            cross3(ok, nn, tmp);
+            R g[3];
+            for (int d = 0; d < 3; ++d) g[d] = nn[d] + tmp[d] * dt;
+            const R ginv = R(1) / std::sqrt(dot3(g, g));
+            for (int d = 0; d < 3; ++d) nn[d] = g[d] * ginv;
+            double rr[3];
+            noise3(s->seed, step, z.tg[size_t(k)], s->sys, rr);
+            const int ty = z.ty[size_t(k)];
+            for (int d = 0; d < 3; ++d) {
+                const R fd = fk[d] - (gamma[ty] * vk[d] + sigma[ty] * R(rr[d]));
+                vk[d] += fd * (dt / F.mass[ty]);
+                xk[d] += vk[d] * dt;
+            }
+        }
+        s->step++;
+    }
+#pragma omp parallel for schedule(static) num_threads(z.T)
+    for (int64_t k = 0; k < n; ++k) {
+        const int64_t i = z.src[size_t(k)];
+        for (int d = 0; d < 3; ++d) {
+            s->x[3 * i + d] = double(z.x[size_t(3 * k + d)]);
+            s->nrm[3 * i + d] = double(z.nr[size_t(3 * k + d)]);
+            s->v[3 * i + d] = double(z.v[size_t(3 * k + d)]);
+            s->o[3 * i + d] = double(z.o[size_t(3 * k + d)]);
+        }
+    }
+    if (th) {
+        th->ke2 = chunked_sum(n, [&](int64_t i) {
+            const double *vv = &s->v[3 * i];
+            return double(F.mass[s->type[i]]) * (vv[0] * vv[0] + vv[1] * vv[1] + vv[2] * vv[2]);
+        });
+        th->temperature = n ? th->ke2 / (3.0 * double(n)) : 0;
+        th->flags = flags;
+        th->npairs = z.builds;
+    }
+    return 0;
+}
+
 }  // namespace
 
 extern "C" {
@@ -860,6 +1331,10 @@ int orc_forces_f32(const orc_system *s, double *f3, double *t3, double *e, orc_t
 }
 int orc_step_langevin_f64(orc_system *s, int nsteps, orc_thermo *th) { return langevin_impl<double>(s, nsteps, th); }
 int orc_step_langevin_f32(orc_system *s, int nsteps, orc_thermo *th) { return langevin_impl<float>(s, nsteps, th); }
+int orc_run_langevin_fast_f32(orc_system *s, int nsteps, double skin, orc_thermo *th) {
+    if (!(skin >= 0)) return 1;
+    return fast_langevin_f32(s, nsteps, skin, th);
+}
 
 int orc_nh_prologue_f64(orc_system *s, orc_thermo *th) {
     forces_impl<double>(s, s->f, s->t, nullptr, th);

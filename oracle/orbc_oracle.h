@@ -86,6 +86,12 @@ int orc_forces_f32(const orc_system *s, double *f3, double *t3, double *e, orc_t
  * update.  Runs nsteps; s->step advances. */
 int orc_step_langevin_f64(orc_system *s, int nsteps, orc_thermo *th);
 int orc_step_langevin_f32(orc_system *s, int nsteps, orc_thermo *th);
+/* The timed CPU baseline: nsteps of the same FP32 Langevin step organised as
+ * the reference's production loop runs (particles sorted by cell, a Verlet
+ * list with the given skin rebuilt when a particle moved more than skin/2,
+ * Newton's third law inside each thread's range; see orbc_oracle.cpp).
+ * th->npairs receives the number of list builds. */
+int orc_run_langevin_fast_f32(orc_system *s, int nsteps, double skin, orc_thermo *th);
 
 /* Nose-Hoover: prologue = forces + post_toque_final_update
  * (src/openrbc.cpp:162-185, src/integrate_nh.h:237-273); step =

@@ -229,6 +229,66 @@ void ref_morton_encode(int64_t n, const double *p3, uint32_t *keys) {
         keys[i] = morton_encode(real(p3[3 * i]), real(p3[3 * i + 1]), real(p3[3 * i + 2]), p);
 }
 
+/* Wall-clock seconds of the reference's own production loop on the given
+ * state: the Voronoi initialisation of src/openrbc.cpp:71-76 (*secs_init),
+ * then the main loop of src/openrbc.cpp:153-256 in the default build
+ * (FUSED_PAIRWISE + LANGEVIN: Voronoi and cell-list updates every
+ * freq_voronoi steps, compute_pairwise_fused, compute_bonded,
+ * integrate(verlet_langevin)) for nsteps steps on `threads` OpenMP threads
+ * (*secs_loop), without I/O and without the stray-lipid cleanup.  For timing
+ * only: the state is not returned. */
+int ref_time_production(int64_t n, const double *x, const double *nrm, const double *v, const double *o,
+                        const int *type, const int *tag, int64_t nb, const int *bonds, double dt, double kBT,
+                        double eta, int nsteps, int threads, double *secs_init, double *secs_loop) {
+    omp_set_num_threads(threads);
+    RTParameter &p = params();
+    if (int(p.prng.size()) < threads) {  // one generator per thread (src/runtime_parameter.h:110-111)
+        p.prng.resize(size_t(threads));
+        for (auto &r : p.prng) r.init(p.rng.uint());
+    }
+    p.dt = dt;
+    p.kBT = real(kBT);
+    p.eta = real(eta);
+    p.nstep = 0;
+    p.freq_cleanup = 1 << 30;
+    State s;
+    s.load(n, x, nrm, v, o, type, tag, nb, bonds);
+    const double t0 = omp_get_wtime();
+    VoronoiDiagram voronoi(std::max<std::size_t>(1, s.lipid.size() / p.voronoi_cell_size));
+    VCellList cell_lipid, cell_protein;
+    {
+        Quiet q;
+        voronoi.init(s.lipid, cell_lipid, p, 64);
+    }
+    cell_lipid.update_particle_affiliation(s.lipid);
+    cell_protein.update(s.protein, voronoi, p);
+    cell_protein.update_particle_affiliation(s.protein);
+    const double t1 = omp_get_wtime();
+    voronoi.update(s.lipid, cell_lipid, p);
+    cell_lipid.update(s.lipid, voronoi, p);
+    cell_protein.update(s.protein, voronoi, p);
+    integrate(clear_force(), s.lipid, s.protein);
+    compute_pairwise_fused(voronoi, s.lipid, s.protein, cell_lipid, cell_protein);
+    compute_bonded(s.protein);
+    integrate(verlet_langevin(p), s.lipid, s.protein);
+    p.nstep = 0;
+    for (int k = 0; k < nsteps; ++k) {
+        if (p.nstep % p.freq_voronoi == 0) {
+            voronoi.update(s.lipid, cell_lipid, p);
+            cell_lipid.update(s.lipid, voronoi, p);
+            cell_protein.update(s.protein, voronoi, p);
+        }
+        compute_pairwise_fused(voronoi, s.lipid, s.protein, cell_lipid, cell_protein);
+        compute_bonded(s.protein);
+        integrate(verlet_langevin(p), s.lipid, s.protein);
+        ++p.nstep;
+    }
+    const double t2 = omp_get_wtime();
+    *secs_init = t1 - t0;
+    *secs_loop = t2 - t1;
+    return 0;
+}
+
 /* init_rbc (src/init_rbc.h:29-337) on a mesh prefix; returns the particle
  * count (proteins first, then lipids) or -1 when cap is too small.  Bonds are
  * written to bonds3 (at most bcap).  Positions are the reference's (real). */

@@ -123,7 +123,7 @@ def ref_temperature(prec, x, nrm, v, ty, tg):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref-src", default=orc.DEFAULT_REF_SRC)
+    ap.add_argument("--ref-src", default="/root/reference/src", help="the reference's src/ directory")
     args = ap.parse_args()
     orc.build(args.ref_src)
     assert orc.ref_available("f64") and orc.ref_available("f32"), "reference harness did not build"

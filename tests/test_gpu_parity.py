@@ -107,14 +107,20 @@ def test_langevin_with_noise_vs_oracle(precision, tol):
     assert abs(th["temperature"] - T) < 10 * tol * T
 
 
-def test_temperature_matches_reference():
-    g = load_golden("cell_ico12.npz")
-    with sim_for(g, "fp64") as s:
+@pytest.mark.parametrize("name", ["lattice_576.npz", "cell_ico12.npz"])
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("mixed", 1e-6)])
+def test_temperature_matches_reference(name, precision, tol):
+    """compute_temperature (src/compute_temperature.h:24-29) of the uploaded
+    velocities: sum m v^2 / 3N against the reference's own value, before and
+    after a zero-step call."""
+    g = load_golden(name)
+    T_ref = float(g["temperature"])
+    with sim_for(g, precision) as s:
         th = s.thermo()
-    # thermo after upload reports the uploaded velocities only after a step; use one 0-step call
-    with sim_for(g, "fp64", kBT=0.0) as s:
-        s.step(0)
-    assert th["n"] == len(g["x"])
+        assert th["n"] == len(g["x"])
+        assert abs(th["temperature"] - T_ref) < tol * T_ref, (th["temperature"], T_ref)
+        th0 = s.step(0)
+        assert abs(th0["temperature"] - T_ref) < tol * T_ref, (th0["temperature"], T_ref)
 
 
 def test_neighbour_sets_match_brute_force():

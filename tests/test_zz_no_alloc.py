@@ -10,13 +10,16 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def _sort_on_device(L, points, bsize):
+def _sort_on_device(L, points, bsize, stream=None):
     import torch
     n = len(points)
     dp = torch.from_numpy(np.ascontiguousarray(points)).to("cuda")
     dout = torch.full((n,), -1, dtype=torch.int32, device="cuda")
     torch.cuda.synchronize()
-    rc = L.orbc_gpu_morton_order_noalloc(dp.data_ptr(), n, bsize.ctypes.data, dout.data_ptr(), None)
+    rc = L.orbc_gpu_morton_order_noalloc(dp.data_ptr(), n, bsize.ctypes.data, dout.data_ptr(),
+                                         stream.cuda_stream if stream is not None else None)
+    if stream is not None:
+        stream.synchronize()
     torch.cuda.synchronize()
     return rc, dout.cpu().numpy()
 
@@ -36,9 +39,26 @@ def test_noalloc_order_matches_allocating_entry_point_twice():
         assert np.array_equal(got, morton_order(p, bsize))
 
 
+def test_noalloc_on_a_caller_stream():
+    """Work queued on the caller's own (non-default) stream."""
+    import torch
+    from openrbc_gb300 import _native as N
+    from openrbc_gb300 import morton_order
+    L = N.lib()
+    bsize = np.array([2000.0, 2000.0, 2000.0])
+    rng = np.random.default_rng(7)
+    s = torch.cuda.Stream()
+    for n in (40_000, 70_001):
+        p = rng.uniform(-1000.0, 1000.0, (n, 3))
+        rc, got = _sort_on_device(L, p, bsize, stream=s)
+        assert rc == 0
+        assert np.array_equal(got, morton_order(p, bsize))
+
+
 def test_noalloc_rejects_sizes_beyond_its_scratch():
     from openrbc_gb300 import _native as N
     L = N.lib()
     bsize = np.array([2000.0, 2000.0, 2000.0])
     assert L.orbc_gpu_morton_order_noalloc(None, N.NOALLOC_MAX_POINTS + 1, bsize.ctypes.data, None, None) == 1
+    assert b"ORBC_NOALLOC_MAX_POINTS" in L.orbc_gpu_error(None)
     assert L.orbc_gpu_morton_order_noalloc(None, 0, bsize.ctypes.data, None, None) == 0
