@@ -281,7 +281,8 @@ def main():
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default skin / kernel form")
     ap.add_argument("--skin", type=float, default=None, help="neighbour skin when not autotuning")
-    ap.add_argument("--form", type=int, default=0, help="kernel form 0..23 (orbc_params.kernel_variant) when not autotuning")
+    ap.add_argument("--form", type=int, default=0, help="kernel form 0..127 (orbc_params.kernel_variant)")
+    ap.add_argument("--rebuild-every", type=int, default=0, help="fixed rebuild cadence when not autotuning")
     args = ap.parse_args()
     rank, ws = dist_setup()
     if args.impl == "reference":
@@ -298,7 +299,8 @@ def main():
         f"({time.perf_counter() - t_gen:.1f} s)")
 
     # ---- mixed precision, device-resident
-    sim = make_sim(w, "mixed", skin=args.skin if args.skin is not None else SKIN, kernel_variant=args.form)
+    sim = make_sim(w, "mixed", skin=args.skin if args.skin is not None else SKIN, kernel_variant=args.form,
+                   rebuild_every=args.rebuild_every)
     f_mixed, _, _ = sim.forces()
     tune = None
     if not args.no_autotune:
@@ -306,7 +308,8 @@ def main():
         trials = sim.autotune(trial_steps=20)
         best = min(trials, key=lambda r: r["ms_per_step"])
         tune = {"chosen": best, "trials": trials, "seconds": time.perf_counter() - t_tune}
-        log(f"autotune: skin {best['skin']}, form {best['variant']}, {best['ms_per_step']:.4f} ms/step "
+        log(f"autotune: skin {best['skin']}, form {best['variant']}, rebuild every {best['rebuild_every']}, "
+            f"{best['ms_per_step']:.4f} ms/step "
             f"({len(trials)} trials, {tune['seconds']:.1f} s)")
     sim.step(args.warmup)
     barrier(ws)
@@ -328,8 +331,9 @@ def main():
     ferr = None
     if not args.skip_fp64 and args.fp64_steps > 0:
         # the mixed run's force-loop and list-build forms and skin; the
-        # occupancy form (bit 2) is sized for FP32 registers and left out
-        form = (tune["chosen"]["variant"] if tune else args.form) & ~4
+        # occupancy form (bit 2) is sized for FP32 registers and compensated
+        # accumulation (bit 6) is an FP32 remedy: both are left out
+        form = (tune["chosen"]["variant"] if tune else args.form) & ~(4 | 64)
         skin = tune["chosen"]["skin"] if tune else (args.skin if args.skin is not None else SKIN)
         sim64 = make_sim(w, "fp64", skin=skin, kernel_variant=form)
         f64, _, _ = sim64.forces()
@@ -398,7 +402,8 @@ def main():
                          "area / volume / kinetic-energy sums)",
             "config": bench_config(w, args.n_lipid),
             "tuning": {"skin": tune["chosen"]["skin"] if tune else (args.skin if args.skin is not None else SKIN),
-                       "kernel_form": tune["chosen"]["variant"] if tune else args.form},
+                       "kernel_form": tune["chosen"]["variant"] if tune else args.form,
+                       "rebuild_every": tune["chosen"]["rebuild_every"] if tune else args.rebuild_every},
             "fp64": fp64, "mixed_over_fp64": (value / ws / fp64["value"]) if fp64 else None,
             "force_rel_err_mixed_vs_fp64": ferr, "rebuilds_in_timed_region": th["rebuilds"] - th0["rebuilds"],
             "roofline": roof, "e2e": e2e, "gpu_launches": launches, "clocks": clk.summary(), "profile": prof,

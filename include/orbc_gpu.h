@@ -84,15 +84,20 @@ typedef struct {
     double bond_K[ORBC_MAX_BOND_TYPES];
     double bond_r0[ORBC_MAX_BOND_TYPES];
     double bond_R[ORBC_MAX_BOND_TYPES];
-    /* kernel forms 0..23: bit 0 = software-pipelined neighbour pass
-       (else 2-way unrolled), bit 1 = non-lipid pair path inlined (else
-       called), bit 2 = Langevin step kernel compiled for 20 resident blocks
-       per SM (48 registers; else 16 blocks, 64 registers), bits 3-4 = how
-       the neighbour list is built: 0 per cell of a warp, 32 candidates at a
-       time, entries placed by prefix count; 1 per-particle 27-cell sweeps;
-       2 per warp in two phases (accept masks per particle, then every lane
-       writes its own column).  All forms write the same list.
-       orbc_gpu_autotune picks the forms per workload */
+    /* kernel forms 0..127 (bits 3 and 4 not both set): bit 0 =
+       software-pipelined neighbour pass (else 2-way unrolled), bit 1 =
+       non-lipid pair path inlined (else called), bit 2 = Langevin step kernel
+       compiled for 20 resident blocks per SM (48 registers; else 16 blocks,
+       64 registers), bits 3-4 = how the neighbour list is built: 0 per cell
+       of a warp, 32 candidates at a time, entries placed by prefix count;
+       1 per-particle 27-cell sweeps; 2 per warp in two phases (accept masks
+       per particle, then every lane writes its own column) -- all three
+       write the same list; bit 5 (32) = merged shell pass: skin-shell rows
+       are distance-tested first and their hits evaluated in the loop of the
+       inner rows (bit-identical results); bit 6 (64) = compensated (Kahan)
+       summation of each particle's force and torque, also in the forces
+       hook.  Bits 5 and 6 imply bits 0 and 1.  orbc_gpu_autotune picks the
+       forms per workload */
     int kernel_variant;
     /* 1: remove each system's mean lipid velocity between the force
        evaluation and the integrator every step, as the disabled call
@@ -169,7 +174,20 @@ int orbc_gpu_set_state_f32(orbc_handle *h, int64_t first, int64_t count, int str
                            const float *v, const float *o);
 
 /* nsteps of the loop body of src/openrbc.cpp:189-242 (pair forces, bonds,
- * constraint, integrator; neighbour rebuild on demand).  out may be NULL. */
+ * constraint, integrator; neighbour rebuild on demand).  out may be NULL.
+ *
+ * A neighbour list that outgrows its capacity at a rebuild inside the call is
+ * not an error: the device stops stepping at that build (no step runs on a
+ * truncated list), the library grows the list, rebuilds it from the current
+ * state and runs the remaining steps (for Nose-Hoover, it first finishes the
+ * interrupted step's second half), so the call still completes nsteps steps.
+ * ORBC_ERR_GRID: a particle of a system with open axes left that system's
+ * grid (set at upload: the particles' extent plus a margin of at least a
+ * quarter of it and five list cutoffs on each side); it was kept in the edge
+ * cell, where pairs beyond that cell's neighbours are missed, so the state is
+ * no longer trustworthy.  Like ORBC_ERR_NAN and ORBC_ERR_BOND, the condition
+ * stays recorded (every later step, minimize and forces call returns it, and
+ * orbc_thermo.flags shows it) until the next orbc_gpu_upload. */
 int orbc_gpu_step(orbc_handle *h, int nsteps, orbc_thermo *out);
 
 /* Current state in upload order (any pointer may be NULL). */
@@ -313,17 +331,22 @@ typedef struct {
 } orbc_profile;
 int orbc_gpu_profile(orbc_handle *h, int nsteps, orbc_profile *out);
 
-/* Autotuner: times trial_steps graph-captured steps for each candidate
- * neighbour-list skin (0.3, 0.45, 0.6, 0.8, 1.0) and force-kernel form (0..3)
- * from a snapshot of the current state, keeps the fastest, and restores the
- * snapshot (state, step counter, thermostat), so the simulation does not
- * advance.  trials (may be NULL) receives up to max_trials rows.  No
- * reference counterpart (the reference's cadences are fixed command-line
- * values, src/runtime_parameter.h:57-60). */
+/* Autotuner: times trial_steps graph-captured steps per candidate from a
+ * snapshot of the current state, keeps the fastest, and restores the snapshot
+ * (state, step counter, thermostat), so the simulation does not advance.
+ * Dimensions, in order: neighbour-list skin (0.3, 0.45, 0.6, 0.8, 1.0) x
+ * force-loop form (kernel_variant bits 0-1, and the merged shell pass, bit 5);
+ * the two skins half-way to the best one's neighbours; the occupancy form
+ * (bit 2); the other two list-build forms (bits 3-4); and the rebuild cadence
+ * (rebuild_every 0 = only when a particle moved more than skin/2, else also
+ * every 5 or 10 steps).  Compensated accumulation (bit 6) is an accuracy
+ * choice and is kept as the caller set it.  trials (may be NULL) receives up
+ * to max_trials rows.  No reference counterpart (the reference's cadences are
+ * fixed command-line values, src/runtime_parameter.h:57-60). */
 typedef struct {
     double skin;
-    int variant;
-    int pad;
+    int variant;        /* kernel_variant of the trial */
+    int rebuild_every;  /* rebuild cadence of the trial */
     double ms_per_step;
     double rebuilds_per_step;
 } orbc_tune_trial;

@@ -85,7 +85,7 @@ class Profile(C.Structure):
 
 
 class TuneTrial(C.Structure):
-    _fields_ = [("skin", C.c_double), ("variant", C.c_int), ("pad", C.c_int), ("ms_per_step", C.c_double),
+    _fields_ = [("skin", C.c_double), ("variant", C.c_int), ("rebuild_every", C.c_int), ("ms_per_step", C.c_double),
                 ("rebuilds_per_step", C.c_double)]
 
 

@@ -156,10 +156,20 @@ struct SysState {
 
 struct Scalars {
     int cur, lp, rebuild, error;
-    int max_nnb, out_of_grid, cond_hint, pad0;
-    unsigned int blk_counter, mesh_counter, pad2, pad3;
+    int max_nnb, out_of_grid, cond_hint;
+    int nh_half;          // 1 between a Nose-Hoover first half and its second half
+    unsigned int blk_counter, mesh_counter;
+    unsigned int iters;   // completed steps or minimisation iterations (k_advance, k_reduce)
+    unsigned int pad3;
     long long step, rebuilds, since_rebuild, pad4;
 };
+
+/* A neighbour list overflowed its capacity at the last build: the step
+ * kernels then leave the state untouched (and the step counters unchanged)
+ * until the host has grown the list and rebuilt it, so that no step is
+ * computed on a truncated list.  The flag is written only by the list build,
+ * so every thread of a step kernel reads the same value. */
+__device__ __forceinline__ bool halted(const Scalars *S) { return (__ldcg(&S->error) & ERRB_NBR_OVERFLOW) != 0; }
 
 template<class R> struct KArgs {
     using T4 = typename Vec<R>::T4;

@@ -722,13 +722,26 @@ template<class R> class Engine : public EngineBase {
         if (!uploaded) return fail(ORBC_ERR_STATE, "minimize before upload");
         if (nsteps < 0 || !(dr_opt > 0) || !(dn_opt > 0))
             return fail(ORBC_ERR_ARG, "minimize: need nsteps >= 0 and positive move limits");
-        for (int k = 0; k < nsteps; ++k) {
-            launch_rebuild<R>(a, st, true);
-            if (has_mesh) launch_mesh<R>(a, st);
-            launch_minimize<R>(a, dr_opt, dn_opt, st);
+        for (int attempt = 0;; ++attempt) {
+            Scalars before;
+            CK(cudaMemcpy(&before, Sd.p, sizeof(Scalars), cudaMemcpyDeviceToHost));
+            for (int k = 0; k < nsteps; ++k) {
+                launch_rebuild<R>(a, st, true);
+                if (has_mesh) launch_mesh<R>(a, st);
+                launch_minimize<R>(a, dr_opt, dn_opt, st);
+            }
+            CK(cudaGetLastError());
+            CK(cudaStreamSynchronize(st));
+            Scalars hs;
+            CK(cudaMemcpy(&hs, Sd.p, sizeof(Scalars), cudaMemcpyDeviceToHost));
+            if (!(hs.error & ERRB_NBR_OVERFLOW)) break;
+            // a list overflowed: the iterations after it did nothing; grow the
+            // list, rebuild it from the current state and run the rest
+            if (attempt == 4) return fail(ORBC_ERR_NBR_OVERFLOW, "minimize: neighbour capacity could not be sized");
+            const int rc = recover_overflow(hs);
+            if (rc) return rc;
+            nsteps -= int(hs.iters - before.iters);
         }
-        CK(cudaGetLastError());
-        CK(cudaStreamSynchronize(st));
         nh_primed = false;   // forces of the new configuration are not carried
         vcom_valid = false;  // walls may have reversed velocities
         Scalars hs;
@@ -737,13 +750,25 @@ template<class R> class Engine : public EngineBase {
             int rc = thermo(-1, out);
             if (rc) return rc;
         }
-        if (hs.max_nnb > cap * 0.85 || (hs.error & ERRB_NBR_OVERFLOW)) {
+        if (hs.max_nnb > cap * 0.85) {
             int rc = grow_capacity(hs.max_nnb);
             if (rc) return rc;
         }
-        const int code = err_code_of(hs.error & ~ERRB_GRID);
+        const int code = err_code_of(hs.error);
         if (code) return fail(code, "minimize: device reported error bits " + std::to_string(hs.error));
         return ORBC_OK;
+    }
+
+    /* After a list overflow (the build truncated some lists and the step
+     * kernels that followed left the state untouched): grow the capacity to
+     * the need the build reported, clear the flag and rebuild from the
+     * current state. */
+    int recover_overflow(const Scalars &hs) {
+        int rc = grow_capacity(hs.max_nnb, false);
+        if (rc) return rc;
+        const int clr = hs.error & ~ERRB_NBR_OVERFLOW;
+        CK(cudaMemcpy(&Sd.p->error, &clr, sizeof(int), cudaMemcpyHostToDevice));
+        return build_lists(false);
     }
 
     /* Frame order (src/trajectory.h:75-77): lipids, then proteins, each in
@@ -1155,15 +1180,40 @@ template<class R> class Engine : public EngineBase {
             int rc = thermo(-1, out);
             if (rc) return rc;
         }
+        if (hs.error & ERRB_NBR_OVERFLOW) {
+            /* A list build inside the call overflowed: the steps after it left
+             * the state untouched.  Grow the list, rebuild it from the current
+             * state, finish the interrupted Nose-Hoover step if its first half
+             * ran, and run the steps that remain. */
+            if (overflow_depth >= 4) return fail(ORBC_ERR_NBR_OVERFLOW, "step: neighbour capacity could not be sized");
+            int rc = recover_overflow(hs);
+            if (rc) return rc;
+            int remaining = nsteps - int(hs.iters - before.iters);
+            if (P.integrator == ORBC_INT_NOSE_HOOVER) {
+                if (hs.nh_half) {  // the second half of the interrupted step
+                    if (has_mesh) launch_mesh<R>(a, st);
+                    launch_nh_final<R>(a, st, P.energy != 0);
+                    CK(cudaGetLastError());
+                    --remaining;
+                } else {
+                    nh_primed = false;  // the overflow hit the prologue's build: prime again
+                }
+            }
+            ++overflow_depth;
+            rc = step(std::max(remaining, 0), out);
+            --overflow_depth;
+            return rc;
+        }
         // keep headroom in the neighbour capacity
-        if (hs.max_nnb > cap * 0.85 || (hs.error & ERRB_NBR_OVERFLOW)) {
+        if (hs.max_nnb > cap * 0.85) {
             int rc = grow_capacity(hs.max_nnb);
             if (rc) return rc;
         }
-        const int code = err_code_of(hs.error & ~ERRB_GRID);
+        const int code = err_code_of(hs.error);
         if (code) return fail(code, "step: device reported error bits " + std::to_string(hs.error));
         return ORBC_OK;
     }
+    int overflow_depth = 0;
 
     int download(double *x3, double *n3, double *v3, double *o3) override {
         if (!uploaded) return fail(ORBC_ERR_STATE, "download before upload");
@@ -1202,10 +1252,20 @@ template<class R> class Engine : public EngineBase {
 
     int forces(double *f3, double *t3, double *e) override {
         if (!uploaded) return fail(ORBC_ERR_STATE, "forces before upload");
-        launch_rebuild<R>(a, st, true);
-        if (has_mesh) launch_mesh<R>(a, st);
-        launch_forces<R>(a, st);
-        CK(cudaGetLastError());
+        Scalars hs;
+        for (int attempt = 0;; ++attempt) {
+            launch_rebuild<R>(a, st, true);
+            if (has_mesh) launch_mesh<R>(a, st);
+            launch_forces<R>(a, st);
+            CK(cudaGetLastError());
+            CK(cudaMemcpyAsync(&hsc[0], Sd.p, sizeof(Scalars), cudaMemcpyDeviceToHost, st));
+            CK(cudaStreamSynchronize(st));
+            hs = hsc[0];
+            if (!(hs.error & ERRB_NBR_OVERFLOW)) break;
+            if (attempt == 4) return fail(ORBC_ERR_NBR_OVERFLOW, "forces: neighbour capacity could not be sized");
+            const int rc = recover_overflow(hs);  // the forces kernel did nothing: grow, rebuild, again
+            if (rc) return rc;
+        }
         double *d = stage.p;
         const size_t m = size_t(nhome) * 3;
         launch_download<R>(a, 0, nhome, nullptr, nullptr, nullptr, nullptr, d, d + m, d + 2 * m, st);
@@ -1216,9 +1276,7 @@ template<class R> class Engine : public EngineBase {
         CK(cudaStreamSynchronize(st));
         // the forces kernel overwrote the carried Nose-Hoover forces
         nh_primed = false;
-        Scalars hs;
-        CK(cudaMemcpy(&hs, Sd.p, sizeof(Scalars), cudaMemcpyDeviceToHost));
-        const int code = err_code_of(hs.error & ~ERRB_GRID);
+        const int code = err_code_of(hs.error);
         if (code) return fail(code, "forces: device reported error bits " + std::to_string(hs.error));
         return ORBC_OK;
     }
@@ -1477,10 +1535,12 @@ template<class R> class Engine : public EngineBase {
         for (size_t k = 0; k < hss.size(); ++k) topo.descs[k].zeta = hss[k].zeta;
         const double skins[] = {0.3, 0.45, 0.6, 0.8, 1.0};
         double best_ms = 1e300, best_skin = P.skin;
-        int best_var = P.kernel_variant, nt = 0;
-        auto trial = [&](double sk, int var) -> int {
+        int best_var = P.kernel_variant, best_every = P.rebuild_every, nt = 0;
+        const int keep = P.kernel_variant & 64;  // compensated accumulation: the caller's accuracy choice
+        auto trial = [&](double sk, int var, int every) -> int {
             P.skin = sk;
-            P.kernel_variant = var;
+            P.kernel_variant = var | keep;
+            P.rebuild_every = every;
             int r = relayout(x, nv, v, o, hs.step);
             if (r) return r;
             r = step(3, nullptr);  // warm: builds the graph
@@ -1494,7 +1554,8 @@ template<class R> class Engine : public EngineBase {
             const double ms = last_ms / trial_steps;
             if (trials && nt < max_trials) {
                 trials[nt].skin = sk;
-                trials[nt].variant = var;
+                trials[nt].variant = var | keep;
+                trials[nt].rebuild_every = every;
                 trials[nt].ms_per_step = ms;
                 trials[nt].rebuilds_per_step = double(af.rebuilds - b4.rebuilds) / trial_steps;
             }
@@ -1502,32 +1563,38 @@ template<class R> class Engine : public EngineBase {
             if (ms < best_ms) {
                 best_ms = ms;
                 best_skin = sk;
-                best_var = var;
+                best_var = var | keep;
+                best_every = every;
             }
             return ORBC_OK;
         };
-        // skin x force-kernel form (bits 0-1); the skins half-way to the best
-        // one's grid neighbours; then at the best pair the occupancy form
-        // (bit 2) and the other two list-build forms (bits 3-4)
-        const int rest = P.kernel_variant & 28;
+        // skin x force-loop form (bits 0-1, and the merged shell pass); the
+        // skins half-way to the best one's grid neighbours; then at the best
+        // pair the occupancy form (bit 2), the other two list-build forms
+        // (bits 3-4) and two fixed rebuild cadences
+        const int rest = P.kernel_variant & 28, every0 = P.rebuild_every;
+        const int loops[] = {0, 1, 2, 3, 3 | 32};
         for (double sk : skins)
-            for (int var = 0; var < 4; ++var)
-                if ((rc = trial(sk, var | rest))) return rc;
+            for (int lf : loops)
+                if ((rc = trial(sk, lf | rest, every0))) return rc;
         const int nsk = int(sizeof(skins) / sizeof(skins[0]));
         int bi = 0;
         while (bi + 1 < nsk && skins[bi] != best_skin) ++bi;
         const double lo_sk = 0.5 * (skins[bi > 0 ? bi - 1 : 0] + best_skin);
         const double hi_sk = 0.5 * (skins[bi + 1 < nsk ? bi + 1 : nsk - 1] + best_skin);
-        const int bv = best_var;
-        if ((rc = trial(lo_sk, bv))) return rc;
-        if ((rc = trial(hi_sk, bv))) return rc;
-        if ((rc = trial(best_skin, best_var ^ 4))) return rc;
+        const int bv = best_var & ~64;
+        if ((rc = trial(lo_sk, bv, every0))) return rc;
+        if ((rc = trial(hi_sk, bv, every0))) return rc;
+        if ((rc = trial(best_skin, (best_var & ~64) ^ 4, every0))) return rc;
         const int lf = (best_var >> 3) & 3;
         for (int f = 0; f < 3; ++f)
-            if (f != lf && (rc = trial(best_skin, (best_var & 7) | (f << 3)))) return rc;
+            if (f != lf && (rc = trial(best_skin, (best_var & (7 | 32)) | (f << 3), every0))) return rc;
+        for (int every : {5, 10})
+            if (every != every0 && (rc = trial(best_skin, best_var & ~64, every))) return rc;
         if (ntrials) *ntrials = nt;
         P.skin = best_skin;
         P.kernel_variant = best_var;
+        P.rebuild_every = best_every;
         return relayout(x, nv, v, o, hs.step);
     }
 
@@ -1681,7 +1748,7 @@ template<class R> class Engine : public EngineBase {
         a.skin_half2 = R(0.25 * P.skin * P.skin);
         a.seed = P.seed;
         a.rebuild_every = P.rebuild_every;
-        a.variant = P.kernel_variant & 7;
+        a.variant = P.kernel_variant & (7 | 32 | 64);
         a.nlist_lane = (P.kernel_variant >> 3) & 3;
         a.carry_forces = P.integrator == ORBC_INT_NOSE_HOOVER ? 1 : 0;
         a.zero_bulk = P.zero_bulk ? 1 : 0;
@@ -1724,11 +1791,9 @@ template<class R> class Engine : public EngineBase {
         cap = nc;
         a.nbr = nbr.p;
         a.cap = cap;
-        if (rebuild_now) {
+        if (rebuild_now) {  // the next step rebuilds into the larger list
             int one = 1;
             CK(cudaMemcpyAsync(&Sd.p->rebuild, &one, sizeof(int), cudaMemcpyHostToDevice, st));
-            int clr = 0;
-            CK(cudaMemcpyAsync(&Sd.p->error, &clr, sizeof(int), cudaMemcpyHostToDevice, st));
             CK(cudaStreamSynchronize(st));
         }
         return ORBC_OK;
@@ -1834,7 +1899,7 @@ int orbc_gpu_create(const orbc_params *p, orbc_handle **out) {
     *out = nullptr;
     if (!(p->dt > 0) || p->skin < 0 || (p->precision != ORBC_PREC_FP64 && p->precision != ORBC_PREC_MIXED) ||
         (p->integrator != ORBC_INT_LANGEVIN && p->integrator != ORBC_INT_NOSE_HOOVER) ||
-        (p->kernel_variant < 0 || p->kernel_variant > 23) || (p->zero_bulk != 0 && p->zero_bulk != 1)) {
+        (p->kernel_variant < 0 || p->kernel_variant > 127 || (p->kernel_variant & 24) == 24) || (p->zero_bulk != 0 && p->zero_bulk != 1)) {
         g_last_error = "create: invalid parameters";
         return ORBC_ERR_ARG;
     }

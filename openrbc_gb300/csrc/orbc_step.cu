@@ -255,8 +255,32 @@ template<class R> __device__ __forceinline__ void init_shift(const KArgs<R> &a, 
  * while spills would). */
 template<class R> constexpr int fp_blocks(int n) { return sizeof(R) == 4 ? n : n / 2; }
 
+/* Form bits of the force loop (orbc_params.kernel_variant; the autotuner
+ * picks one per workload):
+ *   1  software-pipelined list pass (the next entry's gathers in flight while
+ *      the current pair is evaluated) instead of a 2-way unrolled loop;
+ *   2  the rare non-lipid pair path inlined instead of called;
+ *   4  occupancy form of the lite Langevin kernel (more resident blocks);
+ *   32 merged shell pass: the skin-shell rows are only distance-tested, each
+ *      lane records its hits in a bit mask, and the hits are evaluated in the
+ *      same loop as the inner rows, so a shell row that one lane of a warp
+ *      hits no longer costs the whole warp a pair evaluation.  The pairs are
+ *      added in the same order as without it: the results are bit-identical;
+ *   64 compensated accumulation: each particle's force and torque are summed
+ *      with Kahan compensation (the rounding error of each running sum is
+ *      carried into the next addition), for the FP32 form. */
+constexpr int FORM_PIPE = 1, FORM_INLINE = 2, FORM_OCC = 4, FORM_MERGED = 32, FORM_KAHAN = 64;
+
+/* s += d with Kahan compensation c (one component). */
+template<class R> __device__ __forceinline__ void kahan_add(R &s, R &c, R d) {
+    const R y = d - c;
+    const R t = s + y;
+    c = (t - s) - y;
+    s = t;
+}
+
 /* All forces and torques on particle slot i: pair terms over its neighbour
- * list (variant V, see launch_step_langevin), bonds, mesh constraint. */
+ * list (form V, above), bonds, mesh constraint. */
 template<class R, bool E, int V>
 __device__ __forceinline__ void particle_forces(const KArgs<R> &a, const FFDev<R> &F, int i, int cur, int lp, int w,
                                                 const typename Vec<R>::T4 &pi, const typename Vec<R>::T4 &ni,
@@ -264,6 +288,7 @@ __device__ __forceinline__ void particle_forces(const KArgs<R> &a, const FFDev<R
                                                 const typename Vec<R>::T4 *sh, R3<R> &f, R3<R> &t, R &e,
                                                 int &flags) {
     using T4 = typename Vec<R>::T4;
+    constexpr bool KAHAN = (V & FORM_KAHAN) != 0;
     const int ty = w_type(w);
     const T4 *__restrict__ pos = a.pos[cur];
     const T4 *__restrict__ nrm = a.nrm[cur];
@@ -273,6 +298,15 @@ __device__ __forceinline__ void particle_forces(const KArgs<R> &a, const FFDev<R
     const uint32_t *__restrict__ shell = nb + int64_t(a.cap - 1) * 32;  // shell rows run downwards
     const int64_t stride = 32;
     const R ll_cutsq = a.ll.cutsq;
+    R3<R> cf = {0, 0, 0}, ct = {0, 0, 0};  // Kahan compensations (KAHAN only)
+    auto accumulate = [&](const R3<R> &df, const R3<R> &dt) {
+        kahan_add(f.x, cf.x, df.x);
+        kahan_add(f.y, cf.y, df.y);
+        kahan_add(f.z, cf.z, df.z);
+        kahan_add(t.x, ct.x, dt.x);
+        kahan_add(t.y, ct.y, dt.y);
+        kahan_add(t.z, ct.z, dt.z);
+    };
     auto pair = [&](uint32_t ent, const T4 &pj, const T4 &nj) {
         const T4 s = sh[ent >> NB_SHIFT];
         const R dx = (pi.x - pj.x) + s.x;
@@ -280,52 +314,31 @@ __device__ __forceinline__ void particle_forces(const KArgs<R> &a, const FFDev<R
         const R dz = (pi.z - pj.z) + s.z;
         const R r2 = dx * dx + dy * dy + dz * dz;
         const int tj = w_type(wbits(pj.w));
-        if ((ty | tj) == 0) {
+        if (KAHAN) {
+            R3<R> df = {0, 0, 0}, dt = {0, 0, 0};
+            if ((ty | tj) == 0) {
+                if (r2 < ll_cutsq && r2 > R(1e-5)) {
+                    aniso<R, E>(a.ll, dx, dy, dz, r2, ni.x, ni.y, ni.z, nj.x, nj.y, nj.z, df, dt, e);
+                    accumulate(df, dt);
+                }
+            } else {
+                pair_general<R, E, (V & FORM_INLINE) != 0>(F.pair[ty * NT + tj], dx, dy, dz, r2, ni.x, ni.y, ni.z,
+                                                           nj.x, nj.y, nj.z, df, dt, e);
+                accumulate(df, dt);
+            }
+        } else if ((ty | tj) == 0) {
             if (r2 < ll_cutsq && r2 > R(1e-5))
                 aniso<R, E>(a.ll, dx, dy, dz, r2, ni.x, ni.y, ni.z, nj.x, nj.y, nj.z, f, t, e);
         } else {
-            pair_general<R, E, (V & 2) != 0>(F.pair[ty * NT + tj], dx, dy, dz, r2, ni.x, ni.y, ni.z, nj.x, nj.y,
-                                             nj.z, f, t, e);
+            pair_general<R, E, (V & FORM_INLINE) != 0>(F.pair[ty * NT + tj], dx, dy, dz, r2, ni.x, ni.y, ni.z, nj.x,
+                                                       nj.y, nj.z, f, t, e);
         }
     };
-    // Inner rows: partners that were inside the interaction range at the last
-    // build; almost all still are, so every lane does the pair arithmetic.
-    if (V & 1) {
-        /* software-pipelined: the entry two ahead and the gathers one ahead
-         * are in flight while the current pair is evaluated */
-        uint32_t e1 = nin > 0 ? __ldcs(nb) : 0u;
-        uint32_t e2 = nin > 1 ? __ldcs(nb + stride) : 0u;
-        T4 pn, nn;
-        if (nin > 0) {
-            pn = ldg4<R>(pos + int(e1 & NB_MASK));
-            nn = ldg4<R>(nrm + int(e1 & NB_MASK));
-        }
-        for (int k = 0; k < nin; ++k) {
-            const uint32_t ent = e1;
-            const T4 pj = pn, nj = nn;
-            e1 = e2;
-            if (k + 2 < nin) e2 = __ldcs(nb + int64_t(k + 2) * stride);
-            if (k + 1 < nin) {
-                pn = ldg4<R>(pos + int(e1 & NB_MASK));
-                nn = ldg4<R>(nrm + int(e1 & NB_MASK));
-            }
-            pair(ent, pj, nj);
-        }
-    } else {
-#pragma unroll 2
-        for (int k = 0; k < nin; ++k) {
-            const uint32_t ent = __ldcs(nb + int64_t(k) * stride);
-            const int j = int(ent & NB_MASK);
-            pair(ent, ldg4<R>(pos + j), ldg4<R>(nrm + j));
-        }
-    }
     // Shell rows: partners in the skin at the last build, mostly still outside
-    // the range; the orientation is only gathered for the few that came in.
-#pragma unroll 2
-    for (int k = 0; k < nout; ++k) {
-        const uint32_t ent = __ldcs(shell - int64_t(k) * stride);
-        const int j = int(ent & NB_MASK);
-        const T4 pj = ldg4<R>(pos + j);
+    // the range; returns whether row k's partner has come inside it.
+    auto shell_hit = [&](int k, uint32_t &ent, T4 &pj) {
+        ent = __ldcs(shell - int64_t(k) * stride);
+        pj = ldg4<R>(pos + int(ent & NB_MASK));
         const T4 s = sh[ent >> NB_SHIFT];
         const R dx = (pi.x - pj.x) + s.x;
         const R dy = (pi.y - pj.y) + s.y;
@@ -333,7 +346,90 @@ __device__ __forceinline__ void particle_forces(const KArgs<R> &a, const FFDev<R
         const R r2 = dx * dx + dy * dy + dz * dz;
         const int tj = w_type(wbits(pj.w));
         const R lim = ((ty | tj) == 0) ? ll_cutsq : F.pair[ty * NT + tj].anysq;
-        if (r2 < lim) pair(ent, pj, ldg4<R>(nrm + j));
+        return r2 < lim;
+    };
+    if (V & FORM_MERGED) {
+        /* shell rows first, distance only: row k's hit is bit k of hm (rows
+         * beyond 64 are evaluated on the spot, after the merged pass, as
+         * without this form) */
+        uint64_t hm = 0;
+        const int nq = min(nout, 64);
+        for (int k = 0; k < nq; ++k) {
+            uint32_t ent;
+            T4 pj;
+            if (shell_hit(k, ent, pj)) hm |= uint64_t(1) << k;
+        }
+        // inner rows, then the shell hits in row order, in one loop
+        const int total = nin + __popcll(hm);
+        auto entry = [&](int k, uint64_t &m) -> uint32_t {
+            if (k < nin) return __ldcs(nb + int64_t(k) * stride);
+            const int b = __ffsll((long long)m) - 1;
+            m &= m - 1;
+            return __ldcs(shell - int64_t(b) * stride);
+        };
+        uint64_t mq = hm;
+        uint32_t e1 = total > 0 ? entry(0, mq) : 0u;
+        uint32_t e2 = total > 1 ? entry(1, mq) : 0u;
+        T4 pn, nn;
+        if (total > 0) {
+            pn = ldg4<R>(pos + int(e1 & NB_MASK));
+            nn = ldg4<R>(nrm + int(e1 & NB_MASK));
+        }
+        for (int k = 0; k < total; ++k) {
+            const uint32_t ent = e1;
+            const T4 pj = pn, nj = nn;
+            e1 = e2;
+            if (k + 2 < total) e2 = entry(k + 2, mq);
+            if (k + 1 < total) {
+                pn = ldg4<R>(pos + int(e1 & NB_MASK));
+                nn = ldg4<R>(nrm + int(e1 & NB_MASK));
+            }
+            pair(ent, pj, nj);
+        }
+        for (int k = 64; k < nout; ++k) {
+            uint32_t ent;
+            T4 pj;
+            if (shell_hit(k, ent, pj)) pair(ent, pj, ldg4<R>(nrm + int(ent & NB_MASK)));
+        }
+    } else {
+        // Inner rows: partners that were inside the interaction range at the last
+        // build; almost all still are, so every lane does the pair arithmetic.
+        if (V & FORM_PIPE) {
+            /* software-pipelined: the entry two ahead and the gathers one ahead
+             * are in flight while the current pair is evaluated */
+            uint32_t e1 = nin > 0 ? __ldcs(nb) : 0u;
+            uint32_t e2 = nin > 1 ? __ldcs(nb + stride) : 0u;
+            T4 pn, nn;
+            if (nin > 0) {
+                pn = ldg4<R>(pos + int(e1 & NB_MASK));
+                nn = ldg4<R>(nrm + int(e1 & NB_MASK));
+            }
+            for (int k = 0; k < nin; ++k) {
+                const uint32_t ent = e1;
+                const T4 pj = pn, nj = nn;
+                e1 = e2;
+                if (k + 2 < nin) e2 = __ldcs(nb + int64_t(k + 2) * stride);
+                if (k + 1 < nin) {
+                    pn = ldg4<R>(pos + int(e1 & NB_MASK));
+                    nn = ldg4<R>(nrm + int(e1 & NB_MASK));
+                }
+                pair(ent, pj, nj);
+            }
+        } else {
+#pragma unroll 2
+            for (int k = 0; k < nin; ++k) {
+                const uint32_t ent = __ldcs(nb + int64_t(k) * stride);
+                const int j = int(ent & NB_MASK);
+                pair(ent, ldg4<R>(pos + j), ldg4<R>(nrm + j));
+            }
+        }
+        // the orientation is only gathered for the few shell partners that came in
+#pragma unroll 2
+        for (int k = 0; k < nout; ++k) {
+            uint32_t ent;
+            T4 pj;
+            if (shell_hit(k, ent, pj)) pair(ent, pj, ldg4<R>(nrm + int(ent & NB_MASK)));
+        }
     }
     // bonds
     const int bd = w_bdeg(w);
@@ -346,9 +442,15 @@ __device__ __forceinline__ void particle_forces(const KArgs<R> &a, const FFDev<R
             rel_pos<R>(sd, a.cell[lp][bs.partner], ci, pj, pi, dx, dy, dz);
             const R r = sqrt(dx * dx + dy * dy + dz * dz);
             const R kap = bond_kappa<R, E>(F.bond[bs.type], R(bs.r0), r, e, flags);
-            f.x += kap * dx;
-            f.y += kap * dy;
-            f.z += kap * dz;
+            if (KAHAN) {
+                kahan_add(f.x, cf.x, kap * dx);
+                kahan_add(f.y, cf.y, kap * dy);
+                kahan_add(f.z, cf.z, kap * dz);
+            } else {
+                f.x += kap * dx;
+                f.y += kap * dy;
+                f.z += kap * dz;
+            }
         }
     }
     // global area / volume constraint on mesh vertices
@@ -366,9 +468,15 @@ __device__ __forceinline__ void particle_forces(const KArgs<R> &a, const FFDev<R
             const R hx = nx * inn, hy = ny * inn, hz = nz * inn;
             const R ex = bx - cx, ey = by - cy, ez = bz - cz;
             const R gx = ey * hz - ez * hy, gy = ez * hx - ex * hz, gz = ex * hy - ey * hx;  // 2 dA/da
-            f.x += cv * nx + ca * gx;
-            f.y += cv * ny + ca * gy;
-            f.z += cv * nz + ca * gz;
+            if (KAHAN) {
+                kahan_add(f.x, cf.x, cv * nx + ca * gx);
+                kahan_add(f.y, cf.y, cv * ny + ca * gy);
+                kahan_add(f.z, cf.z, cv * nz + ca * gz);
+            } else {
+                f.x += cv * nx + ca * gx;
+                f.y += cv * ny + ca * gy;
+                f.z += cv * nz + ca * gz;
+            }
         }
     }
 }
@@ -471,6 +579,7 @@ __device__ __forceinline__ double combine_part(int k, double x, double y) {
  * thermostat, kinetic energy, potential energy, bulk velocity, rebuild rule,
  * step counter, buffer parity. */
 template<class R> __global__ void __launch_bounds__(RED_GROUP) k_reduce(KArgs<R> a, int mode, int count_step) {
+    if (halted(a.S)) return;  // the kernel before it did nothing; its partials are stale
     __shared__ double red[7][RED_GROUP];
     __shared__ double wmax[RED_GROUP / 32];
     __shared__ int wfl[RED_GROUP / 32];
@@ -559,8 +668,16 @@ template<class R> __global__ void __launch_bounds__(RED_GROUP) k_reduce(KArgs<R>
         if (mode == MODE_LANGEVIN) {
             S->cur ^= 1;
             S->step += 1;
+            S->iters += 1;
         }
-        if (mode == MODE_NH_FINAL && count_step) S->step += 1;
+        if (mode == MODE_NH_INITIAL) S->nh_half = 1;
+        if (mode == MODE_NH_FINAL) {
+            S->nh_half = 0;
+            if (count_step) {
+                S->step += 1;
+                S->iters += 1;
+            }
+        }
         S->blk_counter = 0;
         __threadfence();
     }
@@ -642,6 +759,7 @@ __device__ __forceinline__ void langevin_particle(const KArgs<R> &a, const FFDev
  * k_reduce after the kernel. */
 template<class R, bool E, int V>
 __global__ void __launch_bounds__(LITE_BS, fp_blocks<R>(20)) k_step_langevin(KArgs<R> a) {
+    if (halted(a.S)) return;
     using T4 = typename Vec<R>::T4;
     __shared__ T4 sh[27];
     init_shift<R>(a, sh);
@@ -670,6 +788,7 @@ __global__ void __launch_bounds__(LITE_BS, fp_blocks<R>(20)) k_step_langevin(KAr
  * demand (k_vcom). */
 template<class R, int V>
 __global__ void __launch_bounds__(LITE_BS, fp_blocks<R>((V & 4) ? 20 : 16)) k_step_langevin_lite(KArgs<R> a) {
+    if (halted(a.S)) return;
     using T4 = typename Vec<R>::T4;
     __shared__ T4 sh[27];
     init_shift<R>(a, sh);
@@ -700,6 +819,8 @@ __global__ void __launch_bounds__(LITE_BS, fp_blocks<R>((V & 4) ? 20 : 16)) k_st
  * flip the position buffers, advance the step counter and apply the
  * every-k-steps rebuild rule. */
 __global__ void k_advance(Scalars *S, int rebuild_every, int count_step) {
+    if (halted(S)) return;
+    S->iters += 1;
     S->cur ^= 1;
     S->step += count_step;
     S->since_rebuild += 1;
@@ -714,6 +835,7 @@ __global__ void k_advance(Scalars *S, int rebuild_every, int count_step) {
 template<class R, int V>
 __global__ void __launch_bounds__(LITE_BS, fp_blocks<R>((V & 2) ? 12 : 16))
     k_minimize(KArgs<R> a, double dr_opt, double dn_opt) {
+    if (halted(a.S)) return;
     using T4 = typename Vec<R>::T4;
     __shared__ T4 sh[27];
     init_shift<R>(a, sh);
@@ -776,6 +898,7 @@ __global__ void __launch_bounds__(LITE_BS, fp_blocks<R>((V & 2) ? 12 : 16))
  * kinetic-energy sum that k_reduce turns into the thermostat update. */
 template<class R, bool E, int V>
 __global__ void __launch_bounds__(LITE_BS, fp_blocks<R>(20)) k_nh_final(KArgs<R> a, int count_step) {
+    if (halted(a.S)) return;
     using T4 = typename Vec<R>::T4;
     __shared__ T4 sh[27];
     init_shift<R>(a, sh);
@@ -830,6 +953,7 @@ __global__ void __launch_bounds__(LITE_BS, fp_blocks<R>(20)) k_nh_final(KArgs<R>
 }
 
 template<class R> __global__ void __launch_bounds__(256) k_nh_initial(KArgs<R> a) {
+    if (halted(a.S)) return;
     using T4 = typename Vec<R>::T4;
     const int cur = __ldcg(&a.S->cur), lp = __ldcg(&a.S->lp);
     const int i = blockIdx.x * 256 + threadIdx.x;
@@ -934,6 +1058,7 @@ template<class R> __global__ void __launch_bounds__(256) k_assign_temperature(KA
 }
 
 template<class R, bool E, int V> __global__ void __launch_bounds__(LITE_BS, fp_blocks<R>(16)) k_forces(KArgs<R> a) {
+    if (halted(a.S)) return;
     using T4 = typename Vec<R>::T4;
     __shared__ T4 sh[27];
     init_shift<R>(a, sh);
@@ -1056,19 +1181,22 @@ template<class R> __global__ void __launch_bounds__(256) k_mesh(KArgs<R> a) {
 
 }  // namespace
 
-/* Force-kernel forms (bit 0: software-pipelined list pass -- the next entry's
- * gathers are issued before the current pair is evaluated -- instead of a
- * 2-way unrolled loop; bit 1: the rare non-lipid pair path inlined, with up
- * to 85 registers, instead of called).  The autotuner picks one per workload. */
+/* Force-kernel forms: the bits of FORM_* above (the list-build form, bits 3-4
+ * of orbc_params.kernel_variant, is handled by the rebuild).  The merged and
+ * compensated bits are instantiated on top of the pipelined, inlined loop. */
 template<class R> void reduce_sums(const KArgs<R> &a, int mode, int count_step, cudaStream_t st) {
     k_reduce<R><<<a.ngroups, RED_GROUP, 0, st>>>(a, mode, count_step);
 }
+/* the pair-loop bits of a form (FORM_OCC dropped), rounded to an instantiated one */
+constexpr int loop_form(int v) {
+    return (v & (FORM_MERGED | FORM_KAHAN)) ? ((v & (FORM_MERGED | FORM_KAHAN)) | FORM_PIPE | FORM_INLINE) : (v & 3);
+}
 template<class R, int V> void step_langevin_v(const KArgs<R> &a, cudaStream_t st, bool energy) {
     if (energy) {
-        k_step_langevin<R, true, V & 3><<<a.npad / LITE_BS, LITE_BS, 0, st>>>(a);
+        k_step_langevin<R, true, loop_form(V)><<<a.npad / LITE_BS, LITE_BS, 0, st>>>(a);
         reduce_sums<R>(a, MODE_LANGEVIN, 1, st);
     } else if (a.zero_bulk) {
-        k_step_langevin<R, false, V & 3><<<a.npad / LITE_BS, LITE_BS, 0, st>>>(a);
+        k_step_langevin<R, false, loop_form(V)><<<a.npad / LITE_BS, LITE_BS, 0, st>>>(a);
         reduce_sums<R>(a, MODE_LANGEVIN, 1, st);
     } else {
         k_step_langevin_lite<R, V><<<a.npad / LITE_BS, LITE_BS, 0, st>>>(a);
@@ -1083,6 +1211,19 @@ template<class R, int V> void nh_final_v(const KArgs<R> &a, cudaStream_t st, boo
     reduce_sums<R>(a, MODE_NH_FINAL, 1, st);
 }
 template<class R> void launch_step_langevin(const KArgs<R> &a, cudaStream_t st, bool energy) {
+    const int ext = a.variant & (FORM_MERGED | FORM_KAHAN);
+    if (ext) {  // the extended forms, with or without the occupancy form
+        const bool occ = (a.variant & FORM_OCC) != 0;
+        switch (ext | (occ ? FORM_OCC : 0)) {
+            case FORM_MERGED: step_langevin_v<R, FORM_MERGED | 3>(a, st, energy); break;
+            case FORM_KAHAN: step_langevin_v<R, FORM_KAHAN | 3>(a, st, energy); break;
+            case FORM_MERGED | FORM_KAHAN: step_langevin_v<R, FORM_MERGED | FORM_KAHAN | 3>(a, st, energy); break;
+            case FORM_MERGED | FORM_OCC: step_langevin_v<R, FORM_MERGED | 7>(a, st, energy); break;
+            case FORM_KAHAN | FORM_OCC: step_langevin_v<R, FORM_KAHAN | 7>(a, st, energy); break;
+            default: step_langevin_v<R, FORM_MERGED | FORM_KAHAN | 7>(a, st, energy); break;
+        }
+        return;
+    }
     switch (a.variant & 7) {
         case 1: step_langevin_v<R, 1>(a, st, energy); break;
         case 2: step_langevin_v<R, 2>(a, st, energy); break;
@@ -1095,23 +1236,34 @@ template<class R> void launch_step_langevin(const KArgs<R> &a, cudaStream_t st, 
     }
 }
 template<class R> void launch_nh_final(const KArgs<R> &a, cudaStream_t st, bool energy) {
-    switch (a.variant & 3) {
+    switch (loop_form(a.variant)) {
         case 1: nh_final_v<R, 1>(a, st, energy); break;
         case 2: nh_final_v<R, 2>(a, st, energy); break;
         case 3: nh_final_v<R, 3>(a, st, energy); break;
+        case FORM_MERGED | 3: nh_final_v<R, FORM_MERGED | 3>(a, st, energy); break;
+        case FORM_KAHAN | 3: nh_final_v<R, FORM_KAHAN | 3>(a, st, energy); break;
+        case FORM_MERGED | FORM_KAHAN | 3: nh_final_v<R, FORM_MERGED | FORM_KAHAN | 3>(a, st, energy); break;
         default: nh_final_v<R, 0>(a, st, energy); break;
     }
 }
 template<class R> void launch_nh_prologue(const KArgs<R> &a, cudaStream_t st) {
-    k_nh_final<R, true, 0><<<a.npad / LITE_BS, LITE_BS, 0, st>>>(a, 0);
+    if (a.variant & FORM_KAHAN)
+        k_nh_final<R, true, FORM_KAHAN | 3><<<a.npad / LITE_BS, LITE_BS, 0, st>>>(a, 0);
+    else
+        k_nh_final<R, true, 0><<<a.npad / LITE_BS, LITE_BS, 0, st>>>(a, 0);
     reduce_sums<R>(a, MODE_NH_FINAL, 0, st);
 }
 template<class R> void launch_nh_initial(const KArgs<R> &a, cudaStream_t st) {
     k_nh_initial<R><<<a.npad / 256, 256, 0, st>>>(a);
     reduce_sums<R>(a, MODE_NH_INITIAL, 0, st);
 }
+/* The forces hook evaluates pairs in the form's accumulation (plain or
+ * compensated); the loop structure does not change the sums' order. */
 template<class R> void launch_forces(const KArgs<R> &a, cudaStream_t st) {
-    k_forces<R, true, 0><<<a.npad / LITE_BS, LITE_BS, 0, st>>>(a);
+    if (a.variant & FORM_KAHAN)
+        k_forces<R, true, FORM_KAHAN | 3><<<a.npad / LITE_BS, LITE_BS, 0, st>>>(a);
+    else
+        k_forces<R, true, 0><<<a.npad / LITE_BS, LITE_BS, 0, st>>>(a);
     reduce_sums<R>(a, MODE_FORCES, 0, st);
 }
 template<class R> void launch_mesh(const KArgs<R> &a, cudaStream_t st) {

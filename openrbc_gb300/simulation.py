@@ -262,12 +262,13 @@ class Simulation:
         return pr.as_dict()
 
     def autotune(self, trial_steps: int = 30):
-        """Pick skin and force-kernel form by timing trials (orbc_gpu_autotune);
-        the state is restored afterwards.  Returns the trial table."""
+        """Pick skin, force-kernel and list-build forms and rebuild cadence by
+        timing trials (orbc_gpu_autotune); the state is restored afterwards.
+        Returns the trial table."""
         rows = (N.TuneTrial * 64)()
         nt = C.c_int()
         self._check(N.lib().orbc_gpu_autotune(self.h, int(trial_steps), rows, 64, C.byref(nt)))
-        return [{"skin": r.skin, "variant": r.variant, "ms_per_step": r.ms_per_step,
+        return [{"skin": r.skin, "variant": r.variant, "rebuild_every": r.rebuild_every, "ms_per_step": r.ms_per_step,
                  "rebuilds_per_step": r.rebuilds_per_step} for r in rows[:nt.value]]
 
     def last_timing(self):

@@ -121,13 +121,100 @@ def ref_temperature(prec, x, nrm, v, ty, tg):
     return R.ref_temperature(len(x), x.ctypes.data, nrm.ctypes.data, v.ctypes.data, ty.ctypes.data, tg.ctypes.data)
 
 
+def lattice_config1():
+    """The plain small workload: 32,768 lipids, row-major on a 182-column
+    square lattice of spacing 1.1 (180 full rows and 8 sites), jitter 0.05,
+    normals tilted 0.05 rad, Maxwell-Boltzmann velocities at kT = 1 -- the
+    library's own generator (orbc_gen_lattice, seed 1), built by the oracle's
+    Makefile.  The inputs are rounded to float32 so the fixture stays small
+    (exact values in float64 for the reference).  Forces and torques by the
+    reference's FP64 code at step 0, its FP32 forces, and 100 noise-free
+    Langevin steps (kT = 0, eta = 0.01) in FP64, of which every fourth
+    particle's final state is kept."""
+    from openrbc_gb300 import workloads
+    w = workloads.lattice(n=32768, ncol=182, spacing=1.1, jitter=0.05, tilt=0.05, kT=1.0, seed=1,
+                          lib=orc.workloads_lib())
+    x, nrm, v, o = (np.asarray(w[k], np.float32).astype(np.float64) for k in ("x", "n", "v", "o"))
+    ty, tg = w["type"], w["tag"]
+    nob = np.zeros((0, 3), np.int32)
+    f64, t64 = ref_forces("f64", x, nrm, ty, tg, nob)
+    f32, t32 = ref_forces("f32", x, nrm, ty, tg, nob)
+    T = ref_temperature("f64", x, nrm, v, ty, tg)
+    lx, ln, lv, lo = ref_langevin("f64", x, nrm, v, o, ty, tg, nob, 0.01, 0.0, 0.01, 100)
+    keep = np.arange(0, len(x), 4)
+    np.savez_compressed(os.path.join(OUT, "lattice_32768.npz"), x=x.astype(np.float32), nrm=nrm.astype(np.float32),
+                        v=v.astype(np.float32), o=o.astype(np.float32), type=ty, tag=tg, f64=f64, t64=t64,
+                        f32=f32.astype(np.float32), t32=t32.astype(np.float32), temperature=T,
+                        lang_keep=keep.astype(np.int32), lang_x=lx[keep], lang_n=ln[keep], lang_v=lv[keep],
+                        lang_o=lo[keep], lang_steps=100, lang_dt=0.01, lang_eta=0.01)
+    print("lattice_32768:", len(x), "particles; |f|max", np.abs(f64).max())
+
+
+def example_large_patch(ref_src, r_in=70.0, margin=6.0, seed=11):
+    """The reference's own whole cell: init_rbc on example-large/rbc.{vert,
+    bond,face}.txt (3.2M particles, 19-bead harmonic spectrin) by the
+    reference's FP64 code.  A patch is cut around a seeded lipid: every
+    particle within r_in + margin of it, with the bonds whose two ends are in
+    the patch.  The margin exceeds every interaction range (largest 3.82, the
+    protein-lipid WCA cut), so the forces on the particles within r_in whose
+    bond partners are all in the patch (`check`) equal their forces in the
+    whole cell; those are the reference's FP64 forces and torques on the
+    patch."""
+    prefix = os.path.join(os.path.dirname(os.path.abspath(ref_src)), "example-large", "rbc")
+    R = orc.ref("f64")
+    cap, bcap = 4_000_000, 1_000_000
+    x = np.zeros((cap, 3))
+    nrm = np.zeros((cap, 3))
+    ty = np.zeros(cap, np.int32)
+    tg = np.zeros(cap, np.int32)
+    b3 = np.zeros((bcap, 3), np.int32)
+    nb = C.c_int64()
+    area = C.c_double()
+    n = R.ref_init_rbc(prefix.encode(), cap, x.ctypes.data, nrm.ctypes.data, ty.ctypes.data, tg.ctypes.data, bcap,
+                       b3.ctypes.data, C.byref(nb), C.byref(area))
+    assert n > 0
+    x, nrm, ty, tg, b3 = x[:n], nrm[:n], ty[:n], tg[:n], b3[:nb.value]
+    rng = np.random.default_rng(seed)
+    lip = np.flatnonzero(ty == 0)
+    c = x[lip[rng.integers(len(lip))]]
+    d = np.linalg.norm(x - c, axis=1)
+    sel = np.flatnonzero(d < r_in + margin)
+    inpatch = np.zeros(n, bool)
+    inpatch[sel] = True
+    idx_of_tag = np.full(int(tg.max()) + 1, -1, np.int64)
+    idx_of_tag[tg] = np.arange(n)
+    bi, bj = idx_of_tag[b3[:, 1]], idx_of_tag[b3[:, 2]]
+    both = inpatch[bi] & inpatch[bj]
+    one = inpatch[bi] ^ inpatch[bj]
+    broken = np.zeros(n, bool)
+    broken[bi[one]] = True
+    broken[bj[one]] = True
+    check = (d[sel] < r_in) & ~broken[sel]
+    px, pn, pty, ptg, pb = x[sel], nrm[sel], ty[sel], tg[sel], b3[both]
+    f64, t64 = ref_forces("f64", px, pn, pty, ptg, pb)
+    np.savez_compressed(os.path.join(OUT, "example_large_patch.npz"), x=px, nrm=pn, type=pty, tag=ptg, bonds=pb,
+                        check=check, f64=f64, t64=t64, cell_particles=n, cell_bonds=nb.value, mesh_area=area.value,
+                        centre=c, r_in=r_in, margin=margin)
+    print("example_large_patch:", len(sel), "particles of", n, "; checked", int(check.sum()), "; types",
+          np.bincount(pty, minlength=6), "; bonds", len(pb))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref-src", default="/root/reference/src", help="the reference's src/ directory")
+    ap.add_argument("--only", default="", help="comma-separated fixture names to (re)make: lattice_576, cell_ico12, "
+                                               "morton, frames, lattice_32768, example_large_patch")
     args = ap.parse_args()
     orc.build(args.ref_src)
     assert orc.ref_available("f64") and orc.ref_available("f32"), "reference harness did not build"
     assert orc.ref("f64").ref_real_bytes() == 8 and orc.ref("f32").ref_real_bytes() == 4
+    only = set(filter(None, args.only.split(",")))
+    if only:
+        if "lattice_32768" in only:
+            lattice_config1()
+        if "example_large_patch" in only:
+            example_large_patch(args.ref_src)
+        return
 
     # ---- plain lipid lattice ------------------------------------------------
     x, nrm, v, o, ty, tg = lattice(24, 24)
@@ -204,6 +291,9 @@ def main():
     np.savez_compressed(os.path.join(OUT, "frames.npz"), x=fx, nrm=fn, v=fv, f=ff, type=fty, tag=ftg, affil=faff,
                         **frames)
     print("frames:", {k: len(v) for k, v in frames.items()})
+
+    lattice_config1()
+    example_large_patch(args.ref_src)
 
 
 if __name__ == "__main__":

@@ -168,3 +168,57 @@ def test_morton_order_large_and_empty():
     keys = orc.morton_encode(p)
     assert np.array_equal(morton_order(p), np.lexsort((np.arange(len(keys)), keys)))
     assert len(morton_order(np.zeros((0, 3)))) == 0
+
+
+# ---- the benchmark configurations' own fixtures ------------------------------
+def _f64(a):
+    return np.asarray(a, np.float64)
+
+
+@pytest.mark.parametrize("precision,form,tol", [("fp64", 0, 1e-10), ("mixed", 0, 1e-5), ("mixed", 3 | 16 | 32, 1e-5),
+                                                ("mixed", 3 | 16 | 32 | 64, 1e-5)])
+def test_example_large_patch_forces(precision, form, tol):
+    """A patch of the reference's own whole cell (init_rbc on example-large:
+    lipids, band-III, actin, spectrin beads and their harmonic bonds) against
+    the reference's FP64 forces and torques."""
+    from openrbc_gb300 import RTParameter, Simulation
+    g = load_golden("example_large_patch.npz")
+    p = RTParameter(init="lipid", kBT=0.22, precision=precision)
+    with Simulation(p, box=REF_BOX, kernel_variant=form) as s:
+        s.upload(g["x"], g["nrm"], np.zeros_like(g["x"]), np.zeros_like(g["x"]), g["type"], g["tag"], g["bonds"])
+        f, t, _ = s.forces()
+    c = g["check"]
+    assert rel_l2(f[c], g["f64"][c]) < tol, rel_l2(f[c], g["f64"][c])
+    assert rel_l2(t[c], g["t64"][c]) < tol, rel_l2(t[c], g["t64"][c])
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-10), ("mixed", 1e-5)])
+def test_config1_lattice_forces(precision, tol):
+    """The plain small workload (32,768 lipids on the 182-column lattice)."""
+    g = load_golden("lattice_32768.npz")
+    gg = {k: (_f64(g[k]) if k in ("x", "nrm", "v", "o") else g[k]) for k in g}
+    with sim_for(gg, precision) as s:
+        f, t, _ = s.forces()
+        th = s.thermo()
+    assert rel_l2(f, g["f64"]) < tol
+    assert rel_l2(t, g["t64"]) < tol
+    T_ref = float(g["temperature"])
+    assert abs(th["temperature"] - T_ref) < (1e-12 if precision == "fp64" else 1e-6) * T_ref
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-8), ("mixed", 2e-3)])
+def test_config1_lattice_noise_free_langevin(precision, tol):
+    """100 noise-free Langevin steps of the 32,768-lipid lattice against the
+    reference's FP64 trajectory (every fourth particle kept in the fixture)."""
+    g = load_golden("lattice_32768.npz")
+    gg = {k: (_f64(g[k]) if k in ("x", "nrm", "v", "o") else g[k]) for k in g}
+    with sim_for(gg, precision, kBT=0.0, dt=float(g["lang_dt"]), eta=float(g["lang_eta"])) as s:
+        s.step(int(g["lang_steps"]))
+        x, n, v, o = s.download()
+    k = g["lang_keep"]
+    x0 = gg["x"][k]
+    assert rel_l2(x[k] - x0, g["lang_x"] - x0) < tol
+    assert rel_l2(v[k], g["lang_v"]) < tol
+    if precision == "fp64":
+        assert rel_l2(n[k], g["lang_n"]) < 1e-9
+        assert rel_l2(o[k], g["lang_o"]) < tol

@@ -372,7 +372,10 @@ def test_autotune_restores_state_and_keeps_stepping():
         step0 = s.thermo()["step"]
         trials = s.autotune(trial_steps=4)
         after = s.download()
-        assert len(trials) == 25 and all(t["ms_per_step"] > 0 for t in trials)  # 5 skins x 4 forms, 2 skins, 3 forms
+        # 5 skins x 5 loop forms, 2 skins, the occupancy form, 2 list-build forms, 2 rebuild cadences
+        assert len(trials) == 32 and all(t["ms_per_step"] > 0 for t in trials)
+        assert {t["rebuild_every"] for t in trials} == {0, 5, 10}
+        assert any(t["variant"] & 32 for t in trials)
         assert s.thermo()["step"] == step0
         d = min_image_diff(after[0], before[0], box, (1, 1, 0))
         assert np.abs(d).max() < 1e-5

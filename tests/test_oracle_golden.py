@@ -145,3 +145,43 @@ def test_energy_is_minus_gradient():
             em = orc.forces(sm, energy=True)[2].sum()
             num = -(ep - em) / (2 * h)
             assert abs(num - f[i, d]) < 1e-5 * max(1.0, abs(f[i, d])), (i, d, num, f[i, d])
+
+
+# ---- the benchmark configurations' own fixtures ------------------------------
+def _f64(a):
+    return np.asarray(a, np.float64)
+
+
+def test_example_large_patch_forces_match_reference():
+    """A patch of the reference's own whole cell (init_rbc on example-large,
+    every particle type it holds, its harmonic spectrin bonds)."""
+    g = load_golden("example_large_patch.npz")
+    st = orc.State(x=g["x"], nrm=g["nrm"], v=np.zeros_like(g["x"]), o=np.zeros_like(g["x"]), type=g["type"],
+                   tag=g["tag"], bonds=g["bonds"])
+    f, t, _, _ = orc.forces(st, "f64")
+    assert rel_l2(f, g["f64"]) < 1e-12
+    assert rel_l2(t, g["t64"]) < 1e-12
+    assert g["check"].sum() > 15000 and set(np.unique(g["type"])) == {0, 2, 3, 4, 5}
+
+
+def test_config1_lattice_matches_reference():
+    """The plain small workload (32,768 lipids): forces, temperature and 100
+    noise-free Langevin steps against the reference's FP64 code."""
+    g = load_golden("lattice_32768.npz")
+    st = orc.State(x=_f64(g["x"]), nrm=_f64(g["nrm"]), v=_f64(g["v"]), o=_f64(g["o"]), type=g["type"], tag=g["tag"])
+    f, t, _, _ = orc.forces(st, "f64")
+    assert rel_l2(f, g["f64"]) < 1e-12
+    assert rel_l2(t, g["t64"]) < 1e-12
+    f32, t32, _, _ = orc.forces(st, "f32")
+    assert rel_l2(f32, g["f32"]) < 2e-5
+    T = orc.thermo(st)["temperature"]
+    assert abs(T - float(g["temperature"])) < 1e-12 * float(g["temperature"])
+    st = orc.State(x=_f64(g["x"]), nrm=_f64(g["nrm"]), v=_f64(g["v"]), o=_f64(g["o"]), type=g["type"], tag=g["tag"],
+                   dt=float(g["lang_dt"]), kBT=0.0, eta=float(g["lang_eta"]))
+    orc.set_threads(8)
+    orc.langevin(st, int(g["lang_steps"]))
+    keep = g["lang_keep"]
+    x0 = _f64(g["x"])[keep]
+    assert rel_l2(st.x[keep] - x0, g["lang_x"] - x0) < 1e-9
+    for k, ref in (("nrm", "lang_n"), ("v", "lang_v"), ("o", "lang_o")):
+        assert rel_l2(getattr(st, k)[keep], g[ref]) < 1e-9, k
