@@ -268,6 +268,231 @@ def run_reference(args, rank, ws):
     return 0
 
 
+# ---------------------------------------------------------------------------
+# The other workloads of the configuration list, one JSON line each
+# (python bench.py --config NAME); the default line is the 4M-particle
+# membrane above.
+# ---------------------------------------------------------------------------
+def _roof(prof, n, bytes_per_pstep=BYTES_PER_PSTEP):
+    peak, kind = measured_peaks()
+    kt = prof["step_kernel_ms"]
+    achieved = bytes_per_pstep * n / (kt * 1e-3) / 1e9
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": None, "kernel_ms": kt, "bytes_per_particle_step": bytes_per_pstep,
+            "peak_source": f"{kind} (MEASURED_PEAKS.json hbm_gbs)"}
+
+
+def _line(metric_value, args, cfg, **extra):
+    line = {"metric": METRIC, "value": metric_value, "unit": "particle-steps/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": cfg}
+    line.update(extra)
+    return line
+
+
+def run_config_lattice(args):
+    """Plain method, small: 32,768 lipids on the 182-column square lattice of
+    spacing 1.1 in a periodic 200 x 200 x 40 box, Langevin dt 0.01, kT 1, 100
+    steps: plain FP64 and mixed on the GPU, the oracle's FP64 restatement and
+    FP32 CPU baseline on the host cores."""
+    from openrbc_gb300 import RTParameter, Simulation, workloads
+    from oracle import oracle as orc
+    w = workloads.lattice(n=32768, ncol=182, spacing=1.1, jitter=0.05, tilt=0.05, kT=1.0, seed=1)
+    n = len(w["x"])
+    box, per = ((0.0, 200.0), (0.0, 200.0), (-20.0, 20.0)), (1, 1, 1)
+    steps = args.steps
+    out = {}
+    f_gpu = {}
+    for prec, form in (("fp64", 3 | 16 | 32), ("mixed", 7 | 16 | 32)):
+        p = RTParameter(init="lipid", kBT=KT, dt=DT, eta=0.01, precision=prec)
+        with Simulation(p, box=box, periodic=per, kernel_variant=form, skin=0.5) as s:
+            s.upload(w["x"], w["n"], w["v"], w["o"], w["type"], w["tag"])
+            f_gpu[prec], _, _ = s.forces()
+            s.step(args.warmup)
+            s.step(steps)
+            ms, launches = s.last_timing()
+            prof = s.profile(20)
+        out[prec] = {"value": n * steps / (ms * 1e-3), "ms_per_step": ms / steps, "kernel_form": form,
+                     "gpu_launches": launches, "profile": prof}
+        log(f"lattice {prec}: {ms / steps:.4f} ms/step")
+    threads = os.cpu_count() or 1
+    orc.set_threads(threads)
+    st = orc.State(x=w["x"], nrm=w["n"], v=w["v"], o=w["o"], type=w["type"], tag=w["tag"], kBT=KT, dt=DT, eta=0.01,
+                   lo=tuple(b[0] for b in box), hi=tuple(b[1] for b in box), periodic=per, seed=1)
+    f_ref, _, _, _ = orc.forces(st, "f64")
+    t0 = time.perf_counter()
+    orc.langevin(st.copy(), steps, "f64")
+    cpu64 = n * steps / (time.perf_counter() - t0)
+    st32 = st.copy()
+    t0 = time.perf_counter()
+    orc.cpu_baseline_run(st32, steps, CPU_SKIN)
+    cpu32 = n * steps / (time.perf_counter() - t0)
+    cfg = {"workload": "lattice-32768", "n_particles": n, "lattice": "182 columns, spacing 1.1, jitter 0.05, "
+           "tilt 0.05 rad", "box": "200 x 200 x 40, periodic", "integrator": "langevin", "dt": DT, "kT": KT,
+           "l2": "working set below L2: the state stays in L2 between steps"}
+    return _line(out["fp64"]["value"], args, cfg, dtype="f64", precision="fp64 (the plain FP64 GPU form)",
+                 ms_per_step=out["fp64"]["ms_per_step"], mixed=out["mixed"], fp64=out["fp64"],
+                 force_rel_err_fp64_vs_oracle=float(np.linalg.norm(f_gpu["fp64"] - f_ref) / np.linalg.norm(f_ref)),
+                 force_rel_err_mixed_vs_oracle=float(np.linalg.norm(f_gpu["mixed"] - f_ref) / np.linalg.norm(f_ref)),
+                 cpu_fp64={"value": cpu64, "cores": threads, "kind": "port", "what": "the oracle's FP64 restatement"},
+                 cpu_baseline={"value": cpu32, "unit": "particle-steps/s", "cores": threads, "kind": "port",
+                               "sample": f"{steps} steps, FP32; " + CPU_KIND},
+                 roofline=_roof(out["fp64"]["profile"], n, 192.0), gpu_launches=out["fp64"]["gpu_launches"])
+
+
+def run_config_nh(args):
+    """The 4M-particle membrane in mixed precision under Nose-Hoover at kT 1:
+    --steps steps in chunks of --check-every; after each chunk the mixed state
+    is loaded into a plain FP64 handle of the same system and its forces,
+    torques, potential energy, area and volume are compared with the mixed
+    handle's own at that state."""
+    from openrbc_gb300 import RTParameter, Simulation, workloads
+    w = workload(args.n_lipid)
+    n = len(w["x"])
+    c = w["constraint"]
+    sysdesc = [{"lo": (-1000.0,) * 3, "hi": (1000.0,) * 3, "periodic": (0, 0, 0), "kv": c["kv"], "V0": c["V0"],
+                "ka": c["ka"], "A0": c["A0"]}]
+
+    def handle(prec, form):
+        p = RTParameter(init="trimesh", mesh="synthetic", kBT=KT, dt=DT, precision=prec, integrator="nose-hoover")
+        s = Simulation(p, skin=0.8, bond_table=workloads.RBC_BOND_TABLE, kernel_variant=form, energy=True)
+        s.upload_batch(sysdesc, w["x"], w["n"], w["v"], w["o"], w["type"], w["tag"], [0, n], bonds=w["bonds"],
+                       bond_r0=w["bond_r0"], faces=w["faces"])
+        return s
+
+    form = args.form if args.form else (3 | 16 | 32 | 64)
+    # the running handle, and two probes that receive its state at each check:
+    # calling forces() on the running handle would re-prime its carried forces
+    mixed, probe, ref = handle("mixed", form), handle("mixed", form), handle("fp64", 3 | 16 | 32)
+    mixed.step(args.warmup)
+    checks, total_ms, done = [], 0.0, 0
+    while done < args.steps:
+        k = min(args.check_every, args.steps - done)
+        mixed.step(k)
+        ms, _ = mixed.last_timing()
+        total_ms += ms
+        done += k
+        thm = mixed.thermo()
+        x, nv, v, o = mixed.download()
+        probe.set_state(x, nv, v, o)
+        ref.set_state(x, nv, v, o)
+        fm, tm, em = probe.forces()
+        fr, tr, er = ref.forces()
+        thp, thr = probe.thermo(), ref.thermo()
+        row = {"step": thm["step"], "force_rel_err": float(np.linalg.norm(fm - fr) / np.linalg.norm(fr)),
+               "torque_rel_err": float(np.linalg.norm(tm - tr) / np.linalg.norm(tr)),
+               "energy_rel_err": float(abs(em.sum() - er.sum()) / abs(er.sum())),
+               "area_rel_err": abs(thp["area"] - thr["area"]) / thr["area"],
+               "volume_rel_err": abs(thp["volume"] - thr["volume"]) / thr["volume"],
+               "area": thm["area"], "volume": thm["volume"], "temperature": thm["temperature"], "zeta": thm["zeta"]}
+        checks.append(row)
+        log(f"nh step {row['step']}: force err {row['force_rel_err']:.2e}, area err {row['area_rel_err']:.2e}, "
+            f"volume err {row['volume_rel_err']:.2e}, T {row['temperature']:.4f}")
+    probe.close()
+    ref.close()
+    prof = mixed.profile(20)
+    value = n * args.steps / (total_ms * 1e-3)
+    mixed.close()
+    cfg = dict(bench_config(w, args.n_lipid), integrator="nose-hoover", workload=f"rbc-evans-fung-{n}-nh")
+    return _line(value, args, cfg, ms_per_step=total_ms / args.steps, precision="mixed", kernel_form=form,
+                 checks=checks, check_every=args.check_every,
+                 max_force_rel_err=max(r["force_rel_err"] for r in checks),
+                 max_area_rel_err=max(r["area_rel_err"] for r in checks),
+                 max_volume_rel_err=max(r["volume_rel_err"] for r in checks), profile=prof,
+                 roofline=_roof(prof, n))
+
+
+def _tuned(sim, args):
+    if args.no_autotune:
+        return None
+    trials = sim.autotune(trial_steps=20)
+    best = min(trials, key=lambda r: r["ms_per_step"])
+    return {"chosen": best, "trials": len(trials)}
+
+
+def run_config_vesicles(args):
+    """96 spherical vesicles, log-normal sizes between 10k and 250k lipids
+    (median 40k, about 5M in all), each in its own periodic box of edge 2.5
+    diameters, advanced together in one launch per step (mixed, Langevin)."""
+    from openrbc_gb300 import RTParameter, Simulation, workloads
+    w = workloads.vesicles()
+    n = len(w["x"])
+    p = RTParameter(init="vesicle", kBT=KT, dt=DT, eta=0.01, precision="mixed")
+    with Simulation(p, skin=0.8, kernel_variant=args.form or (7 | 16 | 32)) as s:
+        s.upload_batch(w["systems"], w["x"], w["n"], w["v"], w["o"], w["type"], w["tag"], w["offsets"])
+        tune = _tuned(s, args)
+        s.step(args.warmup)
+        th = s.step(args.steps)
+        ms, launches = s.last_timing()
+        prof = s.profile(20)
+    value = n * args.steps / (ms * 1e-3)
+    sizes = w["sizes"]
+    cfg = {"workload": f"vesicles-96-{n}", "n_particles": n, "systems": 96, "size_min": int(sizes.min()),
+           "size_median": int(np.median(sizes)), "size_max": int(sizes.max()), "integrator": "langevin", "dt": DT,
+           "kT": KT, "l2": "inputs larger than L2", "parallelism": "one launch per step for all systems"}
+    return _line(value, args, cfg, ms_per_step=ms / args.steps, precision="mixed", tuning=tune, profile=prof,
+                 roofline=_roof(prof, n), gpu_launches=launches, temperature=th["temperature"])
+
+
+ENSEMBLE_KV = 0.05  # volume-constraint stiffness of the ensemble's cells
+
+
+def run_config_ensemble(args):
+    """8 whole red cells of about 4.0M particles each (32M in all), reduced
+    volumes 0.60, 0.65, ..., 0.95, each with its own spectrin network (seeds
+    5..12) and volume constraint, Nose-Hoover at kT 1, mixed, one
+    graph-captured step for all cells.  Every cell starts from the same
+    biconcave shape (reduced volume about 0.64), so the cells far from their
+    target are pulled towards it by a soft constraint (kv = ENSEMBLE_KV; with
+    the single cell's kv = 10 the 0.95 cell's spectrin bonds pass their
+    maximum extension within a few hundred steps)."""
+    from openrbc_gb300 import RTParameter, Simulation, workloads
+    cells, sysd, base = [], [], 0
+    for i in range(8):
+        v0 = 0.60 + 0.05 * i
+        wi = workloads.rbc(n_lipid=args.n_lipid, freq=FREQ if args.n_lipid == N_LIPID else
+                           max(4, int(round(FREQ * (args.n_lipid / N_LIPID) ** 0.5))), kT=KT, seed=5 + i,
+                           reduced_volume=v0, kv=ENSEMBLE_KV)
+        shift = base - int(wi["tag"].min()) + 1
+        wi["tag"] = wi["tag"] + shift
+        wi["bonds"] = wi["bonds"].copy()
+        wi["bonds"][:, 1:] += shift
+        wi["faces"] = wi["faces"] + shift
+        base = int(wi["tag"].max())
+        c = wi["constraint"]
+        sysd.append({"lo": (-1000.0,) * 3, "hi": (1000.0,) * 3, "periodic": (0, 0, 0), "kv": c["kv"], "V0": c["V0"],
+                     "ka": c["ka"], "A0": c["A0"]})
+        cells.append(wi)
+        log(f"cell {i}: {len(wi['x'])} particles, reduced volume {v0:.2f}")
+    cat = {k: np.concatenate([c[k] for c in cells]) for k in ("x", "n", "v", "o", "type", "tag", "bonds", "bond_r0",
+                                                             "faces")}
+    offs = np.concatenate([[0], np.cumsum([len(c["x"]) for c in cells])])
+    n = int(offs[-1])
+    p = RTParameter(init="trimesh", mesh="synthetic", kBT=KT, dt=DT, precision="mixed", integrator="nose-hoover")
+    with Simulation(p, skin=0.8, bond_table=workloads.RBC_BOND_TABLE,
+                    kernel_variant=args.form or (3 | 16 | 32 | 64)) as s:
+        s.upload_batch(sysd, cat["x"], cat["n"], cat["v"], cat["o"], cat["type"], cat["tag"], offs,
+                       bonds=cat["bonds"], bond_r0=cat["bond_r0"], faces=cat["faces"])
+        s.step(args.warmup)
+        th = s.step(args.steps)
+        ms, launches = s.last_timing()
+        per_cell = [s.thermo(k) for k in range(8)]
+        prof = s.profile(10)
+    value = n * args.steps / (ms * 1e-3)
+    cfg = {"workload": f"rbc-ensemble-8x{args.n_lipid}", "n_particles": n, "systems": 8,
+           "reduced_volumes": [round(0.60 + 0.05 * i, 2) for i in range(8)], "kv": ENSEMBLE_KV,
+           "integrator": "nose-hoover", "dt": DT,
+           "kT": KT, "l2": "inputs larger than L2", "parallelism": "one graph-captured step for all cells"}
+    return _line(value, args, cfg, ms_per_step=ms / args.steps, precision="mixed", profile=prof,
+                 roofline=_roof(prof, n), gpu_launches=launches,
+                 cells=[{"area": c["area"], "volume": c["volume"], "temperature": c["temperature"], "zeta": c["zeta"]}
+                        for c in per_cell])
+
+
+CONFIGS = {"lattice32k": run_config_lattice, "nh4m": run_config_nh, "vesicles96": run_config_vesicles,
+           "ensemble8": run_config_ensemble}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -283,12 +508,20 @@ def main():
     ap.add_argument("--skin", type=float, default=None, help="neighbour skin when not autotuning")
     ap.add_argument("--form", type=int, default=0, help="kernel form 0..127 (orbc_params.kernel_variant)")
     ap.add_argument("--rebuild-every", type=int, default=0, help="fixed rebuild cadence when not autotuning")
+    ap.add_argument("--config", default="rbc4m", choices=["rbc4m"] + sorted(CONFIGS),
+                    help="workload: rbc4m (default, the headline line), lattice32k, nh4m, vesicles96, ensemble8")
+    ap.add_argument("--check-every", type=int, default=1000, help="nh4m: steps between FP64 comparisons")
     args = ap.parse_args()
     rank, ws = dist_setup()
     if args.impl == "reference":
         return run_reference(args, rank, ws)
     if "LOCAL_RANK" in os.environ:
         os.environ.setdefault("CUDA_VISIBLE_DEVICES", os.environ["LOCAL_RANK"])
+    if args.config != "rbc4m":
+        line = CONFIGS[args.config](args)
+        if rank == 0:
+            print(json.dumps(line), flush=True)
+        return 0
 
     from openrbc_gb300 import _native as N
     L = N.lib()

@@ -104,6 +104,13 @@ typedef struct {
        integrate(zero_bulk_velocity(param), lipid) at src/openrbc.cpp:228 would
        (src/zero_bulk_velocity.h:29-56); 0 (default): off, as in the reference */
     int zero_bulk;
+    /* orbc_gpu_set_state(_f32) / orbc_gpu_download(_f32): 1 (default) = when the
+       caller's arrays are reachable from the GPU -- page-locked and mapped
+       (cudaHostAlloc / cudaHostRegister), or ordinary pageable memory on a
+       GPU that reads the host's page tables (Grace systems) -- the
+       conversion kernels read and write them in place over the host link,
+       with no staging copy; 0 = always copy through a device staging buffer */
+    int host_direct;
 } orbc_params;
 
 /* One independent system of a batched upload (its own box and constraint). */
@@ -176,18 +183,21 @@ int orbc_gpu_set_state_f32(orbc_handle *h, int64_t first, int64_t count, int str
 /* nsteps of the loop body of src/openrbc.cpp:189-242 (pair forces, bonds,
  * constraint, integrator; neighbour rebuild on demand).  out may be NULL.
  *
- * A neighbour list that outgrows its capacity at a rebuild inside the call is
- * not an error: the device stops stepping at that build (no step runs on a
- * truncated list), the library grows the list, rebuilds it from the current
- * state and runs the remaining steps (for Nose-Hoover, it first finishes the
- * interrupted step's second half), so the call still completes nsteps steps.
- * ORBC_ERR_GRID: a particle of a system with open axes left that system's
- * grid (set at upload: the particles' extent plus a margin of at least a
- * quarter of it and five list cutoffs on each side); it was kept in the edge
- * cell, where pairs beyond that cell's neighbours are missed, so the state is
- * no longer trustworthy.  Like ORBC_ERR_NAN and ORBC_ERR_BOND, the condition
- * stays recorded (every later step, minimize and forces call returns it, and
- * orbc_thermo.flags shows it) until the next orbc_gpu_upload. */
+ * Two conditions found by a neighbour rebuild inside the call are handled
+ * without an error: a list that outgrows its capacity, and a particle of a
+ * system with open axes that has left that system's grid (set at upload: the
+ * particles' extent plus a margin of at least a quarter of it and five list
+ * cutoffs on each side; a stray lipid that leaves the membrane reaches it
+ * after enough steps).  The device stops stepping at that build, so no step
+ * runs on a truncated list or with a particle clamped into an edge cell; the
+ * library grows the list, or re-grids the systems from the current state,
+ * rebuilds, finishes the interrupted Nose-Hoover step's second half if its
+ * first half ran, and runs the remaining steps, so the call still completes
+ * nsteps steps.  The same holds for orbc_gpu_minimize and orbc_gpu_forces, and
+ * for particles that orbc_gpu_set_state places outside the grid.
+ * ORBC_ERR_NAN and ORBC_ERR_BOND stay recorded (every later step, minimize
+ * and forces call returns them, and orbc_thermo.flags shows them) until the
+ * next orbc_gpu_upload. */
 int orbc_gpu_step(orbc_handle *h, int nsteps, orbc_thermo *out);
 
 /* Current state in upload order (any pointer may be NULL). */
@@ -334,12 +344,13 @@ int orbc_gpu_profile(orbc_handle *h, int nsteps, orbc_profile *out);
 /* Autotuner: times trial_steps graph-captured steps per candidate from a
  * snapshot of the current state, keeps the fastest, and restores the snapshot
  * (state, step counter, thermostat), so the simulation does not advance.
- * Dimensions, in order: neighbour-list skin (0.3, 0.45, 0.6, 0.8, 1.0) x
- * force-loop form (kernel_variant bits 0-1, and the merged shell pass, bit 5);
- * the two skins half-way to the best one's neighbours; the occupancy form
- * (bit 2); the other two list-build forms (bits 3-4); and the rebuild cadence
- * (rebuild_every 0 = only when a particle moved more than skin/2, else also
- * every 5 or 10 steps).  Compensated accumulation (bit 6) is an accuracy
+ * Dimensions, in order: the list-build form (bits 3-4) at the caller's skin;
+ * with it, neighbour-list
+ * skin (0.3, 0.45, 0.6, 0.8, 1.0) x force-loop form (kernel_variant bits 0-1,
+ * and the merged shell pass, bit 5); the two skins half-way to the best one's
+ * neighbours; the occupancy form (bit 2); the other list-build forms again;
+ * and the rebuild cadence (rebuild_every 0 = only when a particle moved more
+ * than skin/2, else also every 5 or 10 steps).  Compensated accumulation (bit 6) is an accuracy
  * choice and is kept as the caller set it.  trials (may be NULL) receives up
  * to max_trials rows.  No reference counterpart (the reference's cadences are
  * fixed command-line values, src/runtime_parameter.h:57-60). */

@@ -54,7 +54,7 @@ class Params(C.Structure):
         ("kv", C.c_double), ("V0", C.c_double), ("ka", C.c_double), ("A0", C.c_double),
         ("bond_style", C.c_int * MAX_BOND_TYPES), ("bond_K", C.c_double * MAX_BOND_TYPES),
         ("bond_r0", C.c_double * MAX_BOND_TYPES), ("bond_R", C.c_double * MAX_BOND_TYPES),
-        ("kernel_variant", C.c_int), ("zero_bulk", C.c_int),
+        ("kernel_variant", C.c_int), ("zero_bulk", C.c_int), ("host_direct", C.c_int),
     ]
 
 

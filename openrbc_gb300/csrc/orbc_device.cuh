@@ -164,12 +164,16 @@ struct Scalars {
     long long step, rebuilds, since_rebuild, pad4;
 };
 
-/* A neighbour list overflowed its capacity at the last build: the step
- * kernels then leave the state untouched (and the step counters unchanged)
- * until the host has grown the list and rebuilt it, so that no step is
- * computed on a truncated list.  The flag is written only by the list build,
- * so every thread of a step kernel reads the same value. */
-__device__ __forceinline__ bool halted(const Scalars *S) { return (__ldcg(&S->error) & ERRB_NBR_OVERFLOW) != 0; }
+/* The last list build found a list longer than its capacity, or a particle
+ * outside its system's open grid: the step kernels then leave the state
+ * untouched (and the step counters unchanged) until the host has grown the
+ * list or re-gridded the system and rebuilt, so that no step is computed on a
+ * truncated list or with a particle clamped into an edge cell.  The flags are
+ * written only by the list build (and by set_state), so every thread of a step
+ * kernel reads the same value. */
+__device__ __forceinline__ bool halted(const Scalars *S) {
+    return (__ldcg(&S->error) & (ERRB_NBR_OVERFLOW | ERRB_GRID)) != 0;
+}
 
 template<class R> struct KArgs {
     using T4 = typename Vec<R>::T4;

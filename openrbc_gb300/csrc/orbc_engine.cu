@@ -362,8 +362,13 @@ template<class R> class Engine : public EngineBase {
         for (cudaEvent_t &e : xev) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
         for (cudaEvent_t &e : pev) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
         CK(cudaGetDevice(&device));
+        int pma = 0;
+        CK(cudaDeviceGetAttribute(&pma, cudaDevAttrPageableMemoryAccess, device));
+        pageable_access = pma != 0;
         return ORBC_OK;
     }
+    bool pageable_access = false;  // the GPU reads pageable host memory (host page tables)
+    int64_t direct_transfers = 0;  // set_state_f32 / download_f32 calls served in place
 
     /* --------------------------------------------------------------------- */
     int upload(int nsys, const orbc_system_desc *descs, const int64_t *offsets, const double *x3, const double *n3,
@@ -691,8 +696,34 @@ template<class R> class Engine : public EngineBase {
     /* upload indices [first, first + count) from host AoS arrays of TH with
      * `stride` values per particle; chunked: the copy stream moves chunk c + 1
      * while the step stream converts chunk c */
+    /* Whether the GPU can read / write host arrays in place: page-locked
+     * memory mapped at the same address (cudaHostAlloc / cudaHostRegister under
+     * unified addressing), or pageable memory on a GPU that reads the host's
+     * page tables.  Device and managed memory take the staged path. */
+    bool host_reachable(const void *p) {
+        if (!P.host_direct || !p) return false;
+        cudaPointerAttributes at;
+        if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+            cudaGetLastError();
+            return false;
+        }
+        if (at.type == cudaMemoryTypeHost) return at.devicePointer == p;
+        if (at.type == cudaMemoryTypeUnregistered) return pageable_access;
+        return false;
+    }
     template<class TH>
     int set_state_t(int64_t first, int64_t count, int stride, const TH *x, const TH *n, const TH *v, const TH *o) {
+        if (host_reachable(x) && host_reachable(n) && host_reachable(v) && host_reachable(o)) {
+            // one pass over the host link: the conversion kernel reads the caller's arrays
+            launch_set_state<R, TH>(a, x, n, v, o, first, first + count, first, stride, st);
+            vcom_valid = !lite();
+            if (vcom_valid) launch_vcom<R>(a, st);
+            CK(cudaGetLastError());
+            CK(cudaStreamSynchronize(st));  // the caller may reuse its arrays on return
+            nh_primed = false;
+            ++direct_transfers;
+            return ORBC_OK;
+        }
         TH *d = reinterpret_cast<TH *>(stage.p);
         const TH *src[4] = {x, n, v, o};
         const int64_t m = count * stride;  // values per array
@@ -734,11 +765,11 @@ template<class R> class Engine : public EngineBase {
             CK(cudaStreamSynchronize(st));
             Scalars hs;
             CK(cudaMemcpy(&hs, Sd.p, sizeof(Scalars), cudaMemcpyDeviceToHost));
-            if (!(hs.error & ERRB_NBR_OVERFLOW)) break;
-            // a list overflowed: the iterations after it did nothing; grow the
-            // list, rebuild it from the current state and run the rest
+            if (!(hs.error & (ERRB_NBR_OVERFLOW | ERRB_GRID))) break;
+            // a halting build: the iterations after it did nothing; grow the
+            // list or re-grid, rebuild from the current state and run the rest
             if (attempt == 4) return fail(ORBC_ERR_NBR_OVERFLOW, "minimize: neighbour capacity could not be sized");
-            const int rc = recover_overflow(hs);
+            const int rc = recover(hs);
             if (rc) return rc;
             nsteps -= int(hs.iters - before.iters);
         }
@@ -759,17 +790,39 @@ template<class R> class Engine : public EngineBase {
         return ORBC_OK;
     }
 
-    /* After a list overflow (the build truncated some lists and the step
-     * kernels that followed left the state untouched): grow the capacity to
-     * the need the build reported, clear the flag and rebuild from the
-     * current state. */
-    int recover_overflow(const Scalars &hs) {
+    /* After a halting build (see halted(): a list overflowed, or a particle
+     * left its system's open grid; the step kernels that followed left the
+     * state untouched): re-grid the systems from the current state if a
+     * particle left a grid -- a full re-layout, which also sizes the lists --
+     * else grow the capacity to the need the build reported, clear the flag
+     * and rebuild. */
+    int recover(const Scalars &hs) {
+        if (hs.error & ERRB_GRID) return regrid();
         int rc = grow_capacity(hs.max_nnb, false);
         if (rc) return rc;
         const int clr = hs.error & ~ERRB_NBR_OVERFLOW;
         CK(cudaMemcpy(&Sd.p->error, &clr, sizeof(int), cudaMemcpyHostToDevice));
         return build_lists(false);
     }
+    /* New grids for the current positions: the open axes are sized again from
+     * the particles' extent (the state, the step counter and each system's
+     * thermostat variable are kept; carried Nose-Hoover forces are not). */
+    int regrid() {
+        const size_t m = size_t(nhome) * 3;
+        std::vector<double> x(m), nv(m), v(m), o(m);
+        int rc = download(x.data(), nv.data(), v.data(), o.data());
+        if (rc) return rc;
+        Scalars hs;
+        CK(cudaMemcpy(&hs, Sd.p, sizeof(Scalars), cudaMemcpyDeviceToHost));
+        std::vector<SysState> hss(topo.descs.size());
+        CK(cudaMemcpy(hss.data(), ssd.p, hss.size() * sizeof(SysState), cudaMemcpyDeviceToHost));
+        for (size_t k = 0; k < hss.size(); ++k) topo.descs[k].zeta = hss[k].zeta;
+        rc = relayout(x, nv, v, o, hs.step);
+        if (rc) return rc;
+        ++regrids;
+        return ORBC_OK;
+    }
+    int64_t regrids = 0;
 
     /* Frame order (src/trajectory.h:75-77): lipids, then proteins, each in
      * upload order; fmap = file position of each upload index. */
@@ -1180,20 +1233,22 @@ template<class R> class Engine : public EngineBase {
             int rc = thermo(-1, out);
             if (rc) return rc;
         }
-        if (hs.error & ERRB_NBR_OVERFLOW) {
-            /* A list build inside the call overflowed: the steps after it left
-             * the state untouched.  Grow the list, rebuild it from the current
-             * state, finish the interrupted Nose-Hoover step if its first half
-             * ran, and run the steps that remain. */
+        if (hs.error & (ERRB_NBR_OVERFLOW | ERRB_GRID)) {
+            /* A list build inside the call halted the steps (a list
+             * overflowed, or a particle left an open grid): the steps after it
+             * left the state untouched.  Grow the list or re-grid, rebuild
+             * from the current state, finish the interrupted Nose-Hoover step
+             * if its first half ran, and run the steps that remain. */
             if (overflow_depth >= 4) return fail(ORBC_ERR_NBR_OVERFLOW, "step: neighbour capacity could not be sized");
-            int rc = recover_overflow(hs);
+            int rc = recover(hs);
             if (rc) return rc;
             int remaining = nsteps - int(hs.iters - before.iters);
             if (P.integrator == ORBC_INT_NOSE_HOOVER) {
-                if (hs.nh_half) {  // the second half of the interrupted step
+                if (hs.nh_half) {  // the second half of the interrupted step (it also carries the forces)
                     if (has_mesh) launch_mesh<R>(a, st);
                     launch_nh_final<R>(a, st, P.energy != 0);
                     CK(cudaGetLastError());
+                    nh_primed = true;
                     --remaining;
                 } else {
                     nh_primed = false;  // the overflow hit the prologue's build: prime again
@@ -1230,6 +1285,15 @@ template<class R> class Engine : public EngineBase {
      * the copy stream moves chunk c to the host while the step stream converts
      * chunk c + 1 */
     template<class TH> int download_t(int64_t first, int64_t count, int stride, TH *x, TH *n, TH *v, TH *o) {
+        if ((x || n || v || o) && (!x || host_reachable(x)) && (!n || host_reachable(n)) &&
+            (!v || host_reachable(v)) && (!o || host_reachable(o))) {
+            // the conversion kernel writes the caller's arrays over the host link
+            launch_download<R, TH>(a, first, first + count, first, stride, x, n, v, o, nullptr, nullptr, nullptr, st);
+            CK(cudaGetLastError());
+            CK(cudaStreamSynchronize(st));
+            ++direct_transfers;
+            return ORBC_OK;
+        }
         TH *d = reinterpret_cast<TH *>(stage.p);
         const int64_t m = count * stride;
         TH *dst[4] = {x, n, v, o};
@@ -1261,9 +1325,9 @@ template<class R> class Engine : public EngineBase {
             CK(cudaMemcpyAsync(&hsc[0], Sd.p, sizeof(Scalars), cudaMemcpyDeviceToHost, st));
             CK(cudaStreamSynchronize(st));
             hs = hsc[0];
-            if (!(hs.error & ERRB_NBR_OVERFLOW)) break;
+            if (!(hs.error & (ERRB_NBR_OVERFLOW | ERRB_GRID))) break;
             if (attempt == 4) return fail(ORBC_ERR_NBR_OVERFLOW, "forces: neighbour capacity could not be sized");
-            const int rc = recover_overflow(hs);  // the forces kernel did nothing: grow, rebuild, again
+            const int rc = recover(hs);  // the forces kernel did nothing: grow, rebuild, again
             if (rc) return rc;
         }
         double *d = stage.p;
@@ -1568,11 +1632,16 @@ template<class R> class Engine : public EngineBase {
             }
             return ORBC_OK;
         };
-        // skin x force-loop form (bits 0-1, and the merged shell pass); the
-        // skins half-way to the best one's grid neighbours; then at the best
-        // pair the occupancy form (bit 2), the other two list-build forms
-        // (bits 3-4) and two fixed rebuild cadences
-        const int rest = P.kernel_variant & 28, every0 = P.rebuild_every;
+        // the list-build form first (bits 3-4, at the caller's skin and the
+        // pipelined, inlined loop); then skin x force-loop form (bits 0-1, and
+        // the merged shell pass) with it; the skins half-way to the best one's
+        // grid neighbours; at the best pair the occupancy form (bit 2), the
+        // other list-build forms and two fixed rebuild cadences
+        const int occ0 = P.kernel_variant & 4, every0 = P.rebuild_every;
+        const double skin0 = P.skin;
+        for (int f = 0; f < 3; ++f)
+            if ((rc = trial(skin0, 3 | occ0 | (f << 3), every0))) return rc;
+        const int rest = (best_var & 24) | occ0;
         const int loops[] = {0, 1, 2, 3, 3 | 32};
         for (double sk : skins)
             for (int lf : loops)
@@ -1877,6 +1946,7 @@ void orbc_gpu_default_params(orbc_params *p) {
     p->bounce = 1;
     p->use_graph = 1;
     p->energy = 0;
+    p->host_direct = 1;
     for (int d = 0; d < 3; ++d) {
         p->lo[d] = -1000;
         p->hi[d] = 1000;
@@ -1899,7 +1969,8 @@ int orbc_gpu_create(const orbc_params *p, orbc_handle **out) {
     *out = nullptr;
     if (!(p->dt > 0) || p->skin < 0 || (p->precision != ORBC_PREC_FP64 && p->precision != ORBC_PREC_MIXED) ||
         (p->integrator != ORBC_INT_LANGEVIN && p->integrator != ORBC_INT_NOSE_HOOVER) ||
-        (p->kernel_variant < 0 || p->kernel_variant > 127 || (p->kernel_variant & 24) == 24) || (p->zero_bulk != 0 && p->zero_bulk != 1)) {
+        (p->kernel_variant < 0 || p->kernel_variant > 127 || (p->kernel_variant & 24) == 24) || (p->zero_bulk != 0 && p->zero_bulk != 1) ||
+        (p->host_direct != 0 && p->host_direct != 1)) {
         g_last_error = "create: invalid parameters";
         return ORBC_ERR_ARG;
     }

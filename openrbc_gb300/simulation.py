@@ -35,7 +35,8 @@ class Simulation:
                  energy: bool = False, box: Optional[Sequence[Sequence[float]]] = None,
                  periodic: Sequence[int] = (0, 0, 0), bond_table: Optional[dict] = None,
                  max_neighbors: int = 0, rebuild_every: Optional[int] = None, bounce: bool = True,
-                 mesh_constraint: Optional[dict] = None, kernel_variant: int = 0, zero_bulk: bool = False):
+                 mesh_constraint: Optional[dict] = None, kernel_variant: int = 0, zero_bulk: bool = False,
+                 host_direct: bool = True):
         self.param = param or RTParameter(init="lipid")
         p = N.Params()
         L = N.lib()
@@ -53,6 +54,7 @@ class Simulation:
         p.energy = 1 if energy else 0
         p.kernel_variant = int(kernel_variant)
         p.zero_bulk = 1 if zero_bulk else 0
+        p.host_direct = 1 if host_direct else 0
         bx = box if box is not None else prm.box
         for d in range(3):
             p.lo[d], p.hi[d] = float(bx[d][0]), float(bx[d][1])

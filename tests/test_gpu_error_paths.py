@@ -6,8 +6,10 @@
   the call returns the same state as a run whose capacity was large enough
   from the start (Langevin with and without per-step sums, Nose-Hoover whose
   interrupted step is finished, minimisation, the forces hook);
-* a particle that leaves an open system's grid makes step / minimize /
-  forces return ORBC_ERR_GRID, and keeps doing so until the next upload.
+* a particle placed or drifted outside an open system's grid: the rebuild
+  that finds it halts the step, the library re-grids the system from the
+  current state and runs the remaining steps; the particle then moves as a
+  free particle and the rest of the system as if it were not there.
 
 The overflow is provoked by uploading a sparse lattice into a small list
 capacity and then setting a dense state: the builds only ever write inside
@@ -76,23 +78,50 @@ def test_overflow_in_minimize_and_forces_is_recovered(precision):
         assert rel_l2(u, v) < tol
 
 
-def test_particle_leaving_an_open_grid_is_an_error_until_upload():
-    from openrbc_gb300 import OrbcError
+def test_particle_outside_an_open_grid_is_regridded():
+    """One lipid moved 900 sigma away from the lattice, far beyond the grid's
+    margin and every interaction range (noise-free Langevin): the step
+    re-grids from the current state and completes, and the run agrees with
+    one that uploads the moved state directly."""
+    from openrbc_gb300 import RTParameter, Simulation
     _, dense = lattices()
-    with sim("mixed", "langevin", 0) as s:
+
+    def noise_free():
+        p = RTParameter(init="lipid", kBT=0.0, precision="fp64", rseed=5)
+        return Simulation(p, box=BOX, skin=0.4)
+
+    with noise_free() as s:
         s.upload(dense["x"], dense["n"], dense["v"], dense["o"], dense["type"], dense["tag"])
         s.step(3)
         x, n, v, o = s.download()
-        x[17] += np.array([900.0, 0.0, 0.0])  # far beyond the grid's margin
+        x[17] += np.array([900.0, 0.0, 0.0])
         s.set_state(x, n, v, o)
-        with pytest.raises(OrbcError) as ei:
-            s.step(1)
-        assert ei.value.code == 5  # ORBC_ERR_GRID
-        assert s.thermo()["flags"] & (1 << 5)
-        with pytest.raises(OrbcError) as ei:
-            s.forces()
-        assert ei.value.code == 5
-        # a fresh upload clears it
+        th = s.step(5)
+        assert th["step"] == 8 and not th["flags"]
+        got = s.download()
+    with noise_free() as s:
+        s.upload(x, n, v, o, dense["type"], dense["tag"])
+        s.step(5)
+        ref = s.download()
+    for u, w in zip(got, ref):
+        assert rel_l2(u, w) < 1e-12
+    assert np.linalg.norm(got[0][17] - x[17]) < 1.0  # a free particle, friction only
+
+
+def test_forces_after_placing_a_particle_outside_the_grid():
+    """forces() re-grids too: the moved particle feels nothing and the others
+    feel what they feel without it."""
+    _, dense = lattices()
+    x = dense["x"].copy()
+    keep = np.arange(len(x)) != 17
+    with sim("fp64", "langevin", 0) as s:
         s.upload(dense["x"], dense["n"], dense["v"], dense["o"], dense["type"], dense["tag"])
-        th = s.step(2)
-        assert th["step"] == 2 and not th["flags"]
+        x[17] += np.array([0.0, 0.0, -700.0])
+        s.set_state(x, dense["n"], dense["v"], dense["o"])
+        f, t, _ = s.forces()
+    assert np.abs(f[17]).max() == 0.0 and np.abs(t[17]).max() == 0.0
+    with sim("fp64", "langevin", 0) as s:
+        s.upload(x[keep], dense["n"][keep], dense["v"][keep], dense["o"][keep], dense["type"][keep],
+                 dense["tag"][keep])
+        f2, t2, _ = s.forces()
+    assert rel_l2(f[keep], f2) < 1e-12 and rel_l2(t[keep], t2) < 1e-12

@@ -87,3 +87,49 @@ def test_f32_boundary_rejects_bad_ranges():
         with pytest.raises(OrbcError):
             s.download_f32(stride=5)
         s.set_state_f32(x[:0], nv[:0], v[:0], o[:0], first=0)  # empty range is a no-op
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_in_place_host_transfers_equal_staged_copies(precision):
+    """With host_direct the conversion kernels read and write the caller's
+    arrays in place when the GPU can reach them (mapped page-locked memory;
+    pageable memory on GPUs that read the host's page tables): the states and
+    downloads must equal those of the staged copies, for pageable numpy arrays
+    and page-locked ones, in FP32 (stride 3 and 4, index ranges) and FP64."""
+    import torch
+    from openrbc_gb300 import RTParameter, Simulation
+    g = load_golden("cell_ico12.npz")
+    x, nv, v, o = _f32_state(g, shift=0.02)
+
+    def pinned(a):
+        t = torch.empty(a.shape, dtype=torch.float32 if a.dtype == np.float32 else torch.float64, pin_memory=True)
+        t.numpy()[:] = a
+        return t.numpy()
+
+    results = []
+    for direct in (False, True):
+        for kind in ("pageable", "pinned"):
+            conv = pinned if kind == "pinned" else (lambda a: np.ascontiguousarray(a))
+            p = RTParameter(init="lipid", precision=precision, kBT=0.5, rseed=21)
+            with Simulation(p, box=REF_BOX, host_direct=direct) as s:
+                s.upload(g["x"], g["nrm"], g["v"], g["o"], g["type"], g["tag"], g.get("bonds"))
+                s.step(2)
+                a = 1000
+                s.set_state_f32(*[conv(q[a:]) for q in (x, nv, v, o)], first=a)
+                s.set_state_f32(*[conv(q[:a]) for q in (x, nv, v, o)], first=0)
+                s.step(4)
+                f32 = s.download_f32()
+                f32s4 = s.download_f32(stride=4)
+                d64 = [conv(q) for q in s.download()]
+                s.set_state(*[conv(q.astype(np.float64) + 0.001) for q in d64])
+                th = s.step(3)
+                results.append((f32, f32s4, s.download(), th["temperature"]))
+    ref = results[0]
+    for r in results[1:]:
+        for u, w in zip(r[0], ref[0]):
+            assert np.array_equal(u, w)
+        for u, w in zip(r[1], ref[1]):
+            assert np.array_equal(u, w)
+        for u, w in zip(r[2], ref[2]):
+            assert np.array_equal(u, w)
+        assert r[3] == ref[3]

@@ -372,8 +372,10 @@ def test_autotune_restores_state_and_keeps_stepping():
         step0 = s.thermo()["step"]
         trials = s.autotune(trial_steps=4)
         after = s.download()
-        # 5 skins x 5 loop forms, 2 skins, the occupancy form, 2 list-build forms, 2 rebuild cadences
-        assert len(trials) == 32 and all(t["ms_per_step"] > 0 for t in trials)
+        # 3 list-build forms, 5 skins x 5 loop forms, 2 skins, the occupancy form, 2 list-build forms,
+        # 2 rebuild cadences
+        assert len(trials) == 35 and all(t["ms_per_step"] > 0 for t in trials)
+        assert {(t["variant"] >> 3) & 3 for t in trials} == {0, 1, 2}
         assert {t["rebuild_every"] for t in trials} == {0, 5, 10}
         assert any(t["variant"] & 32 for t in trials)
         assert s.thermo()["step"] == step0
