@@ -511,6 +511,8 @@ def main():
     ap.add_argument("--config", default="rbc4m", choices=["rbc4m"] + sorted(CONFIGS),
                     help="workload: rbc4m (default, the headline line), lattice32k, nh4m, vesicles96, ensemble8")
     ap.add_argument("--check-every", type=int, default=1000, help="nh4m: steps between FP64 comparisons")
+    ap.add_argument("--host-direct", type=int, default=1, choices=[0, 1],
+                    help="e2e: 1 = in-place host transfers where the arrays are reachable, 0 = staged copies")
     args = ap.parse_args()
     rank, ws = dist_setup()
     if args.impl == "reference":
@@ -533,7 +535,7 @@ def main():
 
     # ---- mixed precision, device-resident
     sim = make_sim(w, "mixed", skin=args.skin if args.skin is not None else SKIN, kernel_variant=args.form,
-                   rebuild_every=args.rebuild_every)
+                   rebuild_every=args.rebuild_every, host_direct=bool(args.host_direct))
     f_mixed, _, _ = sim.forces()
     tune = None
     if not args.no_autotune:
@@ -602,12 +604,38 @@ def main():
         for _ in range(e2e_steps):
             e2e_step()
         e2e_s = allreduce_max(time.perf_counter() - t0, ws)
+        # where an e2e step's time goes (a separate pass after the timed one)
+        ph = np.zeros(3)
+        for _ in range(20):
+            t1 = time.perf_counter()
+            N.check(L.orbc_gpu_set_state_f32(sim.h, 0, n, 3, *[h.ctypes.data for h in host]), sim.h)
+            t2 = time.perf_counter()
+            N.check(L.orbc_gpu_step(sim.h, 1, None), sim.h)
+            t3 = time.perf_counter()
+            N.check(L.orbc_gpu_download_f32(sim.h, 0, n, 3, *[h.ctypes.data for h in host]), sim.h)
+            ph += [t2 - t1, t3 - t2, time.perf_counter() - t3]
         e2e = {"value": ws * n * e2e_steps / e2e_s, "unit": "particle-steps/s",
                "h2d_bytes_per_step": 4 * 3 * 4 * n, "d2h_bytes_per_step": 4 * 3 * 4 * n, "steps": e2e_steps,
+               "phases_ms": {"set_state_f32": 1e3 * ph[0] / 20, "step": 1e3 * ph[1] / 20,
+                             "download_f32": 1e3 * ph[2] / 20},
                "note": "per step: orbc_gpu_set_state_f32 (pinned H2D of the x, n, v, o float containers; the "
                        "list is rebuilt only when a particle moved more than skin/2) + "
                        "orbc_gpu_step(1) + orbc_gpu_download_f32 (D2H of x, n, v, o)"}
-        log(f"e2e: {e2e['value']:.4e} particle-steps/s")
+        # the same through ordinary pageable arrays, as the reference's own
+        # containers are allocated (in place where the GPU reads host page tables)
+        pg = [np.array(h) for h in host]
+        for _ in range(3):
+            N.check(L.orbc_gpu_set_state_f32(sim.h, 0, n, 3, *[h.ctypes.data for h in pg]), sim.h)
+            N.check(L.orbc_gpu_step(sim.h, 1, None), sim.h)
+            N.check(L.orbc_gpu_download_f32(sim.h, 0, n, 3, *[h.ctypes.data for h in pg]), sim.h)
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            N.check(L.orbc_gpu_set_state_f32(sim.h, 0, n, 3, *[h.ctypes.data for h in pg]), sim.h)
+            N.check(L.orbc_gpu_step(sim.h, 1, None), sim.h)
+            N.check(L.orbc_gpu_download_f32(sim.h, 0, n, 3, *[h.ctypes.data for h in pg]), sim.h)
+        e2e["pageable_value"] = n * e2e_steps / (time.perf_counter() - t0)
+        log(f"e2e: {e2e['value']:.4e} particle-steps/s (pageable containers {e2e['pageable_value']:.4e}); "
+            f"phases {e2e['phases_ms']}")
 
     peak, peak_kind = measured_peaks()
     kt = prof["step_kernel_ms"]

@@ -777,14 +777,12 @@ template<class R> void launch_rebuild(const KArgs<R> &a, cudaStream_t st, bool g
  * type TH per particle (AoS; FP64 vectors of 3, or the reference's own `real`
  * = float vectors of 3, or of 4 under its _VEC4 layout). */
 template<class R, class TH>
-__global__ void k_set_state(KArgs<R> a, const TH *x, const TH *nv, const TH *v, const TH *o, int64_t k0, int64_t k1,
-                            int64_t first, int stride) {
+__device__ __forceinline__ void set_one(const KArgs<R> &a, int cur, int lp, int64_t k, const TH *x, const TH *nv,
+                                        const TH *v, const TH *o, int &out, int &moved) {
     using T4 = typename Vec<R>::T4;
-    const int cur = __ldcg(&a.S->cur), lp = __ldcg(&a.S->lp);
-    int out = 0, moved = 0;
-    for (int64_t k = k0 + blockIdx.x * int64_t(blockDim.x) + threadIdx.x; k < k1; k += int64_t(gridDim.x) * blockDim.x) {
+    {
         const int p = a.slot_of_home[k];
-        const int64_t hk = (k - first) * stride;
+        const int hk = 0;
         const SysDev &sd = a.sys[a.blk_sys[p / SYS_PAD]];
         T4 q = a.pos[cur][p];
         // A particle still within skin/2 of where the list was built keeps its
@@ -856,6 +854,70 @@ __global__ void k_set_state(KArgs<R> a, const TH *x, const TH *nv, const TH *v, 
         t.z = R(o[hk + 2]);
         a.omg[lp][p] = t;
     }
+}
+
+template<class R, class TH>
+__global__ void k_set_state(KArgs<R> a, const TH *x, const TH *nv, const TH *v, const TH *o, int64_t k0, int64_t k1,
+                            int64_t first, int stride) {
+    const int cur = __ldcg(&a.S->cur), lp = __ldcg(&a.S->lp);
+    int out = 0, moved = 0;
+    for (int64_t k = k0 + blockIdx.x * int64_t(blockDim.x) + threadIdx.x; k < k1; k += int64_t(gridDim.x) * blockDim.x) {
+        const int64_t hk = (k - first) * stride;
+        set_one<R, TH>(a, cur, lp, k, x + hk, nv + hk, v + hk, o + hk, out, moved);
+    }
+    if (out) atomicOr(&a.S->error, ERRB_GRID);
+    if (__syncthreads_or(moved) && threadIdx.x == 0) a.S->rebuild = 1;
+}
+
+/* In-place transfers over the host link (the caller's arrays are reachable
+ * from the GPU).  Host memory gives full link bandwidth only to wide, fully
+ * coalesced accesses, so each block moves a tile of HOST_TILE particles of
+ * each array through shared memory with 16-byte loads or stores (a base that
+ * is not 16-byte aligned falls back to contiguous scalar accesses), and the
+ * per-particle conversion works on the staged tile. */
+constexpr int HOST_TILE = 256;
+template<class TH> __device__ __forceinline__ void tile_in(TH *dst, const TH *src, int nvals) {
+    const uintptr_t addr = reinterpret_cast<uintptr_t>(src);
+    if ((addr & 15u) == 0) {
+        const int nv4 = int(nvals * sizeof(TH) / 16);
+        const int4 *s4 = reinterpret_cast<const int4 *>(src);
+        int4 *d4 = reinterpret_cast<int4 *>(dst);
+        for (int t = threadIdx.x; t < nv4; t += blockDim.x) d4[t] = s4[t];
+        for (int t = nv4 * int(16 / sizeof(TH)) + threadIdx.x; t < nvals; t += blockDim.x) dst[t] = src[t];
+    } else {
+        for (int t = threadIdx.x; t < nvals; t += blockDim.x) dst[t] = src[t];
+    }
+}
+template<class TH> __device__ __forceinline__ void tile_out(TH *dst, const TH *src, int nvals) {
+    const uintptr_t addr = reinterpret_cast<uintptr_t>(dst);
+    if ((addr & 15u) == 0) {
+        const int nv4 = int(nvals * sizeof(TH) / 16);
+        const int4 *s4 = reinterpret_cast<const int4 *>(src);
+        int4 *d4 = reinterpret_cast<int4 *>(dst);
+        for (int t = threadIdx.x; t < nv4; t += blockDim.x) d4[t] = s4[t];
+        for (int t = nv4 * int(16 / sizeof(TH)) + threadIdx.x; t < nvals; t += blockDim.x) dst[t] = src[t];
+    } else {
+        for (int t = threadIdx.x; t < nvals; t += blockDim.x) dst[t] = src[t];
+    }
+}
+
+template<class R, class TH>
+__global__ void __launch_bounds__(HOST_TILE) k_set_state_host(KArgs<R> a, const TH *x, const TH *nv, const TH *v,
+                                                              const TH *o, int64_t k0, int64_t k1, int64_t first,
+                                                              int stride) {
+    __shared__ __align__(16) TH buf[4][HOST_TILE * 4];
+    const int cur = __ldcg(&a.S->cur), lp = __ldcg(&a.S->lp);
+    const int64_t kb = k0 + int64_t(blockIdx.x) * HOST_TILE;
+    const int m = int(k1 - kb < HOST_TILE ? k1 - kb : HOST_TILE);
+    const TH *src[4] = {x, nv, v, o};
+    for (int q = 0; q < 4; ++q) tile_in<TH>(buf[q], src[q] + (kb - first) * stride, m * stride);
+    __syncthreads();
+    int out = 0, moved = 0;
+    const int t = threadIdx.x;
+    if (t < m) {
+        const int hk = t * stride;
+        set_one<R, TH>(a, cur, lp, kb + t, buf[0] + hk, buf[1] + hk, buf[2] + hk, buf[3] + hk, out, moved);
+    }
     if (out) atomicOr(&a.S->error, ERRB_GRID);
     if (__syncthreads_or(moved) && threadIdx.x == 0) a.S->rebuild = 1;
 }
@@ -865,6 +927,12 @@ void launch_set_state(const KArgs<R> &a, const TH *x, const TH *n, const TH *v, 
                       int64_t first, int stride, cudaStream_t st) {
     k_set_state<R, TH><<<grid_for(k1 - k0), 256, 0, st>>>(a, x, n, v, o, k0, k1, first, stride);
 }
+template<class R, class TH>
+void launch_set_state_host(const KArgs<R> &a, const TH *x, const TH *n, const TH *v, const TH *o, int64_t k0,
+                           int64_t k1, int64_t first, int stride, cudaStream_t st) {
+    const int64_t nb = (k1 - k0 + HOST_TILE - 1) / HOST_TILE;
+    if (nb > 0) k_set_state_host<R, TH><<<int(nb), HOST_TILE, 0, st>>>(a, x, n, v, o, k0, k1, first, stride);
+}
 
 /* Device state -> caller-order AoS vectors of TH for upload indices [h0, h1),
  * written from upload index `first` on with `stride` values per particle (a
@@ -872,13 +940,11 @@ void launch_set_state(const KArgs<R> &a, const TH *x, const TH *n, const TH *v, 
  * index (the slot comes from slot_of_home), so the writes -- the side that
  * streams to the host -- are coalesced; the slot-side reads are gathers. */
 template<class R, class TH>
-__global__ void k_download(KArgs<R> a, int64_t h0, int64_t h1, int64_t first, int stride, TH *x, TH *nv, TH *v,
-                           TH *o, TH *f, TH *t, double *e) {
+__device__ __forceinline__ void get_one(const KArgs<R> &a, int cur, int lp, int64_t h, int64_t hk, int stride, TH *x,
+                                        TH *nv, TH *v, TH *o, TH *f, TH *t, double *e) {
     using T4 = typename Vec<R>::T4;
-    const int cur = __ldcg(&a.S->cur), lp = __ldcg(&a.S->lp);
-    for (int64_t h = h0 + blockIdx.x * int64_t(blockDim.x) + threadIdx.x; h < h1; h += int64_t(gridDim.x) * blockDim.x) {
+    {
         const int p = a.slot_of_home[h];
-        const int64_t hk = (h - first) * stride;
         const SysDev &sd = a.sys[a.blk_sys[p / SYS_PAD]];
         if (x) {
             const T4 q = a.pos[cur][p];
@@ -906,9 +972,42 @@ __global__ void k_download(KArgs<R> a, int64_t h0, int64_t h1, int64_t first, in
 }
 
 template<class R, class TH>
+__global__ void k_download(KArgs<R> a, int64_t h0, int64_t h1, int64_t first, int stride, TH *x, TH *nv, TH *v,
+                           TH *o, TH *f, TH *t, double *e) {
+    const int cur = __ldcg(&a.S->cur), lp = __ldcg(&a.S->lp);
+    for (int64_t h = h0 + blockIdx.x * int64_t(blockDim.x) + threadIdx.x; h < h1; h += int64_t(gridDim.x) * blockDim.x)
+        get_one<R, TH>(a, cur, lp, h, (h - first) * stride, stride, x, nv, v, o, f, t, e);
+}
+
+/* In-place download: the tile's values are formed in shared memory, then
+ * each array's tile is written to the host with 16-byte stores. */
+template<class R, class TH>
+__global__ void __launch_bounds__(HOST_TILE) k_download_host(KArgs<R> a, int64_t h0, int64_t h1, int64_t first,
+                                                             int stride, TH *x, TH *nv, TH *v, TH *o) {
+    __shared__ __align__(16) TH buf[4][HOST_TILE * 4];
+    const int cur = __ldcg(&a.S->cur), lp = __ldcg(&a.S->lp);
+    const int64_t hb = h0 + int64_t(blockIdx.x) * HOST_TILE;
+    const int m = int(h1 - hb < HOST_TILE ? h1 - hb : HOST_TILE);
+    TH *dst[4] = {x, nv, v, o};
+    const int t = threadIdx.x;
+    if (t < m)
+        get_one<R, TH>(a, cur, lp, hb + t, int64_t(t) * stride, stride, x ? buf[0] : nullptr, nv ? buf[1] : nullptr,
+                       v ? buf[2] : nullptr, o ? buf[3] : nullptr, nullptr, nullptr, nullptr);
+    __syncthreads();
+    for (int q = 0; q < 4; ++q)
+        if (dst[q]) tile_out<TH>(dst[q] + (hb - first) * stride, buf[q], m * stride);
+}
+
+template<class R, class TH>
 void launch_download(const KArgs<R> &a, int64_t h0, int64_t h1, int64_t first, int stride, TH *x, TH *n, TH *v, TH *o,
                      TH *f, TH *t, double *e, cudaStream_t st) {
     k_download<R, TH><<<grid_for(h1 - h0), 256, 0, st>>>(a, h0, h1, first, stride, x, n, v, o, f, t, e);
+}
+template<class R, class TH>
+void launch_download_host(const KArgs<R> &a, int64_t h0, int64_t h1, int64_t first, int stride, TH *x, TH *n, TH *v,
+                          TH *o, cudaStream_t st) {
+    const int64_t nb = (h1 - h0 + HOST_TILE - 1) / HOST_TILE;
+    if (nb > 0) k_download_host<R, TH><<<int(nb), HOST_TILE, 0, st>>>(a, h0, h1, first, stride, x, n, v, o);
 }
 template<class R> void launch_download(const KArgs<R> &a, int64_t h0, int64_t h1, double *x, double *n, double *v,
                                        double *o, double *f, double *t, double *e, cudaStream_t st) {
@@ -952,7 +1051,11 @@ template void launch_rebuild<double>(const KArgs<double> &, cudaStream_t, bool);
     template void launch_set_state<R, TH>(const KArgs<R> &, const TH *, const TH *, const TH *, const TH *, int64_t, \
                                           int64_t, int64_t, int, cudaStream_t);                                      \
     template void launch_download<R, TH>(const KArgs<R> &, int64_t, int64_t, int64_t, int, TH *, TH *, TH *, TH *,    \
-                                         TH *, TH *, double *, cudaStream_t);
+                                         TH *, TH *, double *, cudaStream_t);                                          \
+    template void launch_set_state_host<R, TH>(const KArgs<R> &, const TH *, const TH *, const TH *, const TH *,     \
+                                               int64_t, int64_t, int64_t, int, cudaStream_t);                           \
+    template void launch_download_host<R, TH>(const KArgs<R> &, int64_t, int64_t, int64_t, int, TH *, TH *, TH *,    \
+                                              TH *, cudaStream_t);
 ORBC_IO_INST(float, float)
 ORBC_IO_INST(float, double)
 ORBC_IO_INST(double, float)

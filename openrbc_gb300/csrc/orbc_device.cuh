@@ -255,6 +255,13 @@ void launch_set_state(const KArgs<R> &a, const TH *x, const TH *n, const TH *v, 
 template<class R, class TH>
 void launch_download(const KArgs<R> &a, int64_t h0, int64_t h1, int64_t first, int stride, TH *x, TH *n, TH *v, TH *o,
                      TH *f, TH *t, double *e, cudaStream_t st);
+// the same two transfers reading / writing host arrays the GPU can reach, in tiles
+template<class R, class TH>
+void launch_set_state_host(const KArgs<R> &a, const TH *x, const TH *n, const TH *v, const TH *o, int64_t k0,
+                           int64_t k1, int64_t first, int stride, cudaStream_t st);
+template<class R, class TH>
+void launch_download_host(const KArgs<R> &a, int64_t h0, int64_t h1, int64_t first, int stride, TH *x, TH *n, TH *v,
+                          TH *o, cudaStream_t st);
 // full-size FP64 vectors of 3 (first = 0, stride = 3)
 template<class R> void launch_download(const KArgs<R> &a, int64_t h0, int64_t h1, double *x, double *n, double *v,
                                        double *o, double *f, double *t, double *e, cudaStream_t st);

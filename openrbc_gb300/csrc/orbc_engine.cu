@@ -715,7 +715,7 @@ template<class R> class Engine : public EngineBase {
     int set_state_t(int64_t first, int64_t count, int stride, const TH *x, const TH *n, const TH *v, const TH *o) {
         if (host_reachable(x) && host_reachable(n) && host_reachable(v) && host_reachable(o)) {
             // one pass over the host link: the conversion kernel reads the caller's arrays
-            launch_set_state<R, TH>(a, x, n, v, o, first, first + count, first, stride, st);
+            launch_set_state_host<R, TH>(a, x, n, v, o, first, first + count, first, stride, st);
             vcom_valid = !lite();
             if (vcom_valid) launch_vcom<R>(a, st);
             CK(cudaGetLastError());
@@ -1288,7 +1288,7 @@ template<class R> class Engine : public EngineBase {
         if ((x || n || v || o) && (!x || host_reachable(x)) && (!n || host_reachable(n)) &&
             (!v || host_reachable(v)) && (!o || host_reachable(o))) {
             // the conversion kernel writes the caller's arrays over the host link
-            launch_download<R, TH>(a, first, first + count, first, stride, x, n, v, o, nullptr, nullptr, nullptr, st);
+            launch_download_host<R, TH>(a, first, first + count, first, stride, x, n, v, o, st);
             CK(cudaGetLastError());
             CK(cudaStreamSynchronize(st));
             ++direct_transfers;
