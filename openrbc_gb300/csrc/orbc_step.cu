@@ -350,26 +350,25 @@ __device__ __forceinline__ void particle_forces(const KArgs<R> &a, const FFDev<R
     };
     if (V & FORM_MERGED) {
         /* shell rows first, distance only: row k's hit is bit k of hm (rows
-         * beyond 64 are evaluated on the spot, after the merged pass, as
+         * beyond 32 are evaluated on the spot, after the merged pass, as
          * without this form) */
-        uint64_t hm = 0;
-        const int nq = min(nout, 64);
+        uint32_t hm = 0;
+        const int nq = min(nout, 32);
         for (int k = 0; k < nq; ++k) {
             uint32_t ent;
             T4 pj;
-            if (shell_hit(k, ent, pj)) hm |= uint64_t(1) << k;
+            if (shell_hit(k, ent, pj)) hm |= 1u << k;
         }
         // inner rows, then the shell hits in row order, in one loop
-        const int total = nin + __popcll(hm);
-        auto entry = [&](int k, uint64_t &m) -> uint32_t {
+        const int total = nin + __popc(hm);
+        auto entry = [&](int k) -> uint32_t {
             if (k < nin) return __ldcs(nb + int64_t(k) * stride);
-            const int b = __ffsll((long long)m) - 1;
-            m &= m - 1;
+            const int b = __ffs(hm) - 1;
+            hm &= hm - 1u;
             return __ldcs(shell - int64_t(b) * stride);
         };
-        uint64_t mq = hm;
-        uint32_t e1 = total > 0 ? entry(0, mq) : 0u;
-        uint32_t e2 = total > 1 ? entry(1, mq) : 0u;
+        uint32_t e1 = total > 0 ? entry(0) : 0u;
+        uint32_t e2 = total > 1 ? entry(1) : 0u;
         T4 pn, nn;
         if (total > 0) {
             pn = ldg4<R>(pos + int(e1 & NB_MASK));
@@ -379,14 +378,14 @@ __device__ __forceinline__ void particle_forces(const KArgs<R> &a, const FFDev<R
             const uint32_t ent = e1;
             const T4 pj = pn, nj = nn;
             e1 = e2;
-            if (k + 2 < total) e2 = entry(k + 2, mq);
+            if (k + 2 < total) e2 = entry(k + 2);
             if (k + 1 < total) {
                 pn = ldg4<R>(pos + int(e1 & NB_MASK));
                 nn = ldg4<R>(nrm + int(e1 & NB_MASK));
             }
             pair(ent, pj, nj);
         }
-        for (int k = 64; k < nout; ++k) {
+        for (int k = 32; k < nout; ++k) {
             uint32_t ent;
             T4 pj;
             if (shell_hit(k, ent, pj)) pair(ent, pj, ldg4<R>(nrm + int(ent & NB_MASK)));
@@ -787,7 +786,8 @@ __global__ void __launch_bounds__(LITE_BS, fp_blocks<R>(20)) k_step_langevin(KAr
  * k_advance flips the buffers after the kernel.  The temperature is reduced on
  * demand (k_vcom). */
 template<class R, int V>
-__global__ void __launch_bounds__(LITE_BS, fp_blocks<R>((V & 4) ? 20 : 16)) k_step_langevin_lite(KArgs<R> a) {
+__global__ void __launch_bounds__(LITE_BS, fp_blocks<R>((V & 4) ? ((V & FORM_MERGED) ? 18 : 20) : 16))
+    k_step_langevin_lite(KArgs<R> a) {
     if (halted(a.S)) return;
     using T4 = typename Vec<R>::T4;
     __shared__ T4 sh[27];
