@@ -87,8 +87,9 @@ typedef struct {
     /* kernel forms 0..127 (bits 3 and 4 not both set): bit 0 =
        software-pipelined neighbour pass (else 2-way unrolled), bit 1 =
        non-lipid pair path inlined (else called), bit 2 = Langevin step kernel
-       compiled for 20 resident blocks per SM (48 registers; else 16 blocks,
-       64 registers), bits 3-4 = how the neighbour list is built: 0 per cell
+       compiled for more resident blocks per SM (20 blocks at 48 registers,
+       18 at 56 with bit 5; else 16 blocks at 64 registers), bits 3-4 = how
+       the neighbour list is built: 0 per cell
        of a warp, 32 candidates at a time, entries placed by prefix count;
        1 per-particle 27-cell sweeps; 2 per warp in two phases (accept masks
        per particle, then every lane writes its own column) -- all three

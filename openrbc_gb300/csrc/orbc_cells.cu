@@ -543,14 +543,19 @@ template<class R> __global__ void __launch_bounds__(128) k_nlist(KArgs<R> a, int
 /* Form 2 of the list build (two phases per warp).  The distinct cells of a
  * warp's particles are fetched as in form 0 -- 27 lanes fetch a cell's
  * neighbour ranges -- and each cell's candidates are staged pre-shifted into
- * that cell's frame.  Phase 1: for each particle of the cell the warp tests
- * 32 candidates per ballot, branch-free, and the particle's own lane keeps
- * the accept masks (in range at all / inside the interaction range) in
- * registers.  The candidates' list entries stay staged in shared memory for
- * as many cells as fit, so that phase 2 -- every lane expands its masks in
- * candidate order into its own column -- runs for most warps once, with all
- * their lanes.  The candidates, their order and the arithmetic are those of
- * forms 0 and 1, so all three forms write the same rows. */
+ * that cell's frame, padded with ghosts (never accepted) to a multiple of
+ * 32.  Phase 1: for two particles of the cell at a time the warp tests 32
+ * candidates per ballot pair, branch-free (one staged load serves both
+ * particles), and each particle's own lane keeps the accept masks (in range
+ * at all / inside the interaction range) in registers.  The candidates' list
+ * entries stay staged in shared memory for as many cells as fit, so that
+ * phase 2 -- every lane expands its masks in candidate order into its own
+ * column -- runs for most warps once, with all their lanes.  The candidates,
+ * their order and the arithmetic are those of forms 0 and 1, so all three
+ * forms write the same rows. */
+template<class R> __device__ __forceinline__ R ghost_w_of();  // the w word of a ghost's position
+template<> __device__ __forceinline__ float ghost_w_of<float>() { return __int_as_float(GHOST); }
+template<> __device__ __forceinline__ double ghost_w_of<double>() { return __longlong_as_double((long long)GHOST); }
 // 7 resident blocks per SM: the staging below (about 31 KB per block in FP32)
 // and at most 72 registers; more warps in flight beat fewer passes per warp
 template<class R> __global__ void __launch_bounds__(128, 7) k_nlist2(KArgs<R> a, int gated) {
@@ -596,6 +601,7 @@ template<class R> __global__ void __launch_bounds__(128, 7) k_nlist2(KArgs<R> a,
     T4 *sp = s_pos[warp];
     uint32_t *se = s_ent[warp];
     uint32_t *col = a.nbr + nbr_index(i, 0, a.cap);  // row k of slot i at col[32 k]
+    const R ghost_w = ghost_w_of<R>();
     const int cap = a.cap;
     int qin = 0, qout = 0, qtot = 0;
     // neighbour ranges of cell kd -> off/beg; returns the candidate count
@@ -641,34 +647,57 @@ template<class R> __global__ void __launch_bounds__(128, 7) k_nlist2(KArgs<R> a,
             sp[t] = shifted(a.pos[cur][j], l % 3 - 1, (l / 3) % 3 - 1, l / 9 - 1);
             se[ebase + t] = uint32_t(j) | (uint32_t(l) << NB_SHIFT);
         }
+        if (nch + lane < ((nch + 31) & ~31)) {  // ghosts up to a multiple of 32: never accepted
+            T4 z;
+            z.x = z.y = z.z = R(0);
+            z.w = ghost_w;
+            sp[nch + lane] = z;
+        }
         __syncwarp();
     };
     uint32_t macc[MB], minn[MB];
-    // phase 1 for the particles grp over the staged candidates [0, nch), nch <= REG;
+    // phase 1 for the particles grp, two per pass, over the staged candidates [0, nch), nch <= REG;
     // ts: the owning lane's own staged index (self is not a neighbour), -1 if absent
     auto phase1 = [&](unsigned grp, int nch, int ts) {
-        for (unsigned g = grp; g; g &= g - 1u) {
+        for (unsigned g = grp; g;) {
             const int il = __ffs(g) - 1;
-            T4 pi = p;
+            g &= g - 1u;
+            const int il2 = g ? __ffs(g) - 1 : il;  // the second particle of the pass (il again if none)
+            if (g) g &= g - 1u;
+            T4 pi = p, pi2 = p;
             pi.x = __shfl_sync(0xffffffffu, p.x, il);
             pi.y = __shfl_sync(0xffffffffu, p.y, il);
             pi.z = __shfl_sync(0xffffffffu, p.z, il);
+            pi2.x = __shfl_sync(0xffffffffu, p.x, il2);
+            pi2.y = __shfl_sync(0xffffffffu, p.y, il2);
+            pi2.z = __shfl_sync(0xffffffffu, p.z, il2);
             const int ti = __shfl_sync(0xffffffffu, ty, il) * 16;
             const int tsi = __shfl_sync(0xffffffffu, ts, il);
+            const int ti2 = __shfl_sync(0xffffffffu, ty, il2) * 16;
+            const int tsi2 = __shfl_sync(0xffffffffu, ts, il2);
 #pragma unroll
             for (int b = 0; b < MB; ++b) {
                 if (b * 32 < nch) {
                     const int t = b * 32 + lane;
-                    const bool valid = t < nch;
-                    const T4 q = sp[valid ? t : 0];
-                    const float2 cut = s_cut[ti + w_type(wbits(q.w))];
+                    const T4 q = sp[t];
+                    const int tj = w_type(wbits(q.w));
+                    const float2 cut = s_cut[ti + tj];
+                    const float2 cut2 = s_cut[ti2 + tj];
                     const R r2 = dist2(pi, q);
-                    const bool acc = valid && t != tsi && cut.x > 0.f && r2 < R(cut.x);
+                    const R r2b = dist2(pi2, q);
+                    const bool acc = t != tsi && r2 < R(cut.x);
+                    const bool acc2 = t != tsi2 && r2b < R(cut2.x);
                     const unsigned ma = __ballot_sync(0xffffffffu, acc);
                     const unsigned mi = __ballot_sync(0xffffffffu, acc && r2 < R(cut.y));
+                    const unsigned ma2 = __ballot_sync(0xffffffffu, acc2);
+                    const unsigned mi2 = __ballot_sync(0xffffffffu, acc2 && r2b < R(cut2.y));
                     if (lane == il) {
                         macc[b] = ma;
                         minn[b] = mi;
+                    }
+                    if (lane == il2) {
+                        macc[b] = ma2;
+                        minn[b] = mi2;
                     }
                 }
             }

@@ -264,8 +264,12 @@ template<class R> constexpr int fp_blocks(int n) { return sizeof(R) == 4 ? n : n
  *   32 merged shell pass: the skin-shell rows are only distance-tested, each
  *      lane records its hits in a bit mask, and the hits are evaluated in the
  *      same loop as the inner rows, so a shell row that one lane of a warp
- *      hits no longer costs the whole warp a pair evaluation.  The pairs are
- *      added in the same order as without it: the results are bit-identical;
+ *      hits no longer costs the whole warp a pair evaluation; and where a
+ *      lane's pair involves a protein, all lanes of the warp evaluate their
+ *      lipid-lipid and lipid-protein pairs in one anisotropic code path with
+ *      per-pair parameters instead of two paths one after the other.  The
+ *      pairs are added in the same order as without it: the results are
+ *      bit-identical;
  *   64 compensated accumulation: each particle's force and torque are summed
  *      with Kahan compensation (the rounding error of each running sum is
  *      carried into the next addition), for the FP32 form. */
@@ -325,6 +329,22 @@ __device__ __forceinline__ void particle_forces(const KArgs<R> &a, const FFDev<R
                 pair_general<R, E, (V & FORM_INLINE) != 0>(F.pair[ty * NT + tj], dx, dy, dz, r2, ni.x, ni.y, ni.z,
                                                            nj.x, nj.y, nj.z, df, dt, e);
                 accumulate(df, dt);
+            }
+        } else if ((V & FORM_MERGED) && !__all_sync(__activemask(), (ty | tj) == 0)) {
+            /* Some lane of the warp has a protein in this pair: every lipid-lipid
+             * and lipid-protein pair of the warp goes through the same
+             * anisotropic code with its own parameters (row ty | tj of the
+             * table: the protein's type, 0 for two lipids), so that the
+             * protein's lane does not run after the lipids' lanes.  The
+             * parameters are those of the other branches: the results are
+             * the same bit for bit. */
+            if ((ty == 0 || tj == 0) && F.pair[ty | tj].kind == PAIR_ANISO) {
+                const PairP<R> &P = F.pair[ty | tj];
+                if (r2 < P.cutsq && r2 > R(1e-5))
+                    aniso<R, E>(P, dx, dy, dz, r2, ni.x, ni.y, ni.z, nj.x, nj.y, nj.z, f, t, e);
+            } else {
+                pair_general<R, E, (V & FORM_INLINE) != 0>(F.pair[ty * NT + tj], dx, dy, dz, r2, ni.x, ni.y, ni.z,
+                                                           nj.x, nj.y, nj.z, f, t, e);
             }
         } else if ((ty | tj) == 0) {
             if (r2 < ll_cutsq && r2 > R(1e-5))
