@@ -320,7 +320,16 @@ __device__ __forceinline__ void particle_forces(const KArgs<R> &a, const FFDev<R
         const int tj = w_type(wbits(pj.w));
         if (KAHAN) {
             R3<R> df = {0, 0, 0}, dt = {0, 0, 0};
-            if ((ty | tj) == 0) {
+            if ((V & FORM_MERGED) && !__all_sync(__activemask(), (ty | tj) == 0) && (ty == 0 || tj == 0) &&
+                F.pair[ty | tj].kind == PAIR_ANISO) {
+                // one anisotropic path for the warp, as in the uncompensated form
+                // below; a lipid-lipid pair is added only inside its range, a
+                // protein pair always (as the general path does)
+                const PairP<R> &P = F.pair[ty | tj];
+                const bool inr = r2 < P.cutsq && r2 > R(1e-5);
+                if (inr) aniso<R, E>(P, dx, dy, dz, r2, ni.x, ni.y, ni.z, nj.x, nj.y, nj.z, df, dt, e);
+                if (inr || (ty | tj) != 0) accumulate(df, dt);
+            } else if ((ty | tj) == 0) {
                 if (r2 < ll_cutsq && r2 > R(1e-5)) {
                     aniso<R, E>(a.ll, dx, dy, dz, r2, ni.x, ni.y, ni.z, nj.x, nj.y, nj.z, df, dt, e);
                     accumulate(df, dt);
@@ -915,9 +924,13 @@ __global__ void __launch_bounds__(LITE_BS, fp_blocks<R>((V & 2) ? 12 : 16))
 
 /* Nose-Hoover second half (post_toque_final_update, src/integrate_nh.h:237-273)
  * fused with the forces: the lite structure plus warp partials for the
- * kinetic-energy sum that k_reduce turns into the thermostat update. */
+ * kinetic-energy sum that k_reduce turns into the thermostat update.  The
+ * resident blocks asked for fall with the registers a form needs (20 blocks
+ * at 48 registers, 18 at 56 with the merged shell pass, 16 at 64 with
+ * compensated sums), so that those two forms do not spill. */
 template<class R, bool E, int V>
-__global__ void __launch_bounds__(LITE_BS, fp_blocks<R>(20)) k_nh_final(KArgs<R> a, int count_step) {
+__global__ void __launch_bounds__(LITE_BS, fp_blocks<R>((V & FORM_KAHAN) ? 16 : ((V & FORM_MERGED) ? 18 : 20)))
+    k_nh_final(KArgs<R> a, int count_step) {
     if (halted(a.S)) return;
     using T4 = typename Vec<R>::T4;
     __shared__ T4 sh[27];
