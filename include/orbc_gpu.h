@@ -89,13 +89,13 @@ typedef struct {
        non-lipid pair path inlined (else called), bit 2 = Langevin step kernel
        compiled for more resident blocks per SM (20 blocks at 48 registers,
        18 at 56 with bit 5; else 16 blocks at 64 registers), bits 3-4 = how
-       the neighbour list is built: 0 per cell
-       of a warp, 32 candidates at a time, entries placed by prefix count;
-       1 per-particle 27-cell sweeps; 2 per warp in two phases (accept masks
-       per particle, then every lane writes its own column) -- all three
-       write the same list; bit 5 (32) = merged shell pass: skin-shell rows
-       are distance-tested first and their hits evaluated in the loop of the
-       inner rows (bit-identical results); bit 6 (64) = compensated (Kahan)
+       the neighbour list is built: 0 per cell of a warp, 32 candidates at a
+       time, entries placed by prefix count; 1
+       per-particle 27-cell sweeps; 2 per warp in two phases (accept masks per
+       particle, then every lane writes its own column) -- all three write the
+       same list; bit 5 (32) = merged shell pass: skin-shell rows are
+       distance-tested first and their hits evaluated in the loop of the inner
+       rows (bit-identical results); bit 6 (64) = compensated (Kahan)
        summation of each particle's force and torque, also in the forces
        hook.  Bits 5 and 6 imply bits 0 and 1.  orbc_gpu_autotune picks the
        forms per workload */

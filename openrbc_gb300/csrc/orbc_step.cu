@@ -784,9 +784,12 @@ __device__ __forceinline__ void langevin_particle(const KArgs<R> &a, const FFDev
 /* Langevin step with the per-system sums (energy, bulk-velocity removal):
  * the structure of the lite kernel below (small blocks, force-field table
  * through the read-only path) plus warp partials, summed per system by
- * k_reduce after the kernel. */
+ * k_reduce after the kernel.  Resident blocks as for k_nh_final (20, 18 with
+ * the merged shell pass, 16 with compensated sums): 0.82 against 0.92 ms per
+ * step with the merged pass on the 4.03M cell, where 20 blocks spilled. */
 template<class R, bool E, int V>
-__global__ void __launch_bounds__(LITE_BS, fp_blocks<R>(20)) k_step_langevin(KArgs<R> a) {
+__global__ void __launch_bounds__(LITE_BS, fp_blocks<R>((V & FORM_KAHAN) ? 16 : ((V & FORM_MERGED) ? 18 : 20)))
+    k_step_langevin(KArgs<R> a) {
     if (halted(a.S)) return;
     using T4 = typename Vec<R>::T4;
     __shared__ T4 sh[27];
