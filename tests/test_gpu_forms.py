@@ -59,6 +59,27 @@ def test_merged_shell_pass_is_bit_identical(precision, integrator, base):
     assert tha["zeta"] == thb["zeta"]
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("integrator", ["langevin", "nose-hoover"])
+@pytest.mark.parametrize("base", [3 | 16 | 64, 7 | 16 | 64])
+def test_merged_shell_pass_is_bit_identical_with_compensated_sums(precision, integrator, base):
+    """With compensated sums too: in the merged form a warp whose pairs involve
+    a protein (the cell's anchors) evaluates its lipid and protein pairs in one
+    path, and each pair must still enter the sums exactly as without it."""
+    from openrbc_gb300 import workloads
+    if precision == "fp64" and base & 4:
+        pytest.skip("the occupancy form is an FP32 form")
+    w = cell()
+    assert (w["type"] != 0).sum() > 100  # anchors in the cell
+    kw = dict(table=workloads.RBC_BOND_TABLE, faces=w["faces"], constraint=w["constraint"])
+    a, tha = run(w, precision, base, 40, integrator, **kw)
+    b, thb = run(w, precision, base | 32, 40, integrator, **kw)
+    assert tha["rebuilds"] >= 2
+    for u, v in zip(a, b):
+        assert np.array_equal(u, v)
+    assert tha["zeta"] == thb["zeta"]
+
+
 def test_merged_shell_pass_periodic_lattice_with_energy():
     from openrbc_gb300 import workloads
     w = workloads.lattice(n=6000, ncol=80, kT=1.0, seed=9)
