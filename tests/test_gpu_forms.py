@@ -143,5 +143,5 @@ def test_compensated_langevin_vs_oracle(form):
         s.upload(g["x"], g["nrm"], g["v"], g["o"], g["type"], g["tag"], g["bonds"])
         s.step(10)
         x, n, v, o = s.download()
-    assert rel_l2(x - g["x"], st.x - g["x"]) < 2e-3
-    assert rel_l2(v, st.v) < 2e-3
+    assert rel_l2(x - g["x"], st.x - g["x"]) < 2e-5
+    assert rel_l2(v, st.v) < 2e-5

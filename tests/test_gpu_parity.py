@@ -5,7 +5,8 @@ Tolerances (relative L2 over all particles unless stated):
   FP64 forces / torques vs reference FP64 ........ 1e-10
   mixed forces / torques vs reference FP64 ....... 1e-5  (the stated force-error bound)
   FP64 100-step noise-free trajectory ............ 1e-9
-  mixed trajectories ............................. 2e-3  (FP32 state, chaotic growth)
+  mixed trajectories, 10-100 steps ............... 2e-5 to 3e-5 (FP32 state; about 20 times
+                                                   the largest difference seen on a GB300)
 Integer / index work (neighbour sets, Morton keys and order) is bit-exact.
 """
 import numpy as np
@@ -74,8 +75,8 @@ def test_noise_free_langevin_mixed(name):
     with sim_for(g, "mixed", kBT=0.0, dt=float(g["lang_dt"]), eta=float(g["lang_eta"])) as s:
         s.step(int(g["lang_steps"]))
         x, n, v, o = s.download()
-    assert rel_l2(x - g["x"], g["lang_x"] - g["x"]) < 2e-3
-    assert rel_l2(v, g["lang_v"]) < 2e-3
+    assert rel_l2(x - g["x"], g["lang_x"] - g["x"]) < 3e-5
+    assert rel_l2(v, g["lang_v"]) < 3e-5
 
 
 @pytest.mark.parametrize("name", ["lattice_576.npz", "cell_ico12.npz"])
@@ -90,7 +91,7 @@ def test_nose_hoover_fp64(name):
     assert abs(th["zeta"] - float(g["nh_zeta"])) < 1e-8 * max(1.0, abs(float(g["nh_zeta"])))
 
 
-@pytest.mark.parametrize("precision,tol", [("fp64", 1e-9), ("mixed", 2e-3)])
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-9), ("mixed", 2e-5)])
 def test_langevin_with_noise_vs_oracle(precision, tol):
     """Same counter-based noise on both sides, kT = 1, 10 steps."""
     g = load_golden("cell_ico12.npz")
@@ -206,7 +207,7 @@ def test_config1_lattice_forces(precision, tol):
     assert abs(th["temperature"] - T_ref) < (1e-12 if precision == "fp64" else 1e-6) * T_ref
 
 
-@pytest.mark.parametrize("precision,tol", [("fp64", 1e-8), ("mixed", 2e-3)])
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-8), ("mixed", 3e-5)])
 def test_config1_lattice_noise_free_langevin(precision, tol):
     """100 noise-free Langevin steps of the 32,768-lipid lattice against the
     reference's FP64 trajectory (every fourth particle kept in the fixture)."""

@@ -7,7 +7,8 @@ Tolerances (relative L2):
   assign_temperature FP64 ............. 1e-12 (FP64 Box-Muller, libm vs CUDA log/sin/cos)
   assign_temperature mixed ............ 1e-7  (stored as FP32)
   zero-bulk Langevin / NH FP64 ........ 1e-9  (10 steps, same counter-based noise)
-  zero-bulk Langevin mixed ............ 2e-3  (FP32 state)
+  zero-bulk Langevin mixed ............ 2e-5  (FP32 state; about 20 times the largest
+                                         difference seen on a GB300)
 """
 import numpy as np
 import pytest
@@ -83,7 +84,7 @@ def test_assign_temperature_is_order_independent():
     assert np.array_equal(v1[perm], v2)
 
 
-@pytest.mark.parametrize("precision,tol", [("fp64", 1e-9), ("mixed", 2e-3)])
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-9), ("mixed", 2e-5)])
 def test_zero_bulk_langevin_matches_oracle(precision, tol):
     g = load_golden("cell_ico12.npz")
     v0 = g["v"] + np.array([0.3, -0.2, 0.1])   # give the lipids a bulk drift to remove
