@@ -95,7 +95,8 @@ def test_in_place_host_transfers_equal_staged_copies(precision):
     arrays in place when the GPU can reach them (mapped page-locked memory;
     pageable memory on GPUs that read the host's page tables): the states and
     downloads must equal those of the staged copies, for pageable numpy arrays
-    and page-locked ones, in FP32 (stride 3 and 4, index ranges) and FP64."""
+    and page-locked ones, in FP32 (stride 3 and 4, index ranges, one of them
+    starting off a 16-byte boundary) and FP64."""
     import torch
     from openrbc_gb300 import RTParameter, Simulation
     g = load_golden("cell_ico12.npz")
@@ -114,7 +115,7 @@ def test_in_place_host_transfers_equal_staged_copies(precision):
             with Simulation(p, box=REF_BOX, host_direct=direct) as s:
                 s.upload(g["x"], g["nrm"], g["v"], g["o"], g["type"], g["tag"], g.get("bonds"))
                 s.step(2)
-                a = 1000
+                a = 1001  # x[a:] starts 12 bytes past a 16-byte boundary: the unaligned path
                 s.set_state_f32(*[conv(q[a:]) for q in (x, nv, v, o)], first=a)
                 s.set_state_f32(*[conv(q[:a]) for q in (x, nv, v, o)], first=0)
                 s.step(4)
