@@ -547,6 +547,10 @@ def main():
             f"{best['ms_per_step']:.4f} ms/step "
             f"({len(trials)} trials, {tune['seconds']:.1f} s)")
     sim.step(args.warmup)
+    # the state the timed steps start from: the profiled pass and the end-to-end
+    # passes restart from it, so that every figure covers the same stretch of
+    # the run (at kT = 1 the lipid film thins out as a run goes on)
+    snap = sim.download()
     barrier(ws)
     th0 = sim.thermo()
     with ClockSampler() as clk:
@@ -558,6 +562,7 @@ def main():
         f"rebuilds {th['rebuilds'] - th0['rebuilds']}, T = {th['temperature']:.4f}")
 
     # ---- dominant kernel timing (profiled pass: CUDA events around each launch group)
+    sim.set_state(*snap)
     prof = sim.profile(20)
     log(f"profile: {prof}")
 
@@ -588,7 +593,8 @@ def main():
         import torch
         # the reference's containers: AoS float vectors of 3 (src/config_static.h:34-44)
         host = [torch.empty((n, 3), dtype=torch.float32, pin_memory=True).numpy() for _ in range(4)]
-        for h, arr in zip(host, sim.download()):
+        sim.set_state(*snap)
+        for h, arr in zip(host, snap):
             h[:] = arr
         e2e_steps = max(100, args.steps)
 
@@ -623,7 +629,8 @@ def main():
                        "orbc_gpu_step(1) + orbc_gpu_download_f32 (D2H of x, n, v, o)"}
         # the same through ordinary pageable arrays, as the reference's own
         # containers are allocated (in place where the GPU reads host page tables)
-        pg = [np.array(h) for h in host]
+        sim.set_state(*snap)
+        pg = [np.array(a, dtype=np.float32) for a in snap]
         for _ in range(3):
             N.check(L.orbc_gpu_set_state_f32(sim.h, 0, n, 3, *[h.ctypes.data for h in pg]), sim.h)
             N.check(L.orbc_gpu_step(sim.h, 1, None), sim.h)
