@@ -80,6 +80,24 @@ def test_merged_shell_pass_is_bit_identical_with_compensated_sums(precision, int
     assert tha["zeta"] == thb["zeta"]
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("base", [3, 3 | 64])
+def test_merged_shell_pass_is_bit_identical_with_every_protein_type(precision, base):
+    """The reference's 3,544-particle cell: lipids and band-III, actin,
+    spectrin and glycophorin-type particles, so warps meet lipid-protein
+    anisotropic pairs, protein-protein repulsion and WCA pairs together; the
+    merged form's single anisotropic path must leave every sum as it was."""
+    g = load_golden("cell_ico12.npz")
+    assert len(set(g["type"].tolist())) >= 5
+    w = {"x": g["x"], "n": g["nrm"], "v": g["v"], "o": g["o"], "type": g["type"], "tag": g["tag"],
+         "bonds": g["bonds"]}
+    a, tha = run(w, precision, base, 30, skin=0.4)
+    b, thb = run(w, precision, base | 32, 30, skin=0.4)
+    assert tha["rebuilds"] >= 2
+    for u, v in zip(a, b):
+        assert np.array_equal(u, v)
+
+
 def test_merged_shell_pass_periodic_lattice_with_energy():
     from openrbc_gb300 import workloads
     w = workloads.lattice(n=6000, ncol=80, kT=1.0, seed=9)

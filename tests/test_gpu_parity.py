@@ -91,6 +91,19 @@ def test_nose_hoover_fp64(name):
     assert abs(th["zeta"] - float(g["nh_zeta"])) < 1e-8 * max(1.0, abs(float(g["nh_zeta"])))
 
 
+@pytest.mark.parametrize("name", ["lattice_576.npz", "cell_ico12.npz"])
+def test_nose_hoover_mixed(name):
+    """The mixed form along the reference's own Nose-Hoover trajectory."""
+    g = load_golden(name)
+    with sim_for(g, "mixed", integrator="nose-hoover", kBT=float(g["nh_kBT"]), dt=float(g["nh_dt"])) as s:
+        th = s.step(int(g["nh_steps"]))
+        x, n, v, o = s.download()
+    assert rel_l2(x - g["x"], g["nh_x"] - g["x"]) < 3e-5
+    assert rel_l2(v, g["nh_v"]) < 3e-5
+    assert rel_l2(o, g["nh_o"]) < 3e-5
+    assert abs(th["zeta"] - float(g["nh_zeta"])) < 3e-5 * max(1.0, abs(float(g["nh_zeta"])))
+
+
 @pytest.mark.parametrize("precision,tol", [("fp64", 1e-9), ("mixed", 2e-5)])
 def test_langevin_with_noise_vs_oracle(precision, tol):
     """Same counter-based noise on both sides, kT = 1, 10 steps."""
