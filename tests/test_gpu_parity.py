@@ -206,6 +206,26 @@ def test_example_large_patch_forces(precision, form, tol):
     assert rel_l2(t[c], g["t64"][c]) < tol, rel_l2(t[c], g["t64"][c])
 
 
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-9), ("mixed", 3e-5)])
+def test_example_large_patch_langevin_vs_oracle(precision, tol):
+    """Ten Langevin steps of the same patch at the reference's default kT =
+    0.22, against the oracle on the same input with the same counter-based
+    noise (bonds, every protein type of the whole cell, list rebuilds)."""
+    g = load_golden("example_large_patch.npz")
+    z = np.zeros_like(np.asarray(g["x"], np.float64))
+    st = orc.State(x=g["x"], nrm=g["nrm"], v=z, o=z, type=g["type"], tag=g["tag"], bonds=g["bonds"], kBT=0.22,
+                   dt=0.01, eta=0.01, seed=0xBAD5EED)
+    orc.langevin(st, 10)
+    gg = {"x": g["x"], "nrm": g["nrm"], "v": z, "o": z, "type": g["type"], "tag": g["tag"], "bonds": g["bonds"]}
+    with sim_for(gg, precision, kBT=0.22) as s:
+        th = s.step(10)
+        x, n, v, o = s.download()
+    assert th["rebuilds"] >= 1
+    assert rel_l2(x - g["x"], st.x - g["x"]) < tol
+    assert rel_l2(v, st.v) < tol
+    assert rel_l2(o, st.o) < 3 * tol  # angular velocities: the largest relative differences (6.4e-6 mixed)
+
+
 @pytest.mark.parametrize("precision,tol", [("fp64", 1e-10), ("mixed", 1e-5)])
 def test_config1_lattice_forces(precision, tol):
     """The plain small workload (32,768 lipids on the 182-column lattice)."""
