@@ -14,7 +14,9 @@ value      mixed-precision particle-steps/s, device time of K steps (inputs
 e2e        the same metric through the C ABI the reference host would call
            each step with its own containers (AoS vector<real,3>, real =
            float): orbc_gpu_set_state_f32 from pinned host buffers + one
-           orbc_gpu_step + orbc_gpu_download_f32 back to the host buffers.
+           orbc_gpu_step + orbc_gpu_download_f32 back to the host buffers,
+           restarted from the state the timed steps started from, so that
+           it covers the same stretch of the run as `value`.
 roofline   the fused step kernel: compulsory bytes (104 B per particle-step,
            mixed) / its CUDA-event time vs measured HBM bandwidth; the FP32
            ALU fraction of its algorithmic flops is reported beside it.
