@@ -54,6 +54,21 @@ def test_create_rejects_bad_params_without_exiting():
     assert b"invalid" in L.orbc_gpu_error(None)
 
 
+@pytest.mark.parametrize("field,value", [("kernel_variant", -1), ("kernel_variant", 128), ("kernel_variant", 24),
+                                         ("kernel_variant", 24 | 3), ("host_direct", 2), ("zero_bulk", -1)])
+def test_create_rejects_out_of_range_forms_and_switches(field, value):
+    """Kernel forms are 0..127 with list-build bits 3 and 4 not both set; the
+    switches are 0 or 1: anything else is an argument error, not a guess."""
+    from openrbc_gb300 import _native as N
+    L = N.lib()
+    p = N.Params()
+    L.orbc_gpu_default_params(C.byref(p))
+    setattr(p, field, value)
+    h = C.c_void_p()
+    assert L.orbc_gpu_create(C.byref(p), C.byref(h)) == 1 and not h.value
+    assert b"invalid" in L.orbc_gpu_error(None)
+
+
 def test_create_without_gpu_reports_nodev():
     import torch
     if torch.cuda.is_available():
